@@ -1,0 +1,205 @@
+/*
+ * tcgb300.h — C ABI of the GB300 statevector engine for TensorCircuit's
+ * parameterized-circuit path.
+ *
+ * The engine replaces the tensor-network contraction that TensorCircuit runs
+ * for `Circuit.wavefunction()` / `expectation_ps()` / `sample()` and the
+ * taped autodiff behind `backend.vvag`.  Every entry point is stream ordered,
+ * takes plain device pointers owned by the caller (torch tensors on the Python
+ * side), and returns an int status (TCG_OK == 0).  No entry point exits,
+ * aborts or traps; device-side problems come back as a status.
+ *
+ * State layout (same as the reference): a circuit on n qubits is a complex64
+ * vector of 2^n amplitudes, qubit 0 is the MOST significant bit of the
+ * amplitude index (tensorcircuit/basecircuit.py:213-215 wires gate leg i to
+ * the i-th front edge; tests/test_circuit.py:21-44 pins
+ * `wavefunction()[2] == 8` for `unitary(0, 1, arange(16))`).  A batch of B
+ * circuits with the same structure is B such vectors back to back.
+ *
+ * Gate matrices follow the reference's `reshapem` convention
+ * (tensorcircuit/backends/abstract_backend.py:403-414): a k-qubit gate is a
+ * 2^k x 2^k row-major matrix M[out, in], and the first listed qubit is the
+ * most significant bit of the k-bit sub-index.
+ */
+#ifndef TCGB300_H
+#define TCGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------
+ * Mirrors the reference's error behaviour: duplicated qubits are an
+ * AssertionError there (tensorcircuit/basecircuit.py:143), measuring two
+ * operators on one index a ValueError (basecircuit.py:306-307), anything a
+ * backend lacks a NotImplementedError (backends/abstract_backend.py:914-928).
+ * The Python layer maps these codes back to those exception types. */
+enum {
+  TCG_OK = 0,
+  TCG_ERR_INVALID_ARG = 1,   /* bad size, null pointer, qubit out of range */
+  TCG_ERR_DUP_QUBIT = 2,     /* a gate lists the same qubit twice */
+  TCG_ERR_UNSUPPORTED = 3,   /* valid request this engine does not implement */
+  TCG_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+  TCG_ERR_SCRATCH = 5,       /* caller-provided scratch is too small */
+  TCG_ERR_OOM = 6            /* a host or device allocation failed */
+};
+
+/* ---- gate program --------------------------------------------------------- */
+enum {
+  TCG_GATE_DENSE = 0, /* 2^nq x 2^nq matrix, row-major M[out, in]          */
+  TCG_GATE_DIAG = 1   /* diagonal gate: 2^nq entries d[idx]                  */
+};
+
+#define TCG_MAX_GATE_QUBITS 6
+
+typedef struct tcg_gate {
+  int32_t kind;                         /* TCG_GATE_DENSE or TCG_GATE_DIAG   */
+  int32_t nq;                           /* 1 .. TCG_MAX_GATE_QUBITS          */
+  int32_t qubits[TCG_MAX_GATE_QUBITS];  /* qubit indices, first = sub-index MSB */
+  int64_t mat_off;   /* complex64 offset of this gate's entries in the
+                        per-circuit matrix buffer (4^nq dense, 2^nq diag)  */
+  int64_t grad_off;  /* complex64 offset of this gate's cotangent in the
+                        per-circuit gradient buffer (same entry count as the
+                        matrix), or -1 when no gradient is wanted           */
+} tcg_gate;
+
+typedef struct tcg_plan tcg_plan; /* opaque, host side; owns a small device
+                                     copy of its pass program               */
+
+typedef struct tcg_plan_opts {
+  int32_t tile_bits;     /* local index bits held by one CTA (<=13); 0 = default */
+  int32_t max_stage_grad_entries; /* cap on cotangent entries per stage; 0 = default */
+} tcg_plan_opts;
+
+typedef struct tcg_plan_stats {
+  int32_t nqubits;
+  int32_t ngates;
+  int32_t npasses;       /* HBM passes over the state per forward sweep   */
+  int32_t nstages;       /* register layouts summed over passes           */
+  int32_t tile_bits;
+  int64_t grad_entries;  /* complex64 cotangent entries per circuit       */
+} tcg_plan_stats;
+
+/* Replaces: the gate queue built by AbstractCircuit._meta_apply /
+ * BaseCircuit.apply_general_gate (tensorcircuit/abstractcircuit.py:218-326,
+ * tensorcircuit/basecircuit.py:120-245) plus the contraction path search of
+ * cons._base (tensorcircuit/cons.py:523-631).  Plans the gate list into HBM
+ * passes; the result is reusable for any batch and any matrix values. */
+int tcg_plan_create(int32_t nqubits, const tcg_gate* gates, int32_t ngates,
+                    const tcg_plan_opts* opts, tcg_plan** out);
+int tcg_plan_destroy(tcg_plan* plan);
+int tcg_plan_get_stats(const tcg_plan* plan, tcg_plan_stats* out);
+
+/* Replaces: Circuit.wavefunction() (tensorcircuit/circuit.py:792-810), i.e.
+ * the contractor loop of cons._base (tensorcircuit/cons.py:605-623).
+ * psi [batch][2^n] holds the input states on entry and the output states on
+ * return (in place).  mats holds batch rows of mat_stride complex64 entries. */
+int tcg_forward(const tcg_plan* plan, void* psi, int64_t batch,
+                const void* mats, int64_t mat_stride, void* stream);
+
+/* Replaces: the reverse-mode AD that backend.vvag runs through the taped
+ * tensordots (tensorcircuit/backends/pytorch_backend.py:673-709).  Adjoint
+ * sweep: on entry psi = output states, mu = cotangent of the output (torch
+ * convention, dL/dRe + i dL/dIm); on return psi = input states, mu = the
+ * cotangent of the input states and grads[b][grad_off + e] = the cotangent
+ * of matrix entry e of each gate with grad_off >= 0.
+ * scratch: tcg_backward_scratch_bytes(plan, batch) bytes of device memory. */
+size_t tcg_backward_scratch_bytes(const tcg_plan* plan, int64_t batch);
+int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch,
+                 const void* mats, int64_t mat_stride, void* grads,
+                 int64_t grad_stride, void* scratch, size_t scratch_bytes,
+                 void* stream);
+
+/* ---- observables ---------------------------------------------------------- */
+
+/* A Pauli string over qubits, as masks over AMPLITUDE-INDEX bits
+ * (bit b <-> qubit n-1-b): xmask has X or Y positions, zmask Z or Y
+ * positions.  (P psi)[a] = (-i)^{#Y} (-1)^{popcount(a & zmask)} psi[a ^ xmask].
+ * The reference builds the same operator from its ps codes 1=X, 2=Y, 3=Z
+ * (tensorcircuit/abstractcircuit.py:1208-1288, quantum.py:1025-1045). */
+typedef struct tcg_pauli {
+  uint64_t xmask;
+  uint64_t zmask;
+} tcg_pauli;
+
+typedef struct tcg_mplan tcg_mplan; /* opaque measurement plan for a term list */
+
+/* Plans a list of Pauli terms into read-only passes (terms whose X/Y
+ * positions fit one tile are grouped; the rest get one plain pass each). */
+int tcg_mplan_create(int32_t nqubits, const tcg_pauli* terms, int32_t nterms,
+                     tcg_mplan** out);
+int tcg_mplan_destroy(tcg_mplan* plan);
+/* number of read passes over the state one expectation call makes */
+int tcg_mplan_passes(const tcg_mplan* plan);
+
+/* Replaces: AbstractCircuit.expectation_ps (tensorcircuit/abstractcircuit.py:
+ * 1208-1288) -> Circuit.expectation (tensorcircuit/circuit.py:914-981), one
+ * sandwich contraction per term there.  Here all terms of the plan are read
+ * from the state in the plan's passes.
+ * out[b][t] = <psi_b| P_t |psi_b> as complex128 (re, im interleaved).
+ * scratch: tcg_expect_scratch_bytes(plan, batch) bytes. */
+size_t tcg_expect_scratch_bytes(const tcg_mplan* plan, int64_t batch);
+int tcg_expect_pauli(const tcg_mplan* plan, const void* psi, int64_t batch,
+                     double* out, void* scratch, size_t scratch_bytes,
+                     void* stream);
+
+/* Cotangent seed for Pauli observables: mu[b] += sum_t coef[b][t] P_t psi[b]
+ * (coef real fp32, coef_stride floats per circuit).  With coef = 2 Re(g_t)
+ * this is the cotangent the reference's AD propagates into the state for
+ * outputs <P_t> with incoming gradients g_t. */
+int tcg_pauli_accumulate(const tcg_mplan* plan, const void* psi, void* mu,
+                         int64_t batch, const float* coef, int64_t coef_stride,
+                         void* stream);
+
+/* ---- sampling --------------------------------------------------------------
+ * Replaces: BaseCircuit.sample(allow_state=True, status=u)
+ * (tensorcircuit/basecircuit.py:525-616) -> backend.probability_sample
+ * (tensorcircuit/backends/abstract_backend.py:1124-1157): normalise |psi|^2,
+ * cumulative sum, r = cdf[-1] * (1 - u), left searchsorted.
+ * Declared CDF arithmetic (integer, so every parallel scan order gives the
+ * same bits):  w(x) = floor(x^2 * 2^60) for an fp32 component x, computed
+ * exactly from its bits (0 for zero/subnormal x);  q[a] = w(re) + w(im);
+ * cdf = inclusive uint64 prefix sum of q;  target
+ * t = (uint64) floor((1.0 - (double)u) * (double)cdf[last]) in double;
+ * out = first index with cdf[index] >= t, clamped to 2^n - 1.
+ * Preconditions: |re|, |im| < 2 and sum |psi|^2 < 16 (true for states).
+ * psi [batch][2^n]; u [batch][u_stride] (u_stride 0 shares one draw vector);
+ * out [batch][nshots].  scratch: tcg_sample_scratch_bytes(n, batch) bytes. */
+size_t tcg_sample_scratch_bytes(int32_t nqubits, int64_t batch);
+int tcg_sample(const void* psi, int32_t nqubits, int64_t batch, const float* u,
+               int64_t u_stride, int64_t nshots, int64_t* out, void* scratch,
+               size_t scratch_bytes, void* stream);
+
+/* Replaces: BaseCircuit.probability (tensorcircuit/basecircuit.py:510-523):
+ * p[a] = |psi[a]|^2 in fp32 (computed as re^2 + im^2). */
+int tcg_probability(const void* psi, int64_t len, float* p, void* stream);
+
+/* Inner products <a_b|b_b> for batch rows of len amplitudes, complex128 out. */
+int tcg_inner(const void* a, const void* b, int64_t len, int64_t batch,
+              double* out, void* scratch, size_t scratch_bytes, void* stream);
+size_t tcg_inner_scratch_bytes(int64_t len, int64_t batch);
+
+/* ---- misc ------------------------------------------------------------------ */
+const char* tcg_status_string(int32_t status);
+int32_t tcg_abi_version(void);
+
+/* Diagnostics (no reference counterpart): host pointers to a plan's pass
+ * program so tests can replay its index arithmetic on the CPU.  which = 0
+ * forward, 1 adjoint, 2 the measurement program of an mplan (pass the
+ * mplan as `plan`).  arrays[0..4] = passes, stages, ops, slot_out, runs;
+ * counts[0..4] their lengths; sizes[0..4] the element sizes in bytes. */
+int tcg_debug_program(const void* plan, int32_t which, const void** arrays,
+                      int64_t* counts, int64_t* sizes);
+
+/* Number of kernel launches this library has issued since it was loaded
+ * (all entry points, all devices). */
+int64_t tcg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCGB300_H */

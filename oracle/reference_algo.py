@@ -1,0 +1,81 @@
+"""Reference-algorithm restatement for the CPU baseline (test / bench
+infrastructure only, see oracle/__init__.py).
+
+LABELLED RESTATEMENT, NOT TENSORCIRCUIT: the reference cannot be imported
+here (its third-party ``tensornetwork`` dependency is absent), so its CPU path
+for ``backend.vvag`` on the pytorch backend is restated in torch on the host:
+gates are built with the reference's formulas (tensorcircuit/gates.py:579-594
+rx, :825-865 rzz = exp1 with half angle), contracted one ``tensordot`` per gate
+in circuit order (the ``plain`` contractor semantics, tensorcircuit/cons.py:
+334-370), the energy is a sum of per-term Pauli sandwiches on the cached
+state (basecircuit.py:267-319), and value+gradient is
+``torch.vmap(torch.func.grad_and_value(f))`` with taped reverse-mode AD
+(tensorcircuit/backends/pytorch_backend.py:533-544, 605-617, 673-709).
+"""
+
+from typing import Any, Dict, List, Sequence, Tuple
+
+import numpy as np
+import torch
+
+C64 = torch.complex64
+
+
+def _rx(theta: torch.Tensor) -> torch.Tensor:
+    c = torch.cos(theta / 2).to(C64)
+    s = torch.sin(theta / 2).to(C64)
+    i2 = torch.eye(2, dtype=C64)
+    x = torch.tensor([[0, 1], [1, 0]], dtype=C64)
+    return c * i2 - 1j * s * x
+
+
+def _rzz(theta: torch.Tensor) -> torch.Tensor:
+    c = torch.cos(theta / 2).to(C64)
+    s = torch.sin(theta / 2).to(C64)
+    zz = torch.diag(torch.tensor([1, -1, -1, 1], dtype=C64))
+    return (c * torch.eye(4, dtype=C64) - 1j * s * zz).reshape(2, 2, 2, 2)
+
+
+_PAULI = {
+    "x": torch.tensor([[0, 1], [1, 0]], dtype=C64),
+    "y": torch.tensor([[0, -1j], [1j, 0]], dtype=C64),
+    "z": torch.tensor([[1, 0], [0, -1]], dtype=C64),
+}
+
+
+def _apply(psi: torch.Tensor, g: torch.Tensor, qubits: Sequence[int]) -> torch.Tensor:
+    k = len(qubits)
+    out = torch.tensordot(g, psi, dims=(list(range(k, 2 * k)), list(qubits)))
+    return torch.movedim(out, list(range(k)), list(qubits))
+
+
+def hea_energy_fn(n: int, layout: Sequence[Tuple[str, Tuple[int, ...], int]],
+                  terms: Sequence[Tuple[float, Dict[str, List[int]]]]) -> Any:
+    psi0 = torch.zeros([2] * n, dtype=C64)
+    psi0.view(-1)[0] = 1.0
+
+    def f(params: torch.Tensor) -> torch.Tensor:
+        psi = psi0
+        for name, q, k in layout:
+            g = _rx(params[k]) if name == "rx" else _rzz(params[k])
+            psi = _apply(psi, g, q)
+        e = torch.zeros((), dtype=torch.float32)
+        for coef, t in terms:
+            phi = psi
+            for kind, qs in t.items():
+                for qq in qs:
+                    phi = _apply(phi, _PAULI[kind], (qq,))
+            e = e + coef * torch.real(torch.sum(torch.conj(psi) * phi))
+        return e
+
+    return f
+
+
+def vvag_hea(n: int, layout: Sequence[Tuple[str, Tuple[int, ...], int]],
+             terms: Sequence[Tuple[float, Dict[str, List[int]]]], params: np.ndarray,
+             threads: int) -> Tuple[np.ndarray, np.ndarray]:
+    torch.set_num_threads(threads)
+    f = hea_energy_fn(n, layout, terms)
+    vg = torch.func.vmap(torch.func.grad_and_value(f))
+    g, v = vg(torch.as_tensor(params, dtype=torch.float32))
+    return v.numpy(), g.numpy()

@@ -1,0 +1,185 @@
+"""ctypes binding of the engine's C ABI (``include/tcgb300.h``).
+
+The library is loaded from the package's ``lib/`` folder.  There is no CPU
+fallback: when the library or a CUDA device is missing, every entry point
+raises, so a silent non-native path can never stand in for the kernels.
+"""
+
+import ctypes
+import os
+import threading
+from typing import Any, Optional
+
+from . import _build
+
+TCG_OK = 0
+TCG_ERR_INVALID_ARG = 1
+TCG_ERR_DUP_QUBIT = 2
+TCG_ERR_UNSUPPORTED = 3
+TCG_ERR_CUDA = 4
+TCG_ERR_SCRATCH = 5
+TCG_ERR_OOM = 6
+
+TCG_GATE_DENSE = 0
+TCG_GATE_DIAG = 1
+MAX_GATE_QUBITS = 6
+MIN_QUBITS = 6
+
+
+class TcgGate(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("nq", ctypes.c_int32),
+        ("qubits", ctypes.c_int32 * MAX_GATE_QUBITS),
+        ("mat_off", ctypes.c_int64),
+        ("grad_off", ctypes.c_int64),
+    ]
+
+
+class TcgPlanOpts(ctypes.Structure):
+    _fields_ = [("tile_bits", ctypes.c_int32), ("max_stage_grad_entries", ctypes.c_int32)]
+
+
+class TcgPlanStats(ctypes.Structure):
+    _fields_ = [
+        ("nqubits", ctypes.c_int32),
+        ("ngates", ctypes.c_int32),
+        ("npasses", ctypes.c_int32),
+        ("nstages", ctypes.c_int32),
+        ("tile_bits", ctypes.c_int32),
+        ("grad_entries", ctypes.c_int64),
+    ]
+
+
+class TcgPauli(ctypes.Structure):
+    _fields_ = [("xmask", ctypes.c_uint64), ("zmask", ctypes.c_uint64)]
+
+
+# (name, restype, argtypes) for every exported symbol
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_SZ = ctypes.c_size_t
+SIGNATURES = [
+    ("tcg_abi_version", _I32, []),
+    ("tcg_status_string", ctypes.c_char_p, [_I32]),
+    ("tcg_plan_create", ctypes.c_int, [_I32, ctypes.POINTER(TcgGate), _I32, ctypes.POINTER(TcgPlanOpts), ctypes.POINTER(_P)]),
+    ("tcg_plan_destroy", ctypes.c_int, [_P]),
+    ("tcg_plan_get_stats", ctypes.c_int, [_P, ctypes.POINTER(TcgPlanStats)]),
+    ("tcg_forward", ctypes.c_int, [_P, _P, _I64, _P, _I64, _P]),
+    ("tcg_backward_scratch_bytes", _SZ, [_P, _I64]),
+    ("tcg_backward", ctypes.c_int, [_P, _P, _P, _I64, _P, _I64, _P, _I64, _P, _SZ, _P]),
+    ("tcg_mplan_create", ctypes.c_int, [_I32, ctypes.POINTER(TcgPauli), _I32, ctypes.POINTER(_P)]),
+    ("tcg_mplan_destroy", ctypes.c_int, [_P]),
+    ("tcg_mplan_passes", ctypes.c_int, [_P]),
+    ("tcg_expect_scratch_bytes", _SZ, [_P, _I64]),
+    ("tcg_expect_pauli", ctypes.c_int, [_P, _P, _I64, _P, _P, _SZ, _P]),
+    ("tcg_pauli_accumulate", ctypes.c_int, [_P, _P, _P, _I64, _P, _I64, _P]),
+    ("tcg_sample_scratch_bytes", _SZ, [_I32, _I64]),
+    ("tcg_sample", ctypes.c_int, [_P, _I32, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),
+    ("tcg_probability", ctypes.c_int, [_P, _I64, _P, _P]),
+    ("tcg_inner_scratch_bytes", _SZ, [_I64, _I64]),
+    ("tcg_inner", ctypes.c_int, [_P, _P, _I64, _I64, _P, _P, _SZ, _P]),
+    ("tcg_launch_count", _I64, []),
+    ("tcg_debug_program", ctypes.c_int, [_P, _I32, ctypes.POINTER(_P), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+]
+
+
+# Mirrors of the device-program records (tensorcircuit_gb300/csrc/engine.h),
+# read by the CPU replay in the tests.
+class DevPass(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_int32), ("nnonlocal", ctypes.c_int32), ("lbits", ctypes.c_int32 * 13),
+                ("nlbits", ctypes.c_int32 * 32), ("stage_begin", ctypes.c_int32), ("stage_end", ctypes.c_int32),
+                ("runs_off", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class DevStage(ctypes.Structure):
+    _fields_ = [("R", ctypes.c_int32), ("smem_stage", ctypes.c_int32), ("lanes_low", ctypes.c_int32),
+                ("nthread_bits", ctypes.c_int32), ("reg_tile", ctypes.c_int32 * 6),
+                ("thr_tile", ctypes.c_int32 * 16), ("op_begin", ctypes.c_int32), ("op_end", ctypes.c_int32),
+                ("nslots", ctypes.c_int32), ("slot_out_begin", ctypes.c_int32), ("slot_out_end", ctypes.c_int32)]
+
+
+class DevOp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("k", ctypes.c_int32), ("p", ctypes.c_int32 * 6),
+                ("xreg", ctypes.c_int32), ("nY", ctypes.c_int32), ("zmask", ctypes.c_uint32),
+                ("slot", ctypes.c_int32), ("mat_off", ctypes.c_int64), ("grad_off", ctypes.c_int64)]
+
+
+class SlotOut(ctypes.Structure):
+    _fields_ = [("slot", ctypes.c_int32), ("pad", ctypes.c_int32), ("out_off", ctypes.c_int64)]
+
+
+def debug_program(handle: Any, which: int) -> dict:
+    """Copy of a plan's device program as lists of ctypes records."""
+    lib = load()
+    arrs = (ctypes.c_void_p * 5)()
+    cnts = (ctypes.c_int64 * 5)()
+    szs = (ctypes.c_int64 * 5)()
+    check(lib.tcg_debug_program(handle, which, arrs, cnts, szs), "debug_program")
+    out = {}
+    for i, (name, typ) in enumerate([("passes", DevPass), ("stages", DevStage), ("ops", DevOp),
+                                     ("slot_out", SlotOut), ("runs", ctypes.c_uint32)]):
+        if ctypes.sizeof(typ) != szs[i]:
+            raise EngineError("record size mismatch for %s: %d vs %d" % (name, ctypes.sizeof(typ), szs[i]))
+        if cnts[i] == 0:
+            out[name] = []
+            continue
+        arr = (typ * cnts[i]).from_address(arrs[i])
+        out[name] = [arr[j] for j in range(cnts[i])] if typ is not ctypes.c_uint32 else list(arr)
+    return out
+
+_lib: Optional[ctypes.CDLL] = None
+_lock = threading.Lock()
+
+
+class EngineError(RuntimeError):
+    """A status code other than TCG_OK from the native engine."""
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load (building first if needed) the engine library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.lib_path()
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise EngineError("engine library %s is missing; run tensorcircuit_gb300._build.build()" % path)
+        lib = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    """Map a status code to the exception type the reference raises."""
+    if status == TCG_OK:
+        return
+    msg = load().tcg_status_string(status).decode()
+    if what:
+        msg = "%s: %s" % (what, msg)
+    if status == TCG_ERR_DUP_QUBIT:
+        raise AssertionError(msg)
+    if status == TCG_ERR_INVALID_ARG:
+        raise ValueError(msg)
+    if status == TCG_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise EngineError(msg)
+
+
+def ptr(t: Any) -> int:
+    return int(t.data_ptr())
+
+
+def stream_ptr(device: Any = None) -> int:
+    import torch
+
+    return int(torch.cuda.current_stream(device).cuda_stream)

@@ -1,0 +1,736 @@
+"""``Circuit``: the reference's circuit API on top of the GB300 engine.
+
+Gate methods are registered from the same name lists as the reference
+(``sgates``, ``vgates``, ``mpogates``, ``gate_aliases``;
+tensorcircuit/abstractcircuit.py:28-66, ``_meta_apply`` :218-326), take the
+same keyword parameters and broadcast over index lists the same way
+(``apply_list``, :149-165).  A gate call only RECORDS the gate
+(tensorcircuit/basecircuit.py:120-245 queues a tensor-network node instead);
+the state is computed by the engine when it is first needed and cached, like
+the reference's ``state_tensor`` cache (basecircuit.py:249-265).
+"""
+
+import hashlib
+from typing import Any, Dict, List, Optional, Sequence, Tuple, Union
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from . import engine as eng
+from . import gates
+from .quantum import sample2all, sample_int2bin
+
+Tensor = Any
+C64 = torch.complex64
+
+_PAULI_1Q = {
+    0: np.eye(2, dtype=np.complex128),
+    1: gates._x_matrix.astype(np.complex128),
+    2: gates._y_matrix.astype(np.complex128),
+    3: gates._z_matrix.astype(np.complex128),
+}
+
+
+def _is_seq(x: Any) -> bool:
+    return isinstance(x, (list, tuple, range)) or (isinstance(x, np.ndarray) and x.ndim > 0)
+
+
+def _to_np_matrix(m: Any) -> Optional[np.ndarray]:
+    """numpy matrix for constant operands, None for torch tensors."""
+    if isinstance(m, gates.Gate):
+        m = m.tensor
+    if isinstance(m, torch.Tensor):
+        return None
+    a = np.asarray(m, dtype=np.complex128)
+    d = int(round(np.sqrt(a.size)))
+    return a.reshape(d, d)
+
+
+def _pauli_decompose(m: np.ndarray) -> Optional[List[int]]:
+    """If m is a tensor product of single-qubit Paulis, return their codes."""
+    d = m.shape[0]
+    k = int(round(np.log2(d)))
+    if (1 << k) != d:
+        return None
+    codes: List[int] = []
+
+    def rec(mat: np.ndarray, kk: int) -> bool:
+        if kk == 0:
+            return bool(np.allclose(mat, 1.0, atol=1e-12))
+        h = mat.shape[0] // 2
+        for c, p in _PAULI_1Q.items():
+            # mat = p (x) rest  ->  rest = block / p_ij for a nonzero p entry
+            i, j = (0, 0) if abs(p[0, 0]) > 0 else (0, 1)
+            rest = mat[i * h:(i + 1) * h, j * h:(j + 1) * h] / p[i, j]
+            if np.allclose(np.kron(p, rest), mat, atol=1e-10):
+                codes.append(c)
+                if rec(rest, kk - 1):
+                    return True
+                codes.pop()
+        return False
+
+    return codes if rec(m, k) else None
+
+
+class _Op:
+    """One recorded gate.
+
+    kind: "const" (numpy matrix), "fam" (parameterized family), "any"
+    (user torch matrix), "exp1"/"exp" (exponential of a given hermitian)."""
+
+    __slots__ = ("kind", "name", "qubits", "data", "diag", "nq")
+
+    def __init__(self, kind: str, name: str, qubits: Tuple[int, ...], data: Any, diag: bool, nq: int) -> None:
+        self.kind = kind
+        self.name = name
+        self.qubits = qubits
+        self.data = data
+        self.diag = diag
+        self.nq = nq
+
+
+class _PlanEntry:
+    """Cached per-structure data: native plan + matrix-buffer layout."""
+
+    def __init__(self, plan: eng.GatePlan, const_block: Optional[np.ndarray], groups: List[Any], nmat: int,
+                 gates_c: Optional[List[Any]] = None) -> None:
+        self.plan = plan
+        self.gates_c = gates_c or []  # (kind, qubits, mat_off, grad_off) per gate
+        self.const_np = const_block
+        self.const_dev: Dict[int, torch.Tensor] = {}
+        self.groups = groups  # (gkey, op indices, E)
+        self.nmat = nmat
+
+    def const_block(self, dev: torch.device) -> Optional[torch.Tensor]:
+        if self.const_np is None:
+            return None
+        t = self.const_dev.get(dev.index)
+        if t is None:
+            t = torch.as_tensor(self.const_np, dtype=C64, device=dev)
+            self.const_dev[dev.index] = t
+        return t
+
+
+_entries: Dict[Any, _PlanEntry] = {}
+
+
+def _group_key(op: _Op) -> Any:
+    if op.kind == "fam":
+        return ("fam", op.name)
+    if op.kind == "any":
+        return ("any", op.nq, op.diag)
+    if op.kind == "exp1":
+        return ("exp1", op.nq, op.data[2], op.diag)
+    if op.kind == "exp":
+        return ("exp", op.nq)
+    raise ValueError(op.kind)
+
+
+def _struct_key(n: int, ops: Sequence[_Op]) -> Any:
+    parts = []
+    for op in ops:
+        if op.kind == "const":
+            parts.append(("c", op.name, op.qubits))
+        else:
+            parts.append((_group_key(op), op.qubits))
+    return (n, tuple(parts))
+
+
+def _build_entry(n_eng: int, ops: Sequence[_Op]) -> _PlanEntry:
+    # constant block first, then one block per parameterized group
+    const_mats: List[np.ndarray] = []
+    const_off: Dict[int, int] = {}
+    off = 0
+    for i, op in enumerate(ops):
+        if op.kind == "const":
+            m = op.data
+            e = np.diag(m) if op.diag else m.reshape(-1)
+            const_off[i] = off
+            const_mats.append(e.astype(np.complex64))
+            off += e.size
+    groups: Dict[Any, List[int]] = {}
+    order: List[Any] = []
+    for i, op in enumerate(ops):
+        if op.kind != "const":
+            k = _group_key(op)
+            if k not in groups:
+                groups[k] = []
+                order.append(k)
+            groups[k].append(i)
+    mat_off: Dict[int, int] = dict(const_off)
+    grad_off: Dict[int, int] = {}
+    glist = []
+    for k in order:
+        idx = groups[k]
+        E = (1 << ops[idx[0]].nq) if ops[idx[0]].diag else (1 << (2 * ops[idx[0]].nq))
+        for j, i in enumerate(idx):
+            mat_off[i] = off + j * E
+            if ops[i].nq <= 2:
+                grad_off[i] = off + j * E
+        off += E * len(idx)
+        glist.append((k, idx, E))
+    gates_c = []
+    for i, op in enumerate(ops):
+        kind = nat.TCG_GATE_DIAG if op.diag else nat.TCG_GATE_DENSE
+        gates_c.append((kind, op.qubits, mat_off[i], grad_off.get(i, -1)))
+    plan = eng.GatePlan(n_eng, gates_c, off)
+    const_block = np.concatenate(const_mats) if const_mats else None
+    return _PlanEntry(plan, const_block, glist, off, gates_c)
+
+
+def _stack_scalars(vals: Sequence[Any], dev: torch.device) -> torch.Tensor:
+    if all(not isinstance(v, torch.Tensor) for v in vals):
+        arr = np.asarray([np.asarray(v) for v in vals])
+        if np.iscomplexobj(arr):
+            return torch.as_tensor(arr.astype(np.complex64), device=dev)
+        return torch.as_tensor(arr.astype(np.float32), device=dev)
+    cplx = any((isinstance(v, torch.Tensor) and v.is_complex()) or np.iscomplexobj(v) for v in vals)
+    dt = torch.complex64 if cplx else torch.float32
+    ts = []
+    for v in vals:
+        if isinstance(v, torch.Tensor):
+            t = v.to(device=dev, dtype=dt)
+        else:
+            t = torch.as_tensor(np.asarray(v), device=dev).to(dt)
+        ts.append(t.reshape(()))
+    return torch.stack(ts)
+
+
+def _stack_mats(vals: Sequence[Any], d: int, dev: torch.device) -> torch.Tensor:
+    ts = []
+    for v in vals:
+        if isinstance(v, gates.Gate):
+            v = v.tensor
+        if not isinstance(v, torch.Tensor):
+            v = torch.as_tensor(np.asarray(v, dtype=np.complex64))
+        ts.append(v.to(device=dev, dtype=C64).reshape(d, d))
+    return torch.stack(ts)
+
+
+def _group_block(key: Any, ops: Sequence[_Op], idx: Sequence[int], dev: torch.device) -> torch.Tensor:
+    kind = key[0]
+    if kind == "fam":
+        fam = gates.FAMILIES[key[1]]
+        args = []
+        for p, (pname, _) in enumerate(fam.params):
+            args.append(_stack_scalars([ops[i].data[p] for i in idx], dev))
+        return fam.build(*args)
+    if kind == "any":
+        nq, diag = key[1], key[2]
+        d = 1 << nq
+        m = _stack_mats([ops[i].data for i in idx], d, dev)
+        if diag:
+            return torch.diagonal(m, dim1=-2, dim2=-1)
+        return m.reshape(m.shape[:-2] + (d * d,))
+    if kind == "exp1":
+        nq, half, diag = key[1], key[2], key[3]
+        d = 1 << nq
+        theta = _stack_scalars([ops[i].data[0] for i in idx], dev)
+        u = _stack_mats([ops[i].data[1] for i in idx], d, dev)
+        if diag:
+            return gates.build_exp1_diag(theta, torch.diagonal(u, dim1=-2, dim2=-1), half)
+        return gates.build_exp1_dense(theta, u, half)
+    if kind == "exp":
+        d = 1 << key[1]
+        theta = _stack_scalars([ops[i].data[0] for i in idx], dev)
+        u = _stack_mats([ops[i].data[1] for i in idx], d, dev)
+        return gates.build_exp_dense(theta, u)
+    raise ValueError(kind)
+
+
+class Circuit:
+    """Statevector circuit with the reference's ``tc.Circuit`` surface."""
+
+    sgates = gates.sgates
+    vgates = gates.vgates
+    mpogates = gates.mpogates
+    gate_aliases = gate_aliases = gates.gate_aliases
+    is_dm = False
+    is_mps = False
+
+    def __init__(self, nqubits: int, inputs: Optional[Tensor] = None, mps_inputs: Optional[Any] = None,
+                 split: Optional[Dict[str, Any]] = None) -> None:
+        if mps_inputs is not None:
+            raise NotImplementedError("mps_inputs is not supported by the statevector engine")
+        if nqubits < 1:
+            raise ValueError("a circuit needs at least one qubit")
+        self._nqubits = nqubits
+        self.inputs = inputs
+        self.mps_inputs = None
+        self.split = split
+        self.circuit_param = {"nqubits": nqubits, "inputs": inputs, "mps_inputs": None, "split": split}
+        self._qir: List[Dict[str, Any]] = []
+        self._extra_qir: List[Dict[str, Any]] = []
+        self._ops: List[_Op] = []
+        self._cache: Optional[Tuple[Any, ...]] = None
+
+    # ------------------------------------------------------------------ gates
+    def _norm_index(self, index: Sequence[int]) -> Tuple[int, ...]:
+        n = self._nqubits
+        idx = tuple(int(i) if int(i) >= 0 else n + int(i) for i in index)
+        for i in idx:
+            if not 0 <= i < n:
+                raise ValueError("qubit index %d out of range for %d qubits" % (i, n))
+        assert len(idx) == len(set(idx)), "a gate cannot act twice on one qubit"
+        return idx
+
+    def _record(self, op: _Op, ir: Dict[str, Any]) -> None:
+        self._qir.append(ir)
+        self._ops.append(op)
+        self._cache = None
+
+    def _apply_const(self, name: str, index: Sequence[int], ir_extra: Optional[Dict[str, Any]] = None) -> None:
+        idx = self._norm_index(index)
+        m = gates.CONSTANT_GATES[name]
+        k = int(round(np.log2(m.shape[0])))
+        if k != len(idx):
+            raise ValueError("gate %s acts on %d qubits, got %d indices" % (name, k, len(idx)))
+        ir = {"gatef": getattr(gates, name), "index": tuple(index), "name": name, "split": None, "mpo": False}
+        if ir_extra:
+            ir.update(ir_extra)
+        if name == "i":  # identity: recorded, nothing to apply
+            self._qir.append(ir)
+            return
+        self._record(_Op("const", name, idx, m, gates.is_diagonal(m), k), ir)
+
+    def _apply_var(self, name: str, index: Sequence[int], vars: Dict[str, Any]) -> None:
+        localname = vars.pop("name", name)
+        split = vars.pop("split", None)
+        idx = self._norm_index(index)
+        ir = {"gatef": name, "index": tuple(index), "target": list(index), "name": localname, "split": split,
+              "mpo": False, "parameters": dict(vars)}
+        if name in gates.FAMILIES:
+            fam = gates.FAMILIES[name]
+            if len(idx) != fam.nq:
+                raise ValueError("gate %s acts on %d qubits, got %d indices" % (name, fam.nq, len(idx)))
+            data = tuple(vars.get(p, d) for p, d in fam.params)
+            self._record(_Op("fam", name, idx, data, fam.diag, fam.nq), ir)
+            return
+        if name == "any":
+            u = vars.get("unitary")
+            if u is None:
+                raise ValueError("any/unitary gate needs unitary=")
+            self._apply_matrix(u, idx, ir, localname)
+            return
+        if name in ("exp1", "exp"):
+            u = vars.get("unitary", vars.get("hermitian", vars.get("hamiltonian")))
+            theta = vars.get("theta")
+            if u is None or theta is None:
+                raise ValueError("%s gate needs unitary= and theta=" % name)
+            half = bool(vars.get("half", False))
+            un = _to_np_matrix(u)
+            d = 1 << len(idx)
+            if un is not None and un.shape[0] != d:
+                raise ValueError("unitary size does not match %d qubits" % len(idx))
+            if name == "exp1":
+                diag = un is not None and gates.is_diagonal(un)
+                self._record(_Op("exp1", name, idx, (theta, u if un is None else un, half), diag, len(idx)), ir)
+            else:
+                self._record(_Op("exp", name, idx, (theta, u if un is None else un), False, len(idx)), ir)
+            return
+        raise NotImplementedError("gate %s" % name)
+
+    def _apply_matrix(self, u: Any, idx: Tuple[int, ...], ir: Dict[str, Any], name: str) -> None:
+        un = _to_np_matrix(u)
+        k = len(idx)
+        if k > nat.MAX_GATE_QUBITS:
+            raise NotImplementedError("gates on more than %d qubits" % nat.MAX_GATE_QUBITS)
+        if un is not None:
+            if un.shape[0] != (1 << k):
+                raise ValueError("matrix of size %d does not act on %d qubits" % (un.shape[0], k))
+            key = "m:" + hashlib.sha1(un.astype(np.complex128).tobytes()).hexdigest()
+            gates.CONSTANT_GATES.setdefault(key, un)
+            self._record(_Op("const", key, idx, un, gates.is_diagonal(un), k), ir)
+        else:
+            t = u.tensor if isinstance(u, gates.Gate) else u
+            if int(np.prod(t.shape[-2 * k:] if t.dim() >= 2 * k else t.shape)) != (1 << (2 * k)):
+                raise ValueError("matrix does not act on %d qubits" % k)
+            self._record(_Op("any", "any", idx, t, False, k), ir)
+
+    def apply_general_gate(self, gate: Any, *index: int, name: Optional[str] = None,
+                           split: Optional[Dict[str, Any]] = None, mpo: bool = False,
+                           ir_dict: Optional[Dict[str, Any]] = None) -> None:
+        if mpo:
+            raise NotImplementedError("MPO gates are not supported by the statevector engine")
+        idx = self._norm_index(index)
+        ir = {"gate": gate, "index": index, "name": name or "", "split": split, "mpo": mpo}
+        if ir_dict is not None:
+            ir_dict.update(ir)
+            ir = ir_dict
+        self._apply_matrix(gate, idx, ir, name or "any")
+
+    apply = apply_general_gate
+
+    def multicontrol(self, *index: int, ctrl: Union[int, Sequence[int]] = 1, unitary: Any = None,
+                     **kws: Any) -> None:
+        """Controlled unitary: U on the trailing qubits when the leading
+        qubits equal ``ctrl`` (tensorcircuit/gates.py:871-940)."""
+        if isinstance(ctrl, int):
+            ctrl = [ctrl]
+        ctrl = [int(c) for c in ctrl]
+        u = _to_np_matrix(unitary)
+        if u is None:
+            raise NotImplementedError("multicontrol with a traced unitary")
+        nc = len(ctrl)
+        du = u.shape[0]
+        full = np.eye((1 << nc) * du, dtype=np.complex128)
+        cidx = 0
+        for c in ctrl:
+            cidx = cidx * 2 + c
+        full[cidx * du:(cidx + 1) * du, cidx * du:(cidx + 1) * du] = u
+        idx = self._norm_index(index)
+        ir = {"gatef": "multicontrol", "index": tuple(index), "name": "multicontrol", "split": None, "mpo": True,
+              "parameters": {"ctrl": ctrl, "unitary": unitary}}
+        self._apply_matrix(full, idx, ir, "multicontrol")
+
+    def mpo(self, *index: int, **kws: Any) -> None:
+        raise NotImplementedError("MPO gates are not supported by the statevector engine")
+
+    # ------------------------------------------------------------------ state
+    def _engine_state(self) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor, eng.Run, int]:
+        if self._cache is not None:
+            return self._cache  # type: ignore
+        dev = eng.device()
+        n = self._nqubits
+        n_eng = max(n, nat.MIN_QUBITS)
+        pad = n_eng - n
+        key = _struct_key(n_eng, self._ops)
+        entry = _entries.get(key)
+        if entry is None:
+            entry = _build_entry(n_eng, self._ops)
+            _entries[key] = entry
+        blocks = []
+        cb = entry.const_block(dev)
+        if cb is not None:
+            blocks.append(cb)
+        for gkey, idx, E in entry.groups:
+            b = _group_block(gkey, self._ops, idx, dev).to(C64)
+            blocks.append(b.reshape(b.shape[:-2] + (b.shape[-2] * b.shape[-1],)))
+        if blocks:
+            mats = blocks[0] if len(blocks) == 1 else torch.cat(blocks, -1)
+        else:
+            mats = torch.zeros(1, dtype=C64, device=dev)
+        # input state
+        N = 1 << n
+        if self.inputs is None:
+            psi0 = _basis0(n_eng, dev)
+        else:
+            inp = self.inputs
+            if isinstance(inp, gates.Gate):
+                inp = inp.tensor
+            if not isinstance(inp, torch.Tensor):
+                inp = torch.as_tensor(np.asarray(inp, dtype=np.complex64))
+            inp = inp.to(device=dev, dtype=C64).reshape(-1)
+            if inp.shape[-1] != N:
+                raise ValueError("inputs has %d amplitudes, %d qubits need %d" % (inp.shape[-1], n, N))
+            if pad:
+                inp = torch.cat([inp.unsqueeze(-1), torch.zeros(inp.shape + ((1 << pad) - 1,), dtype=C64,
+                                                                device=dev)], -1).reshape(inp.shape[:-1] + (1 << n_eng,))
+            psi0 = inp
+        run = eng.Run(entry.plan, n_eng)
+        psi_eng, anchor = eng.StateFn.apply(mats, psi0, run)
+        psi = psi_eng if pad == 0 else psi_eng.reshape(psi_eng.shape[:-1] + (N, 1 << pad))[..., 0]
+        self._cache = (psi, psi_eng, anchor, run, n_eng)
+        return self._cache  # type: ignore
+
+    def wavefunction(self, form: str = "default") -> Tensor:
+        psi = self._engine_state()[0]
+        if form == "default":
+            return psi
+        if form == "ket":
+            return psi.reshape(psi.shape[:-1] + (-1, 1))
+        if form == "bra":
+            return psi.reshape(psi.shape[:-1] + (1, -1))
+        raise ValueError("unknown form %s" % form)
+
+    state = wavefunction
+
+    def get_state_as_quvector(self) -> Any:
+        raise NotImplementedError("QuVector views are tensor-network objects; use wavefunction()")
+
+    quvector = get_state_as_quvector
+
+    def matrix(self) -> Tensor:
+        """The circuit unitary, from running the plan on all 2^n basis states
+        as one batch."""
+        n = self._nqubits
+        dev = eng.device()
+        c = Circuit(n, inputs=torch.eye(1 << n, dtype=C64, device=dev))
+        c._ops = list(self._ops)
+        c._qir = list(self._qir)
+        return c.wavefunction().transpose(-1, -2)
+
+    # ------------------------------------------------------------ observables
+    def _pauli_term(self, x: Sequence[int], y: Sequence[int], z: Sequence[int], n_eng: int) -> Tuple[int, int]:
+        n = self._nqubits
+        occupied = set()
+        norm = []
+        for lst in (x, y, z):
+            out = []
+            for q in lst:
+                q = int(q)
+                q = q if q >= 0 else n + q
+                if not 0 <= q < n:
+                    raise ValueError("qubit index out of range")
+                if q in occupied:
+                    raise ValueError("Cannot measure two operators in one index")
+                occupied.add(q)
+                out.append(q)
+            norm.append(out)
+        return eng.pauli_masks(n_eng, *norm)
+
+    def expectation_ps(self, x: Optional[Sequence[int]] = None, y: Optional[Sequence[int]] = None,
+                       z: Optional[Sequence[int]] = None, ps: Optional[Sequence[int]] = None, reuse: bool = True,
+                       noise_conf: Optional[Any] = None, nmc: int = 1000, status: Optional[Tensor] = None,
+                       **kws: Any) -> Tensor:
+        """Pauli-string expectation (tensorcircuit/abstractcircuit.py:1208-1288).
+
+        ``ps`` codes 0/1/2/3 = I/X/Y/Z override x/y/z.  Returns a complex64
+        tensor, like the reference."""
+        if noise_conf is not None:
+            raise NotImplementedError("noisy expectations are outside the statevector engine")
+        if ps is not None:
+            from .quantum import ps2xyz
+
+            d = ps2xyz(list(ps))
+            x, y, z = d.get("x", None), d.get("y", None), d.get("z", None)
+        _, psi_eng, anchor, run, n_eng = self._engine_state()
+        term = self._pauli_term(x or [], y or [], z or [], n_eng)
+        return eng.ExpectFn.apply(psi_eng, anchor, (term,), run)[..., 0]
+
+    def expectation_ps_batch(self, terms: Sequence[Dict[str, Sequence[int]]]) -> Tensor:
+        """Many Pauli strings in one call (one engine measurement plan).
+
+        ``terms`` is a list of ``{"x": [...], "y": [...], "z": [...]}``; the
+        result has one complex entry per term in the last dimension."""
+        _, psi_eng, anchor, run, n_eng = self._engine_state()
+        spec = tuple(self._pauli_term(t.get("x", []), t.get("y", []), t.get("z", []), n_eng) for t in terms)
+        return eng.ExpectFn.apply(psi_eng, anchor, spec, run)
+
+    def expectation(self, *ops: Any, reuse: bool = True, enable_lightcone: bool = False,
+                    noise_conf: Optional[Any] = None, nmc: int = 1000, status: Optional[Tensor] = None,
+                    **kws: Any) -> Tensor:
+        """<psi| (x)_k O_k |psi> for ``(operator, [indices])`` pairs
+        (tensorcircuit/circuit.py:914-981).  Pauli products take the
+        measurement kernel; other operators are applied to a copy of the
+        state by a forward sweep and contracted."""
+        if noise_conf is not None:
+            raise NotImplementedError("noisy expectations are outside the statevector engine")
+        n = self._nqubits
+        occupied = set()
+        xs: List[int] = []
+        ys: List[int] = []
+        zs: List[int] = []
+        general: List[Tuple[Any, Tuple[int, ...]]] = []
+        for op, index in ops:
+            if isinstance(index, (int, np.integer)):
+                index = [int(index)]
+            idx = tuple(int(i) if int(i) >= 0 else n + int(i) for i in index)
+            for q in idx:
+                if q in occupied:
+                    raise ValueError("Cannot measure two operators in one index")
+                occupied.add(q)
+            m = _to_np_matrix(op)
+            codes = _pauli_decompose(m) if m is not None and m.shape[0] == (1 << len(idx)) else None
+            if codes is not None:
+                for c, q in zip(codes, idx):
+                    if c == 1:
+                        xs.append(q)
+                    elif c == 2:
+                        ys.append(q)
+                    elif c == 3:
+                        zs.append(q)
+            else:
+                general.append((op, idx))
+        psi, psi_eng, anchor, run, n_eng = self._engine_state()
+        if not general:
+            term = eng.pauli_masks(n_eng, xs, ys, zs)
+            return eng.ExpectFn.apply(psi_eng, anchor, (term,), run)[..., 0]
+        # general operators: phi = O psi through a forward sweep on a copy
+        c = Circuit(n, inputs=psi)
+        for op, idx in general:
+            c._apply_matrix(op, idx, {"gate": op, "index": idx, "name": "op"}, "op")
+        for q in xs:
+            c._apply_const("x", [q])
+        for q in ys:
+            c._apply_const("y", [q])
+        for q in zs:
+            c._apply_const("z", [q])
+        phi = c.wavefunction()
+        return torch.sum(torch.conj(psi) * phi, -1)
+
+    def probability(self) -> Tensor:
+        """|psi|^2 over the computational basis (basecircuit.py:510-523)."""
+        s = self.wavefunction()
+        return torch.abs(s) ** 2
+
+    def amplitude(self, l: Union[str, Tensor]) -> Tensor:
+        """<l|psi> for a bitstring (basecircuit.py:447-508)."""
+        psi = self.wavefunction()
+        n = self._nqubits
+        if isinstance(l, str):
+            if len(l) != n:
+                raise ValueError("bitstring length %d != %d qubits" % (len(l), n))
+            return psi[..., int(l, 2)]
+        lt = l if isinstance(l, torch.Tensor) else torch.as_tensor(np.asarray(l))
+        lt = lt.to(device=psi.device, dtype=C64)
+        t = psi.reshape(psi.shape[:-1] + (2,) * n)
+        for i in range(n):
+            vec = torch.stack([1 - lt[..., i], lt[..., i]], -1)
+            t = torch.sum(t * vec.reshape(vec.shape[:-1] + (2,) + (1,) * (n - 1 - i)), dim=-(n - i))
+        return t
+
+    def sample(self, batch: Optional[int] = None, allow_state: bool = False,
+               readout_error: Optional[Sequence[Any]] = None, format: Optional[str] = None,
+               random_generator: Optional[Any] = None, status: Optional[Tensor] = None, **kws: Any) -> Any:
+        """Samples of the final state (basecircuit.py:525-616).
+
+        With ``status`` (uniforms in [0, 1)) the draw follows the reference's
+        inverse-CDF rule bit-exactly under the engine's declared integer CDF
+        (see ``include/tcgb300.h``).  Without it, uniforms come from torch's
+        generator (``random_generator`` may be a ``torch.Generator``).
+        ``allow_state=False`` selects the reference's per-qubit perfect
+        sampling there; the samples here come from the same distribution
+        through the state's CDF."""
+        if "format_" in kws:
+            format = kws.pop("format_")
+        if readout_error is not None:
+            raise NotImplementedError("readout error is outside the statevector engine")
+        nb = 1 if batch is None else int(batch)
+        psi, psi_eng, anchor, run, n_eng = self._engine_state()
+        dev = psi_eng.device
+        if status is None:
+            gen = random_generator if isinstance(random_generator, torch.Generator) else None
+            if gen is not None and gen.device.type != "cuda":
+                u = torch.rand(nb, generator=gen).to(dev)
+            else:
+                u = torch.rand(nb, generator=gen, device=dev)
+        else:
+            u = status if isinstance(status, torch.Tensor) else torch.as_tensor(np.asarray(status))
+            u = u.to(device=dev, dtype=torch.float32)
+            if u.shape[-1] < nb:
+                raise ValueError("status has %d draws, batch needs %d" % (u.shape[-1], nb))
+            u = u[..., :nb]
+        ch = eng.SampleFn.apply(psi_eng, u, n_eng, nb)
+        pad = n_eng - self._nqubits
+        if pad:
+            ch = torch.bitwise_right_shift(ch, pad)
+        n = self._nqubits
+        if format is None:
+            confg = sample_int2bin(ch, n)
+            p = torch.abs(psi.detach()) ** 2
+            prob = torch.gather(p, -1, ch)
+            r = list(zip(confg, prob))
+            if batch is None:
+                return r[0]
+            return r
+        return sample2all(sample=ch, n=n, format=format, jittable=True)
+
+    def sample_expectation_ps(self, x: Optional[Sequence[int]] = None, y: Optional[Sequence[int]] = None,
+                              z: Optional[Sequence[int]] = None, shots: Optional[int] = None,
+                              random_generator: Optional[Any] = None, status: Optional[Tensor] = None,
+                              readout_error: Optional[Sequence[Any]] = None, noise_conf: Optional[Any] = None,
+                              nmc: int = 1000, statusc: Optional[Tensor] = None, **kws: Any) -> Tensor:
+        """Pauli expectation from measurement shots (basecircuit.py:618-756):
+        rotate X sites by H and Y sites by rx(pi/2), then average the parity
+        of the measured bits.  ``shots=None`` gives the exact value."""
+        if noise_conf is not None or readout_error is not None:
+            raise NotImplementedError("noisy sampling is outside the statevector engine")
+        x, y, z = list(x or []), list(y or []), list(z or [])
+        if shots is None:
+            return torch.real(self.expectation_ps(x=x, y=y, z=z))
+        psi = self.wavefunction()
+        c = Circuit(self._nqubits, inputs=psi)
+        for i in x:
+            c.H(i)
+        for i in y:
+            c.rx(i, theta=np.pi / 2)
+        s = c.sample(batch=shots, allow_state=True, status=status, random_generator=random_generator,
+                     format="sample_bin")
+        sites = [q if q >= 0 else self._nqubits + q for q in x + y + z]
+        if not sites:
+            return torch.ones(s.shape[:-2], dtype=torch.float32, device=s.device)
+        par = torch.sum(s[..., sites], -1) % 2
+        return torch.mean((1 - 2 * par).to(torch.float32), -1)
+
+    sexpps = sample_expectation_ps
+
+    # ---------------------------------------------------------------- misc
+    def to_qir(self) -> List[Dict[str, Any]]:
+        return self._qir
+
+    def __len__(self) -> int:
+        return len(self._ops)
+
+    def gate_count(self) -> int:
+        return len(self._qir)
+
+    def engine_stats(self) -> Dict[str, int]:
+        """Pass/stage counts of the plan the engine uses for this circuit."""
+        _, _, _, run, n_eng = self._engine_state()
+        return {"nqubits": n_eng, "gates": run.plan.ngates, "passes": run.plan.npasses,
+                "stages": run.plan.nstages, "tile_bits": run.plan.tile_bits}
+
+
+_basis_cache: Dict[Tuple[int, int], torch.Tensor] = {}
+
+
+def _basis0(n: int, dev: torch.device) -> torch.Tensor:
+    key = (n, dev.index)
+    t = _basis_cache.get(key)
+    if t is None:
+        t = torch.zeros(1 << n, dtype=C64, device=dev)
+        t[0] = 1.0
+        _basis_cache[key] = t
+    return t
+
+
+# ----------------------------------------------------------------------------
+# gate-method registration (tensorcircuit/abstractcircuit.py:218-326)
+# ----------------------------------------------------------------------------
+def _make_sgate(name: str) -> Any:
+    def apply(self: Circuit, *index: Any, split: Optional[Dict[str, Any]] = None, name_: Optional[str] = None,
+              **kws: Any) -> None:
+        if index and _is_seq(index[0]):
+            for ind in zip(*index):
+                self._apply_const(name, ind)
+            return
+        self._apply_const(name, index)
+
+    apply.__name__ = name
+    apply.__doc__ = "Apply the constant **%s** gate (tensorcircuit/gates.py)." % name.upper()
+    return apply
+
+
+def _make_vgate(name: str) -> Any:
+    def apply(self: Circuit, *index: Any, **vars: Any) -> None:
+        if index and _is_seq(index[0]):
+            for i, ind in enumerate(zip(*index)):
+                nvars = {}
+                for k, v in vars.items():
+                    try:
+                        nvars[k] = v[i]
+                    except Exception:  # scalars broadcast to every index
+                        nvars[k] = v
+                self._apply_var(name, ind, nvars)
+            return
+        self._apply_var(name, index, dict(vars))
+
+    apply.__name__ = name
+    apply.__doc__ = "Apply the parameterized **%s** gate (tensorcircuit/gates.py)." % name.upper()
+    return apply
+
+
+for _g in gates.sgates:
+    setattr(Circuit, _g, _make_sgate(_g))
+    setattr(Circuit, _g.upper(), _make_sgate(_g))
+for _g in gates.vgates:
+    setattr(Circuit, _g, _make_vgate(_g))
+    setattr(Circuit, _g.upper(), _make_vgate(_g))
+setattr(Circuit, "MULTICONTROL", Circuit.multicontrol)
+setattr(Circuit, "MPO", Circuit.mpo)
+for _a in gates.gate_aliases:
+    for _alias in _a[1:]:
+        setattr(Circuit, _alias, getattr(Circuit, _a[0]))
+        setattr(Circuit, _alias.upper(), getattr(Circuit, _a[0].upper()))

@@ -1,0 +1,420 @@
+// api.cu — the extern "C" entry points declared in include/tcgb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "kernels.h"
+#include "plan.h"
+
+using namespace tcg;
+
+namespace {
+
+constexpr int kAbiVersion = 1;
+
+inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int check_gate(int n, const tcg_gate& g) {
+  if (g.kind != TCG_GATE_DENSE && g.kind != TCG_GATE_DIAG) return TCG_ERR_INVALID_ARG;
+  if (g.nq < 1 || g.nq > TCG_MAX_GATE_QUBITS) return TCG_ERR_INVALID_ARG;
+  if (g.mat_off < 0) return TCG_ERR_INVALID_ARG;
+  for (int i = 0; i < g.nq; ++i) {
+    if (g.qubits[i] < 0 || g.qubits[i] >= n) return TCG_ERR_INVALID_ARG;
+    for (int j = 0; j < i; ++j)
+      if (g.qubits[i] == g.qubits[j]) return TCG_ERR_DUP_QUBIT;
+  }
+  if (g.grad_off >= 0 && g.nq > 2) return TCG_ERR_UNSUPPORTED;
+  return TCG_OK;
+}
+
+int cuda_rc(cudaError_t e) { return e == cudaSuccess ? TCG_OK : TCG_ERR_CUDA; }
+
+int mplan_device(tcg_mplan* p, tcg_mplan::Dev* out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(p->mu);
+  auto it = p->dev.find(dev);
+  if (it != p->dev.end()) {
+    *out = it->second;
+    return TCG_OK;
+  }
+  const size_t nt = p->terms.size(), nd = p->direct.size();
+  const size_t o_terms = 0;
+  const size_t o_dir = (nt * sizeof(tcg_pauli) + 255) & ~size_t(255);
+  const size_t o_ent = o_dir + ((nd * sizeof(int) + 255) & ~size_t(255));
+  const size_t total = o_ent + nd * sizeof(int64_t) + 256;
+  std::vector<char> host(total, 0);
+  if (nt) std::memcpy(host.data() + o_terms, p->terms.data(), nt * sizeof(tcg_pauli));
+  for (size_t i = 0; i < nd; ++i) {
+    reinterpret_cast<int*>(host.data() + o_dir)[i] = p->direct[i];
+    reinterpret_cast<int64_t*>(host.data() + o_ent)[i] = p->direct[i];
+  }
+  void* d = nullptr;
+  if (cudaMalloc(&d, total) != cudaSuccess) return TCG_ERR_OOM;
+  if (cudaMemcpy(d, host.data(), total, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return TCG_ERR_CUDA;
+  }
+  tcg_mplan::Dev dv;
+  dv.base = d;
+  dv.terms = reinterpret_cast<tcg_pauli*>(static_cast<char*>(d) + o_terms);
+  dv.direct = reinterpret_cast<int*>(static_cast<char*>(d) + o_dir);
+  dv.direct_entries = reinterpret_cast<int64_t*>(static_cast<char*>(d) + o_ent);
+  p->dev[dev] = dv;
+  *out = dv;
+  return TCG_OK;
+}
+
+constexpr uint32_t kDirectBlocks = 304;
+
+}  // namespace
+
+extern "C" {
+
+int32_t tcg_abi_version(void) { return kAbiVersion; }
+
+int64_t tcg_launch_count(void) { return launch_count(); }
+
+const char* tcg_status_string(int32_t s) {
+  switch (s) {
+    case TCG_OK: return "ok";
+    case TCG_ERR_INVALID_ARG: return "invalid argument";
+    case TCG_ERR_DUP_QUBIT: return "a gate lists the same qubit twice";
+    case TCG_ERR_UNSUPPORTED: return "not supported by the engine";
+    case TCG_ERR_CUDA: return "CUDA runtime error";
+    case TCG_ERR_SCRATCH: return "scratch buffer too small";
+    case TCG_ERR_OOM: return "allocation failed";
+    default: return "unknown status";
+  }
+}
+
+int tcg_plan_create(int32_t nqubits, const tcg_gate* gates, int32_t ngates, const tcg_plan_opts* opts,
+                    tcg_plan** out) {
+  if (!out) return TCG_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (nqubits < kMinQubits || nqubits > kMaxQubits || ngates < 0 || (ngates > 0 && !gates))
+    return TCG_ERR_INVALID_ARG;
+  std::vector<PGate> pg;
+  bool has_grad = false;
+  int64_t grad_entries = 0;
+  for (int i = 0; i < ngates; ++i) {
+    const int rc = check_gate(nqubits, gates[i]);
+    if (rc != TCG_OK) return rc;
+    PGate g;
+    std::memset(&g, 0, sizeof(g));
+    g.kind = gates[i].kind;
+    g.k = gates[i].nq;
+    for (int q = 0; q < g.k; ++q) g.gbits[q] = nqubits - 1 - gates[i].qubits[q];
+    g.mat_off = gates[i].mat_off;
+    g.grad_off = gates[i].grad_off;
+    if (g.grad_off >= 0) {
+      has_grad = true;
+      const int64_t E = (g.kind == TCG_GATE_DIAG) ? (1 << g.k) : (1 << (2 * g.k));
+      grad_entries = std::max(grad_entries, g.grad_off + E);
+    }
+    pg.push_back(g);
+  }
+  PlanOpts po;
+  if (opts && opts->tile_bits > 0) {
+    po.tile_bits_fwd = std::min(opts->tile_bits, kRFwd + 8);  // at most 256 threads
+    po.tile_bits_bwd = std::min(opts->tile_bits, kRBwd + 8);
+  }
+  if (opts && opts->max_stage_grad_entries > 0) po.max_stage_slots = std::max(16, opts->max_stage_grad_entries);
+  if (po.tile_bits_fwd < kRFwd + 1 || po.tile_bits_bwd < kRBwd + 1) return TCG_ERR_INVALID_ARG;
+  tcg_plan* p = new (std::nothrow) tcg_plan();
+  if (!p) return TCG_ERR_OOM;
+  p->n = nqubits;
+  p->ngates = ngates;
+  p->has_grad = has_grad;
+  p->grad_entries = grad_entries;
+  std::vector<PGate> fwd_gates = pg;
+  for (PGate& g : fwd_gates) g.grad_off = -1;
+  int rc = build_gate_program(nqubits, fwd_gates, po.tile_bits_fwd, kRFwd, false, po.max_stage_slots, &p->fwd);
+  if (rc == TCG_OK)
+    rc = build_gate_program(nqubits, pg, po.tile_bits_bwd, kRBwd, true, po.max_stage_slots, &p->bwd);
+  if (rc != TCG_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return TCG_OK;
+}
+
+int tcg_plan_destroy(tcg_plan* plan) {
+  if (!plan) return TCG_OK;
+  program_free(&plan->fwd);
+  program_free(&plan->bwd);
+  delete plan;
+  return TCG_OK;
+}
+
+int tcg_plan_get_stats(const tcg_plan* plan, tcg_plan_stats* out) {
+  if (!plan || !out) return TCG_ERR_INVALID_ARG;
+  out->nqubits = plan->n;
+  out->ngates = plan->ngates;
+  out->npasses = (int)plan->fwd.passes.size();
+  out->nstages = (int)plan->fwd.stages.size();
+  out->tile_bits = plan->fwd.L;
+  out->grad_entries = plan->grad_entries;
+  return TCG_OK;
+}
+
+int tcg_forward(const tcg_plan* plan, void* psi, int64_t batch, const void* mats, int64_t mat_stride,
+                void* stream) {
+  if (!plan || !psi || batch < 0) return TCG_ERR_INVALID_ARG;
+  if (batch == 0) return TCG_OK;
+  if (plan->ngates > 0 && !mats) return TCG_ERR_INVALID_ARG;
+  tcg_plan* p = const_cast<tcg_plan*>(plan);
+  ProgramView view;
+  int rc = program_device_view(&p->fwd, &view);
+  if (rc != TCG_OK) return rc;
+  if (plan->ngates == 0) return TCG_OK;
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.prog = view;
+  a.n = plan->n;
+  a.psi = static_cast<float2*>(psi);
+  a.mats = static_cast<const float2*>(mats);
+  a.mat_stride = mat_stride;
+  a.max_slots = 0;
+  for (int ps = 0; ps < (int)p->fwd.passes.size(); ++ps) {
+    a.pass = ps;
+    rc = cuda_rc(launch_pass(MODE_FWD, kRFwd, a, p->fwd.L, batch, as_stream(stream)));
+    if (rc != TCG_OK) return rc;
+  }
+  return TCG_OK;
+}
+
+size_t tcg_backward_scratch_bytes(const tcg_plan* plan, int64_t batch) {
+  if (!plan) return 0;
+  const size_t ntiles = size_t(1) << (plan->n - plan->bwd.L);
+  return size_t(batch) * size_t(std::max<int64_t>(plan->bwd.nout, 1)) * ntiles * sizeof(float2) + 256;
+}
+
+int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch, const void* mats,
+                 int64_t mat_stride, void* grads, int64_t grad_stride, void* scratch, size_t scratch_bytes,
+                 void* stream) {
+  if (!plan || !psi || !mu || batch < 0) return TCG_ERR_INVALID_ARG;
+  if (batch == 0 || plan->ngates == 0) return TCG_OK;
+  if (!mats) return TCG_ERR_INVALID_ARG;
+  if (plan->has_grad && (!grads || grad_stride < plan->grad_entries)) return TCG_ERR_INVALID_ARG;
+  tcg_plan* p = const_cast<tcg_plan*>(plan);
+  const size_t need = tcg_backward_scratch_bytes(plan, batch);
+  if (plan->has_grad && (!scratch || scratch_bytes < need)) return TCG_ERR_SCRATCH;
+  ProgramView view;
+  int rc = program_device_view(&p->bwd, &view);
+  if (rc != TCG_OK) return rc;
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.prog = view;
+  a.n = plan->n;
+  a.psi = static_cast<float2*>(psi);
+  a.mu = static_cast<float2*>(mu);
+  a.mats = static_cast<const float2*>(mats);
+  a.mat_stride = mat_stride;
+  a.partial = static_cast<float2*>(scratch);
+  a.part_stride = std::max<int64_t>(p->bwd.nout, 1);
+  a.max_slots = std::max(p->bwd.max_slots, 1);
+  for (int ps = 0; ps < (int)p->bwd.passes.size(); ++ps) {
+    a.pass = ps;
+    rc = cuda_rc(launch_pass(MODE_BWD, kRBwd, a, p->bwd.L, batch, as_stream(stream)));
+    if (rc != TCG_OK) return rc;
+  }
+  if (plan->has_grad) {
+    const uint32_t ntiles = 1u << (plan->n - p->bwd.L);
+    rc = cuda_rc(launch_reduce_partials(a.partial, a.part_stride, ntiles, view.entries, view.nentries, batch,
+                                        static_cast<float2*>(grads), grad_stride, nullptr, 0,
+                                        as_stream(stream)));
+  }
+  return rc;
+}
+
+int tcg_mplan_create(int32_t nqubits, const tcg_pauli* terms, int32_t nterms, tcg_mplan** out) {
+  if (!out) return TCG_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (nqubits < kMinQubits || nqubits > kMaxQubits || nterms < 0 || (nterms > 0 && !terms))
+    return TCG_ERR_INVALID_ARG;
+  const uint64_t full = (nqubits >= 64) ? ~0ull : ((1ull << nqubits) - 1);
+  for (int t = 0; t < nterms; ++t)
+    if ((terms[t].xmask & ~full) || (terms[t].zmask & ~full)) return TCG_ERR_INVALID_ARG;
+  tcg_mplan* p = new (std::nothrow) tcg_mplan();
+  if (!p) return TCG_ERR_OOM;
+  p->n = nqubits;
+  p->nterms = nterms;
+  p->terms.assign(terms, terms + nterms);
+  PlanOpts po;
+  int rc = build_term_program(nqubits, p->terms, po.tile_bits_fwd, kRFwd, po.max_stage_slots, &p->prog,
+                              &p->direct);
+  if (rc != TCG_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return TCG_OK;
+}
+
+int tcg_mplan_destroy(tcg_mplan* plan) {
+  if (!plan) return TCG_OK;
+  program_free(&plan->prog);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (auto& kv : plan->dev) {
+    cudaSetDevice(kv.first);
+    cudaFree(kv.second.base);
+  }
+  cudaSetDevice(cur);
+  delete plan;
+  return TCG_OK;
+}
+
+int tcg_mplan_passes(const tcg_mplan* plan) {
+  if (!plan) return -1;
+  return (int)plan->prog.passes.size() + (int)plan->direct.size();
+}
+
+size_t tcg_expect_scratch_bytes(const tcg_mplan* plan, int64_t batch) {
+  if (!plan) return 0;
+  const size_t ntiles = size_t(1) << (plan->n - plan->prog.L);
+  const size_t nt = std::max(plan->nterms, 1);
+  return size_t(batch) * nt * (ntiles + kDirectBlocks) * sizeof(float2) + 512;
+}
+
+int tcg_expect_pauli(const tcg_mplan* plan, const void* psi, int64_t batch, double* out, void* scratch,
+                     size_t scratch_bytes, void* stream) {
+  if (!plan || !psi || !out || batch < 0) return TCG_ERR_INVALID_ARG;
+  if (batch == 0 || plan->nterms == 0) return TCG_OK;
+  if (!scratch || scratch_bytes < tcg_expect_scratch_bytes(plan, batch)) return TCG_ERR_SCRATCH;
+  tcg_mplan* p = const_cast<tcg_mplan*>(plan);
+  ProgramView view;
+  int rc = program_device_view(&p->prog, &view);
+  if (rc != TCG_OK) return rc;
+  tcg_mplan::Dev dv;
+  rc = mplan_device(p, &dv);
+  if (rc != TCG_OK) return rc;
+  const uint32_t ntiles = 1u << (plan->n - p->prog.L);
+  float2* part_tiles = static_cast<float2*>(scratch);
+  float2* part_direct = part_tiles + size_t(batch) * plan->nterms * ntiles;
+  cudaStream_t st = as_stream(stream);
+  if (!p->prog.passes.empty()) {
+    PassArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.prog = view;
+    a.n = plan->n;
+    a.psi = const_cast<float2*>(static_cast<const float2*>(psi));
+    a.partial = part_tiles;
+    a.part_stride = plan->nterms;
+    a.max_slots = std::max(p->prog.max_slots, 1);
+    for (int ps = 0; ps < (int)p->prog.passes.size(); ++ps) {
+      a.pass = ps;
+      rc = cuda_rc(launch_pass(MODE_MEAS, kRFwd, a, p->prog.L, batch, st));
+      if (rc != TCG_OK) return rc;
+    }
+    rc = cuda_rc(launch_reduce_partials(part_tiles, plan->nterms, ntiles, view.entries, view.nentries, batch,
+                                        nullptr, 0, out, plan->nterms, st));
+    if (rc != TCG_OK) return rc;
+  }
+  if (!p->direct.empty()) {
+    rc = cuda_rc(launch_direct_expect(static_cast<const float2*>(psi), plan->n, batch, dv.terms, dv.direct,
+                                      (int)p->direct.size(), plan->nterms, part_direct, kDirectBlocks, st));
+    if (rc != TCG_OK) return rc;
+    rc = cuda_rc(launch_reduce_partials(part_direct, plan->nterms, kDirectBlocks, dv.direct_entries,
+                                        (int64_t)p->direct.size(), batch, nullptr, 0, out, plan->nterms, st));
+  }
+  return rc;
+}
+
+int tcg_pauli_accumulate(const tcg_mplan* plan, const void* psi, void* mu, int64_t batch, const float* coef,
+                         int64_t coef_stride, void* stream) {
+  if (!plan || !psi || !mu || !coef || batch < 0) return TCG_ERR_INVALID_ARG;
+  if (batch == 0 || plan->nterms == 0) return TCG_OK;
+  tcg_mplan* p = const_cast<tcg_mplan*>(plan);
+  ProgramView view;
+  int rc = program_device_view(&p->prog, &view);
+  if (rc != TCG_OK) return rc;
+  tcg_mplan::Dev dv;
+  rc = mplan_device(p, &dv);
+  if (rc != TCG_OK) return rc;
+  cudaStream_t st = as_stream(stream);
+  if (!p->prog.passes.empty()) {
+    PassArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.prog = view;
+    a.n = plan->n;
+    a.psi = const_cast<float2*>(static_cast<const float2*>(psi));
+    a.mu = static_cast<float2*>(mu);
+    a.coef = coef;
+    a.coef_stride = coef_stride;
+    a.max_slots = 0;
+    for (int ps = 0; ps < (int)p->prog.passes.size(); ++ps) {
+      a.pass = ps;
+      rc = cuda_rc(launch_pass(MODE_PACC, kRFwd, a, p->prog.L, batch, st));
+      if (rc != TCG_OK) return rc;
+    }
+  }
+  if (!p->direct.empty())
+    rc = cuda_rc(launch_direct_pacc(static_cast<const float2*>(psi), static_cast<float2*>(mu), plan->n, batch,
+                                    dv.terms, dv.direct, (int)p->direct.size(), coef, coef_stride, st));
+  return rc;
+}
+
+size_t tcg_sample_scratch_bytes(int32_t nqubits, int64_t batch) {
+  if (nqubits < 1 || nqubits > kMaxQubits || batch < 0) return 0;
+  return sample_scratch_bytes(nqubits, batch) + 256;
+}
+
+int tcg_sample(const void* psi, int32_t nqubits, int64_t batch, const float* u, int64_t u_stride,
+               int64_t nshots, int64_t* out, void* scratch, size_t scratch_bytes, void* stream) {
+  if (!psi || nqubits < 1 || nqubits > kMaxQubits || batch < 0 || nshots < 0 || u_stride < 0)
+    return TCG_ERR_INVALID_ARG;
+  if (batch == 0 || nshots == 0) return TCG_OK;
+  if (!u || !out) return TCG_ERR_INVALID_ARG;
+  if (!scratch || scratch_bytes < tcg_sample_scratch_bytes(nqubits, batch)) return TCG_ERR_SCRATCH;
+  return cuda_rc(launch_sample(static_cast<const float2*>(psi), nqubits, batch, u, u_stride, nshots, out,
+                               scratch, as_stream(stream)));
+}
+
+int tcg_probability(const void* psi, int64_t len, float* p, void* stream) {
+  if (len < 0 || (len > 0 && (!psi || !p))) return TCG_ERR_INVALID_ARG;
+  return cuda_rc(launch_probability(static_cast<const float2*>(psi), len, p, as_stream(stream)));
+}
+
+size_t tcg_inner_scratch_bytes(int64_t len, int64_t batch) { return inner_scratch_bytes(len, batch) + 256; }
+
+int tcg_inner(const void* a, const void* b, int64_t len, int64_t batch, double* out, void* scratch,
+              size_t scratch_bytes, void* stream) {
+  if (!a || !b || !out || len <= 0 || batch < 0) return TCG_ERR_INVALID_ARG;
+  if (batch == 0) return TCG_OK;
+  if (!scratch || scratch_bytes < tcg_inner_scratch_bytes(len, batch)) return TCG_ERR_SCRATCH;
+  return cuda_rc(launch_inner(static_cast<const float2*>(a), static_cast<const float2*>(b), len, batch, out,
+                              scratch, as_stream(stream)));
+}
+
+int tcg_debug_program(const void* plan, int32_t which, const void** arrays, int64_t* counts, int64_t* sizes) {
+  if (!plan || !arrays || !counts || !sizes) return TCG_ERR_INVALID_ARG;
+  const Program* p = nullptr;
+  if (which == 0) p = &static_cast<const tcg_plan*>(plan)->fwd;
+  else if (which == 1) p = &static_cast<const tcg_plan*>(plan)->bwd;
+  else if (which == 2) p = &static_cast<const tcg_mplan*>(plan)->prog;
+  else return TCG_ERR_INVALID_ARG;
+  arrays[0] = p->passes.data();
+  arrays[1] = p->stages.data();
+  arrays[2] = p->ops.data();
+  arrays[3] = p->slot_out.data();
+  arrays[4] = p->runs.data();
+  counts[0] = (int64_t)p->passes.size();
+  counts[1] = (int64_t)p->stages.size();
+  counts[2] = (int64_t)p->ops.size();
+  counts[3] = (int64_t)p->slot_out.size();
+  counts[4] = (int64_t)p->runs.size();
+  sizes[0] = sizeof(DevPass);
+  sizes[1] = sizeof(DevStage);
+  sizes[2] = sizeof(DevOp);
+  sizes[3] = sizeof(SlotOut);
+  sizes[4] = sizeof(uint32_t);
+  return TCG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,90 @@
+// engine.h — internal data structures shared by the host planner (plan.cpp)
+// and the CUDA pass kernels (pass.cu).  Not part of the C ABI.
+//
+// Execution model.  A circuit's gate list is cut into PASSES.  A pass holds a
+// set of L "local" amplitude-index bits (the low LO bits always included, so
+// every tile is a set of 2^(L-LO) contiguous runs of 2^LO amplitudes); one CTA
+// owns one TILE = the 2^L amplitudes that differ only in the local bits, so a
+// pass reads and writes the state exactly once.  Inside a pass the gates run
+// in STAGES: a stage picks R of the L local bits as REGISTER bits, every thread
+// holds the 2^R amplitudes of one register group, and the stage's gates run on
+// those registers with no further memory traffic (dense gates on register
+// bits, diagonal gates on any bits, Pauli terms whose X/Y bits are register
+// bits).  Between two stages the tile goes through shared memory once to
+// change which bits are register bits.
+#pragma once
+#include <cstdint>
+
+namespace tcg {
+
+constexpr int kLo = 5;            // low index bits always local (256 B runs)
+constexpr int kMaxTileBits = 13;  // 2^13 amplitudes = 64 KiB per tile
+constexpr int kMaxPassBits = 20;  // non-local bits of one circuit (n <= 33)
+constexpr int kMinQubits = 6;     // smaller circuits are padded by the host
+constexpr int kMaxQubits = 32;
+
+// device op kinds
+enum OpKind : int32_t {
+  OP_DENSE1 = 0,   // 1-qubit dense on register position p0
+  OP_DENSE2 = 1,   // 2-qubit dense on register positions (p0 = sub-index MSB, p1)
+  OP_DIAG = 2,     // k-qubit diagonal on global bits gb[0..k-1] (gb[0] = MSB)
+  OP_DENSEK = 3,   // k-qubit dense on tile bits tb[0..k-1], run on the smem tile
+  OP_EXPECT = 4,   // Pauli term: acc += conj(psi[a]) s(a) psi[a ^ x]
+  OP_PACC = 5      // Pauli term: mu[a] += c s(a) psi[a ^ x]
+};
+
+// One device op, 48 bytes.
+struct DevOp {
+  int32_t kind;
+  int32_t k;
+  int32_t p[6];        // register positions (DENSE1/2), tile bits (DENSEK),
+                       // global bits (DIAG)
+  int32_t xreg;        // EXPECT/PACC: register-position mask of the X/Y bits
+  int32_t nY;          // EXPECT/PACC: number of Y factors (phase (-i)^nY)
+  uint32_t zmask;      // EXPECT/PACC: global Z/Y mask
+  int32_t slot;        // first accumulator slot in the stage (or -1)
+  int64_t mat_off;     // per-circuit matrix offset (complex entries); term id
+  int64_t grad_off;    // per-circuit gradient offset, -1 = none
+};
+
+struct DevStage {
+  int32_t R;             // register bits (<= template R of the kernel)
+  int32_t smem_stage;    // 1: ops run on the smem tile (OP_DENSEK only)
+  int32_t lanes_low;     // 1: lane bits are tile bits 0..4 in order
+  int32_t nthread_bits;  // L - R
+  int32_t reg_tile[6];   // tile bit of register bit i
+  int32_t thr_tile[16];  // tile bit of thread-id bit i
+  int32_t op_begin, op_end;
+  int32_t nslots;        // accumulator slots (complex) used by the stage
+  int32_t slot_out_begin, slot_out_end; // entries of pass slot->output map
+};
+
+struct DevPass {
+  int32_t L;                 // local bits
+  int32_t nnonlocal;         // n - L
+  int32_t lbits[kMaxTileBits];       // global bit of tile bit i
+  int32_t nlbits[kMaxQubits];        // global bits that are not local
+  int32_t stage_begin, stage_end;
+  int32_t runs_off;          // offset of the 2^(L-LO) run table in the program
+  int32_t pad;
+};
+
+// slot -> output mapping written at the end of each stage
+struct SlotOut {
+  int32_t slot;      // stage slot index
+  int32_t pad;
+  int64_t out_off;   // per-circuit output offset (complex entries)
+};
+
+// Whole device program of one plan direction, in one device allocation.
+struct ProgramView {
+  const DevPass* passes;
+  const DevStage* stages;
+  const DevOp* ops;
+  const SlotOut* slot_out;
+  const uint32_t* runs;   // run tables
+  const int64_t* entries; // distinct accumulator outputs, for the final reduce
+  int64_t nentries;
+};
+
+}  // namespace tcg

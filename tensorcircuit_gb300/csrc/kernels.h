@@ -1,0 +1,64 @@
+// kernels.h — launch interface between the C ABI (api.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "engine.h"
+#include "../../include/tcgb300.h"
+
+namespace tcg {
+
+enum { MODE_FWD = 0, MODE_BWD = 1, MODE_MEAS = 2, MODE_PACC = 3 };
+
+constexpr int kRFwd = 4;   // register bits of forward / measure kernels
+constexpr int kRBwd = 4;   // register bits of the adjoint kernel (psi + mu live)
+constexpr int kMaxThreads = 256;
+
+struct PassArgs {
+  ProgramView prog;
+  int pass;
+  int n;
+  float2* psi;              // [B][2^n]
+  float2* mu;               // [B][2^n] (BWD, PACC)
+  const float2* mats;       // [B][mat_stride]
+  int64_t mat_stride;
+  float2* partial;          // [B][part_stride][ntiles] accumulator partials
+  int64_t part_stride;
+  const float* coef;        // PACC: [B][coef_stride]
+  int64_t coef_stride;
+  int max_slots;
+};
+
+// every kernel launch of the library increments this counter
+void count_launch(int64_t n = 1);
+int64_t launch_count();
+
+cudaError_t launch_pass(int mode, int R, const PassArgs& a, int L, int64_t batch, cudaStream_t st);
+
+// partial[b][e][t] (complex64) summed over t in fp64 for the listed entries.
+// out_c64 (complex64) or out_c128 (complex128), one of them non-null.
+cudaError_t launch_reduce_partials(const float2* partial, int64_t part_stride, uint32_t ntiles,
+                                   const int64_t* entries_dev, int64_t nentries, int64_t batch,
+                                   float2* out_c64, int64_t out_stride_c64, double* out_c128,
+                                   int64_t out_stride_c128, cudaStream_t st);
+
+// Pauli terms with many X/Y bits, one global pass per term.
+cudaError_t launch_direct_expect(const float2* psi, int n, int64_t batch, const tcg_pauli* terms_dev,
+                                 const int* term_ids_dev, int nterms_direct, int64_t nterms_total,
+                                 float2* partial, uint32_t nblocks, cudaStream_t st);
+cudaError_t launch_direct_pacc(const float2* psi, float2* mu, int n, int64_t batch,
+                               const tcg_pauli* terms, const int* term_ids, int nterms_direct,
+                               const float* coef, int64_t coef_stride, cudaStream_t st);
+
+cudaError_t launch_probability(const float2* psi, int64_t len, float* p, cudaStream_t st);
+cudaError_t launch_inner(const float2* a, const float2* b, int64_t len, int64_t batch, double* out,
+                         void* scratch, cudaStream_t st);
+size_t inner_scratch_bytes(int64_t len, int64_t batch);
+
+// sampling
+size_t sample_scratch_bytes(int n, int64_t batch);
+cudaError_t launch_sample(const float2* psi, int n, int64_t batch, const float* u, int64_t u_stride,
+                          int64_t nshots, int64_t* out, void* scratch, cudaStream_t st);
+
+}  // namespace tcg

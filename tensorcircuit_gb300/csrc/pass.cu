@@ -1,0 +1,767 @@
+// pass.cu — the tile-pass kernels.
+//
+// One CTA = one tile = the 2^L amplitudes of one circuit that differ only in
+// the pass's local index bits.  The CTA reads its tile from HBM once, runs
+// every stage of the pass on it and writes it back once.  In a register stage
+// each of the 2^(L-R) threads holds the 2^R amplitudes spanned by the stage's
+// R register bits; gates on register bits are register-only arithmetic,
+// diagonal gates work on any bit through the amplitude's global index, and
+// the only shared-memory traffic is one transpose between stages whose
+// register bits differ.
+//
+// Modes (template MODE):
+//   FWD  : psi <- G_k ... G_1 psi                       (Circuit.wavefunction)
+//   BWD  : adjoint sweep over psi and mu: psi <- G^H psi, gradient slot
+//          += mu (x) conj(psi) over the gate's sub-indices, mu <- G^H mu
+//   MEAS : Pauli expectations, psi read only
+//   PACC : mu += c_t P_t psi, psi read only
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "engine.h"
+#include "kernels.h"
+
+namespace tcg {
+
+namespace {
+
+__device__ __forceinline__ uint32_t swz(uint32_t j) {
+  return j ^ (((j >> 5) ^ (j >> 10)) & 31u);
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * b + c
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)),
+                     fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+// a * conj(b) + c
+__device__ __forceinline__ float2 cfmac(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)),
+                     fmaf(a.y, b.x, fmaf(-a.x, b.y, c.y)));
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 czero() { return make_float2(0.f, 0.f); }
+
+__device__ __forceinline__ float2 ldm(const float2* p) {
+  return __ldg(reinterpret_cast<const float2*>(p));
+}
+
+// Sum over the lanes of a warp; blocks smaller than a warp (tiny tiles) use
+// only their nl = blockDim.x lanes.
+__device__ __forceinline__ float2 warp_sum(float2 v, int nl) {
+  const unsigned mask = nl >= 32 ? 0xffffffffu : ((1u << nl) - 1u);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    if (o < nl) {
+      v.x += __shfl_xor_sync(mask, v.x, o);
+      v.y += __shfl_xor_sync(mask, v.y, o);
+    }
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------- dense 1q
+template <int R, int P>
+__device__ __forceinline__ void dense1(float2 (&v)[1 << R], const float2 (&m)[4]) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    if (r & (1 << P)) continue;
+    const int r1 = r | (1 << P);
+    const float2 x0 = v[r], x1 = v[r1];
+    v[r] = cfma(m[0], x0, cmul(m[1], x1));
+    v[r1] = cfma(m[2], x0, cmul(m[3], x1));
+  }
+}
+
+// adjoint step for a 1q gate: a = M^H
+template <int R, int P, bool GRAD>
+__device__ __forceinline__ void dense1_bwd(float2 (&v)[1 << R], float2 (&w)[1 << R],
+                                           const float2 (&a)[4], float2 (&acc)[16]) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    if (r & (1 << P)) continue;
+    const int r1 = r | (1 << P);
+    const float2 x0 = v[r], x1 = v[r1];
+    const float2 y0 = cfma(a[0], x0, cmul(a[1], x1));
+    const float2 y1 = cfma(a[2], x0, cmul(a[3], x1));
+    v[r] = y0;
+    v[r1] = y1;
+    const float2 u0 = w[r], u1 = w[r1];
+    if (GRAD) {
+      acc[0] = cfmac(u0, y0, acc[0]);
+      acc[1] = cfmac(u0, y1, acc[1]);
+      acc[2] = cfmac(u1, y0, acc[2]);
+      acc[3] = cfmac(u1, y1, acc[3]);
+    }
+    w[r] = cfma(a[0], u0, cmul(a[1], u1));
+    w[r1] = cfma(a[2], u0, cmul(a[3], u1));
+  }
+}
+
+// ---------------------------------------------------------------- dense 2q
+template <int R, int P0, int P1>
+__device__ __forceinline__ void dense2(float2 (&v)[1 << R], const float2 (&m)[16]) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    if (r & ((1 << P0) | (1 << P1))) continue;
+    const int i0 = r, i1 = r | (1 << P1), i2 = r | (1 << P0), i3 = r | (1 << P0) | (1 << P1);
+    const float2 x0 = v[i0], x1 = v[i1], x2 = v[i2], x3 = v[i3];
+    v[i0] = cfma(m[0], x0, cfma(m[1], x1, cfma(m[2], x2, cmul(m[3], x3))));
+    v[i1] = cfma(m[4], x0, cfma(m[5], x1, cfma(m[6], x2, cmul(m[7], x3))));
+    v[i2] = cfma(m[8], x0, cfma(m[9], x1, cfma(m[10], x2, cmul(m[11], x3))));
+    v[i3] = cfma(m[12], x0, cfma(m[13], x1, cfma(m[14], x2, cmul(m[15], x3))));
+  }
+}
+
+template <int R, int P0, int P1, bool GRAD>
+__device__ __forceinline__ void dense2_bwd(float2 (&v)[1 << R], float2 (&w)[1 << R],
+                                           const float2 (&a)[16], float2 (&acc)[16]) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    if (r & ((1 << P0) | (1 << P1))) continue;
+    const int idx[4] = {r, r | (1 << P1), r | (1 << P0), r | (1 << P0) | (1 << P1)};
+    float2 y[4], u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      y[i] = cfma(a[4 * i + 0], v[idx[0]],
+                  cfma(a[4 * i + 1], v[idx[1]],
+                       cfma(a[4 * i + 2], v[idx[2]], cmul(a[4 * i + 3], v[idx[3]]))));
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      v[idx[i]] = y[i];
+      u[i] = w[idx[i]];
+    }
+    if (GRAD) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[4 * i + j] = cfmac(u[i], y[j], acc[4 * i + j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      w[idx[i]] = cfma(a[4 * i + 0], u[0],
+                       cfma(a[4 * i + 1], u[1], cfma(a[4 * i + 2], u[2], cmul(a[4 * i + 3], u[3]))));
+    }
+  }
+}
+
+// switch helpers --------------------------------------------------------------
+template <int R>
+__device__ __forceinline__ void dispatch_dense1(int p, float2 (&v)[1 << R], const float2 (&m)[4]) {
+  switch (p) {
+    case 0: dense1<R, 0>(v, m); break;
+    case 1: if (R > 1) dense1<R, (R > 1 ? 1 : 0)>(v, m); break;
+    case 2: if (R > 2) dense1<R, (R > 2 ? 2 : 0)>(v, m); break;
+    case 3: if (R > 3) dense1<R, (R > 3 ? 3 : 0)>(v, m); break;
+    case 4: if (R > 4) dense1<R, (R > 4 ? 4 : 0)>(v, m); break;
+    default: break;
+  }
+}
+
+template <int R, bool G>
+__device__ __forceinline__ void dispatch_dense1_bwd(int p, float2 (&v)[1 << R], float2 (&w)[1 << R],
+                                                    const float2 (&a)[4], float2 (&acc)[16]) {
+  switch (p) {
+    case 0: dense1_bwd<R, 0, G>(v, w, a, acc); break;
+    case 1: if (R > 1) dense1_bwd<R, (R > 1 ? 1 : 0), G>(v, w, a, acc); break;
+    case 2: if (R > 2) dense1_bwd<R, (R > 2 ? 2 : 0), G>(v, w, a, acc); break;
+    case 3: if (R > 3) dense1_bwd<R, (R > 3 ? 3 : 0), G>(v, w, a, acc); break;
+    case 4: if (R > 4) dense1_bwd<R, (R > 4 ? 4 : 0), G>(v, w, a, acc); break;
+    default: break;
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void dispatch_dense2(int p0, int p1, float2 (&v)[1 << R],
+                                                const float2 (&m)[16]) {
+#define TCG_D2(P0, P1)                                                               \
+  case (P0) * 8 + (P1):                                                              \
+    if ((P0) < R && (P1) < R) dense2<R, ((P0) < R ? (P0) : 0), ((P1) < R ? (P1) : 1)>(v, m); \
+    break;
+  switch (p0 * 8 + p1) {
+    TCG_D2(0, 1) TCG_D2(0, 2) TCG_D2(0, 3) TCG_D2(0, 4)
+    TCG_D2(1, 0) TCG_D2(1, 2) TCG_D2(1, 3) TCG_D2(1, 4)
+    TCG_D2(2, 0) TCG_D2(2, 1) TCG_D2(2, 3) TCG_D2(2, 4)
+    TCG_D2(3, 0) TCG_D2(3, 1) TCG_D2(3, 2) TCG_D2(3, 4)
+    TCG_D2(4, 0) TCG_D2(4, 1) TCG_D2(4, 2) TCG_D2(4, 3)
+    default: break;
+  }
+#undef TCG_D2
+}
+
+template <int R, bool G>
+__device__ __forceinline__ void dispatch_dense2_bwd(int p0, int p1, float2 (&v)[1 << R],
+                                                    float2 (&w)[1 << R], const float2 (&a)[16],
+                                                    float2 (&acc)[16]) {
+#define TCG_D2B(P0, P1)                                                                 \
+  case (P0) * 8 + (P1):                                                                 \
+    if ((P0) < R && (P1) < R)                                                           \
+      dense2_bwd<R, ((P0) < R ? (P0) : 0), ((P1) < R ? (P1) : 1), G>(v, w, a, acc);    \
+    break;
+  switch (p0 * 8 + p1) {
+    TCG_D2B(0, 1) TCG_D2B(0, 2) TCG_D2B(0, 3) TCG_D2B(0, 4)
+    TCG_D2B(1, 0) TCG_D2B(1, 2) TCG_D2B(1, 3) TCG_D2B(1, 4)
+    TCG_D2B(2, 0) TCG_D2B(2, 1) TCG_D2B(2, 3) TCG_D2B(2, 4)
+    TCG_D2B(3, 0) TCG_D2B(3, 1) TCG_D2B(3, 2) TCG_D2B(3, 4)
+    TCG_D2B(4, 0) TCG_D2B(4, 1) TCG_D2B(4, 2) TCG_D2B(4, 3)
+    default: break;
+  }
+#undef TCG_D2B
+}
+
+// ---------------------------------------------------------------- Pauli terms
+// acc += sum_r conj(v[r]) s(r) v[r ^ X], s(r) = (-1)^(sbase ^ popc(r & zr))
+template <int R, int X>
+__device__ __forceinline__ float2 expect_x(const float2 (&v)[1 << R], int sbase, int zr) {
+  float2 acc = czero();
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    const float2 t = v[r ^ X];
+    const float2 c = make_float2(fmaf(v[r].x, t.x, v[r].y * t.y), fmaf(v[r].x, t.y, -v[r].y * t.x));
+    const int s = (sbase ^ __popc(r & zr)) & 1;
+    acc.x += s ? -c.x : c.x;
+    acc.y += s ? -c.y : c.y;
+  }
+  return acc;
+}
+
+// w[r] += cf * s(r) * v[r ^ X]   (cf complex, includes (-i)^nY and the coefficient)
+template <int R, int X>
+__device__ __forceinline__ void pacc_x(const float2 (&v)[1 << R], float2 (&w)[1 << R], float2 cf,
+                                       int sbase, int zr) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    const int s = (sbase ^ __popc(r & zr)) & 1;
+    const float2 c = s ? make_float2(-cf.x, -cf.y) : cf;
+    w[r] = cfma(c, v[r ^ X], w[r]);
+  }
+}
+
+// Terms reaching the register path have at most two X/Y bits (the planner
+// sends wider ones to the plain kernel), so 16 compiled patterns cover them.
+#define TCG_XCASES(M)                                                      \
+  M(0) M(1) M(2) M(4) M(8) M(16) M(3) M(5) M(9) M(17) M(6) M(10) M(18) M(12) \
+  M(20) M(24)
+
+template <int R>
+__device__ __forceinline__ float2 dispatch_expect(int x, const float2 (&v)[1 << R], int sbase, int zr) {
+  float2 r = czero();
+#define TCG_EX(XX) case XX: if ((XX) < (1 << R)) r = expect_x<R, ((XX) < (1 << R) ? (XX) : 0)>(v, sbase, zr); break;
+  switch (x) {
+    TCG_XCASES(TCG_EX)
+    default: break;
+  }
+#undef TCG_EX
+  return r;
+}
+
+template <int R>
+__device__ __forceinline__ void dispatch_pacc(int x, const float2 (&v)[1 << R], float2 (&w)[1 << R],
+                                              float2 cf, int sbase, int zr) {
+#define TCG_PA(XX) case XX: if ((XX) < (1 << R)) pacc_x<R, ((XX) < (1 << R) ? (XX) : 0)>(v, w, cf, sbase, zr); break;
+  switch (x) {
+    TCG_XCASES(TCG_PA)
+    default: break;
+  }
+#undef TCG_PA
+}
+
+// (-i)^nY
+__device__ __forceinline__ float2 ypow(int nY) {
+  switch (nY & 3) {
+    case 0: return make_float2(1.f, 0.f);
+    case 1: return make_float2(0.f, -1.f);
+    case 2: return make_float2(-1.f, 0.f);
+    default: return make_float2(0.f, 1.f);
+  }
+}
+
+// ---------------------------------------------------------------- smem dense k
+template <int K>
+__device__ void denseK_smem(float2* tile, int L, const int* tb, const float2* m, bool adj,
+                            int tid, int nthreads) {
+  constexpr int D = 1 << K;
+  const uint32_t ngroups = 1u << (L - K);
+  // sorted tile bits for zero insertion
+  int srt[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) srt[i] = tb[i];
+#pragma unroll
+  for (int i = 0; i < K; ++i)
+#pragma unroll
+    for (int j = 0; j + 1 < K - i; ++j)
+      if (srt[j] > srt[j + 1]) { int t = srt[j]; srt[j] = srt[j + 1]; srt[j + 1] = t; }
+  for (uint32_t g = tid; g < ngroups; g += nthreads) {
+    uint32_t j0 = g;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const uint32_t lowm = (1u << srt[i]) - 1u;
+      j0 = ((j0 & ~lowm) << 1) | (j0 & lowm);
+    }
+    float2 x[D];
+#pragma unroll
+    for (int s = 0; s < D; ++s) {
+      uint32_t j = j0;
+#pragma unroll
+      for (int i = 0; i < K; ++i)
+        if ((s >> (K - 1 - i)) & 1) j |= 1u << tb[i];
+      x[s] = tile[swz(j)];
+    }
+#pragma unroll
+    for (int s = 0; s < D; ++s) {
+      float2 y = czero();
+#pragma unroll 8
+      for (int t = 0; t < D; ++t) {
+        const float2 e = adj ? cconj(ldm(m + t * D + s)) : ldm(m + s * D + t);
+        y = cfma(e, x[t], y);
+      }
+      uint32_t j = j0;
+#pragma unroll
+      for (int i = 0; i < K; ++i)
+        if ((s >> (K - 1 - i)) & 1) j |= 1u << tb[i];
+      tile[swz(j)] = y;
+    }
+  }
+}
+
+__device__ void dispatch_denseK(int k, float2* tile, int L, const int* tb, const float2* m, bool adj,
+                                int tid, int nthreads) {
+  switch (k) {
+    case 1: denseK_smem<1>(tile, L, tb, m, adj, tid, nthreads); break;
+    case 2: denseK_smem<2>(tile, L, tb, m, adj, tid, nthreads); break;
+    case 3: denseK_smem<3>(tile, L, tb, m, adj, tid, nthreads); break;
+    case 4: denseK_smem<4>(tile, L, tb, m, adj, tid, nthreads); break;
+    case 5: denseK_smem<5>(tile, L, tb, m, adj, tid, nthreads); break;
+    case 6: denseK_smem<6>(tile, L, tb, m, adj, tid, nthreads); break;
+    default: break;
+  }
+}
+
+// ------------------------------------------------------------------ tile I/O
+__device__ __forceinline__ void tile_load_smem(float2* sm, const float2* __restrict__ src, uint32_t base,
+                                               const uint32_t* runs, int L, int tid, int nthreads) {
+  const uint32_t half = 1u << (L - 1);
+  for (uint32_t i = tid; i < half; i += nthreads) {
+    const uint32_t j = 2 * i;
+    const uint32_t off = __ldg(runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
+    const float4 q = __ldg(reinterpret_cast<const float4*>(src + (base | off)));
+    sm[swz(j)] = make_float2(q.x, q.y);
+    sm[swz(j + 1)] = make_float2(q.z, q.w);
+  }
+}
+
+__device__ __forceinline__ void tile_store_smem(const float2* sm, float2* __restrict__ dst, uint32_t base,
+                                                const uint32_t* runs, int L, int tid, int nthreads) {
+  const uint32_t half = 1u << (L - 1);
+  for (uint32_t i = tid; i < half; i += nthreads) {
+    const uint32_t j = 2 * i;
+    const uint32_t off = __ldg(runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
+    const float2 a = sm[swz(j)], b = sm[swz(j + 1)];
+    *reinterpret_cast<float4*>(dst + (base | off)) = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+struct Layout {
+  uint32_t jt;      // tile offset of this thread's group
+  uint32_t gt;      // global offset (local bits) of this thread's group
+  uint32_t rt[6];   // tile offset of register bit i
+  uint32_t rg[6];   // global offset of register bit i
+};
+
+template <int R>
+__device__ __forceinline__ void make_layout(Layout& ly, const DevStage& S, const DevPass& P, int tid) {
+  ly.jt = 0;
+  ly.gt = 0;
+  for (int i = 0; i < S.nthread_bits; ++i) {
+    if ((tid >> i) & 1) {
+      const int t = S.thr_tile[i];
+      ly.jt |= 1u << t;
+      ly.gt |= 1u << P.lbits[t];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int t = S.reg_tile[i];
+    ly.rt[i] = 1u << t;
+    ly.rg[i] = 1u << P.lbits[t];
+  }
+}
+
+template <int R>
+__device__ __forceinline__ uint32_t roff(const Layout& ly, int r, bool global) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int i = 0; i < R; ++i)
+    if ((r >> i) & 1) o |= global ? ly.rg[i] : ly.rt[i];
+  return o;
+}
+
+template <int R>
+__device__ __forceinline__ void regs_from_smem(float2 (&v)[1 << R], const float2* sm, const Layout& ly) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) v[r] = sm[swz(ly.jt | roff<R>(ly, r, false))];
+}
+template <int R>
+__device__ __forceinline__ void regs_to_smem(const float2 (&v)[1 << R], float2* sm, const Layout& ly) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) sm[swz(ly.jt | roff<R>(ly, r, false))] = v[r];
+}
+template <int R>
+__device__ __forceinline__ void regs_from_global(float2 (&v)[1 << R], const float2* __restrict__ src,
+                                                 uint32_t base, const Layout& ly) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) v[r] = __ldg(src + (base | ly.gt | roff<R>(ly, r, true)));
+}
+template <int R>
+__device__ __forceinline__ void regs_to_global(const float2 (&v)[1 << R], float2* __restrict__ dst,
+                                               uint32_t base, const Layout& ly) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) dst[base | ly.gt | roff<R>(ly, r, true)] = v[r];
+}
+
+__device__ __forceinline__ bool same_layout(const DevStage& a, const DevStage& b) {
+  if (a.smem_stage || b.smem_stage || a.R != b.R || a.nthread_bits != b.nthread_bits) return false;
+  for (int i = 0; i < a.R; ++i)
+    if (a.reg_tile[i] != b.reg_tile[i]) return false;
+  for (int i = 0; i < a.nthread_bits; ++i)
+    if (a.thr_tile[i] != b.thr_tile[i]) return false;
+  return true;
+}
+
+}  // namespace
+
+// ============================================================================
+template <int MODE, int R>
+__global__ void __launch_bounds__(256, 1) pass_kernel(PassArgs A) {
+  constexpr int NR = 1 << R;
+  constexpr bool HAS_MU = (MODE == MODE_BWD || MODE == MODE_PACC);
+  constexpr bool STORE_PSI = (MODE == MODE_FWD || MODE == MODE_BWD);
+  constexpr bool STORE_MU = HAS_MU;
+  extern __shared__ __align__(16) float2 smem_raw[];
+
+  const DevPass& P = A.prog.passes[A.pass];
+  const int L = P.L;
+  const int tid = threadIdx.x;
+  const int nthreads = blockDim.x;
+  const int warp = tid >> 5;
+  const int lane = tid & 31;
+  const int nwarps = (nthreads + 31) >> 5;
+  const int nl = nthreads < 32 ? nthreads : 32;
+  const uint32_t tile = blockIdx.x;
+  const int64_t b = blockIdx.y;
+  const uint32_t ntiles = gridDim.x;
+
+  float2* sm_psi = smem_raw;
+  float2* sm_mu = smem_raw + (HAS_MU ? (1u << L) : 0u);
+  float2* sm_slot = smem_raw + (HAS_MU ? 2u : 1u) * (1u << L);
+
+  uint32_t base = 0;
+  for (int i = 0; i < P.nnonlocal; ++i)
+    if ((tile >> i) & 1u) base |= 1u << P.nlbits[i];
+
+  const size_t state_len = size_t(1) << A.n;
+  float2* psi = A.psi + b * state_len;
+  float2* mu = HAS_MU ? (A.mu + b * state_len) : nullptr;
+  const float2* mats = A.mats ? (A.mats + b * A.mat_stride) : nullptr;
+  const uint32_t* runs = A.prog.runs + P.runs_off;
+
+  float2 v[NR];
+  float2 w[NR];  // mu registers; dead (and removed) in modes without mu
+  bool live = false;     // registers hold the tile
+  bool in_smem = false;  // smem holds the tile
+  int prev = -1;
+  Layout ly;
+
+  for (int s = P.stage_begin; s < P.stage_end; ++s) {
+    const DevStage& S = A.prog.stages[s];
+    if (S.smem_stage) {
+      if (live) {
+        regs_to_smem<R>(v, sm_psi, ly);
+        if (HAS_MU) regs_to_smem<R>(w, sm_mu, ly);
+        live = false;
+      } else if (!in_smem) {
+        tile_load_smem(sm_psi, psi, base, runs, L, tid, nthreads);
+        if (HAS_MU) tile_load_smem(sm_mu, mu, base, runs, L, tid, nthreads);
+      }
+      in_smem = true;
+      __syncthreads();
+      for (int o = S.op_begin; o < S.op_end; ++o) {
+        const DevOp& op = A.prog.ops[o];
+        const float2* m = mats + op.mat_off;
+        if (MODE == MODE_FWD) {
+          dispatch_denseK(op.k, sm_psi, L, op.p, m, false, tid, nthreads);
+        } else if (MODE == MODE_BWD) {
+          dispatch_denseK(op.k, sm_psi, L, op.p, m, true, tid, nthreads);
+          dispatch_denseK(op.k, sm_mu, L, op.p, m, true, tid, nthreads);
+        }
+        __syncthreads();
+      }
+      prev = s;
+      continue;
+    }
+
+    // ---- register stage: bring the tile into registers in this layout
+    if (!live) {
+      make_layout<R>(ly, S, P, tid);
+      if (in_smem) {
+        regs_from_smem<R>(v, sm_psi, ly);
+        if (HAS_MU) regs_from_smem<R>(w, sm_mu, ly);
+        __syncthreads();
+      } else if (S.lanes_low) {
+        regs_from_global<R>(v, psi, base, ly);
+        if (HAS_MU) regs_from_global<R>(w, mu, base, ly);
+      } else {
+        tile_load_smem(sm_psi, psi, base, runs, L, tid, nthreads);
+        if (HAS_MU) tile_load_smem(sm_mu, mu, base, runs, L, tid, nthreads);
+        __syncthreads();
+        regs_from_smem<R>(v, sm_psi, ly);
+        if (HAS_MU) regs_from_smem<R>(w, sm_mu, ly);
+        __syncthreads();
+      }
+      live = true;
+      in_smem = false;
+    } else if (!same_layout(A.prog.stages[prev], S)) {
+      regs_to_smem<R>(v, sm_psi, ly);
+      if (HAS_MU) regs_to_smem<R>(w, sm_mu, ly);
+      __syncthreads();
+      make_layout<R>(ly, S, P, tid);
+      regs_from_smem<R>(v, sm_psi, ly);
+      if (HAS_MU) regs_from_smem<R>(w, sm_mu, ly);
+      __syncthreads();
+    }
+    const uint32_t gthr = base | ly.gt;  // global index of register 0
+
+    // ---- ops
+    for (int o = S.op_begin; o < S.op_end; ++o) {
+      const DevOp& op = A.prog.ops[o];
+      const int kind = op.kind;
+      if (kind == OP_DENSE1) {
+        const float2* m = mats + op.mat_off;
+        if (MODE == MODE_FWD) {
+          const float2 mm[4] = {ldm(m), ldm(m + 1), ldm(m + 2), ldm(m + 3)};
+          dispatch_dense1<R>(op.p[0], v, mm);
+        } else if (MODE == MODE_BWD) {
+          const float2 a[4] = {cconj(ldm(m)), cconj(ldm(m + 2)), cconj(ldm(m + 1)), cconj(ldm(m + 3))};
+          float2 acc[16];
+#pragma unroll
+          for (int e = 0; e < 16; ++e) acc[e] = czero();
+          if (op.slot >= 0) {
+            dispatch_dense1_bwd<R, true>(op.p[0], v, w, a, acc);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float2 t = warp_sum(acc[e], nl);
+              if (lane == 0) sm_slot[warp * A.max_slots + op.slot + e] = t;
+            }
+          } else {
+            dispatch_dense1_bwd<R, false>(op.p[0], v, w, a, acc);
+          }
+        }
+      } else if (kind == OP_DENSE2) {
+        const float2* m = mats + op.mat_off;
+        if (MODE == MODE_FWD) {
+          float2 mm[16];
+#pragma unroll
+          for (int e = 0; e < 16; ++e) mm[e] = ldm(m + e);
+          dispatch_dense2<R>(op.p[0], op.p[1], v, mm);
+        } else if (MODE == MODE_BWD) {
+          float2 a[16];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) a[4 * i + j] = cconj(ldm(m + 4 * j + i));
+          float2 acc[16];
+#pragma unroll
+          for (int e = 0; e < 16; ++e) acc[e] = czero();
+          if (op.slot >= 0) {
+            dispatch_dense2_bwd<R, true>(op.p[0], op.p[1], v, w, a, acc);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+              const float2 t = warp_sum(acc[e], nl);
+              if (lane == 0) sm_slot[warp * A.max_slots + op.slot + e] = t;
+            }
+          } else {
+            dispatch_dense2_bwd<R, false>(op.p[0], op.p[1], v, w, a, acc);
+          }
+        }
+      } else if (kind == OP_DIAG) {
+        const float2* m = mats + op.mat_off;
+        const int k = op.k;
+        // index contribution of the fixed part and of each register bit
+        int idx_t = 0;
+        for (int i = 0; i < k; ++i) idx_t |= ((gthr >> op.p[i]) & 1u) << (k - 1 - i);
+        int dbit[R];
+#pragma unroll
+        for (int ri = 0; ri < R; ++ri) {
+          int d = 0;
+          for (int i = 0; i < k; ++i)
+            if (ly.rg[ri] == (1u << op.p[i])) d = 1 << (k - 1 - i);
+          dbit[ri] = d;
+        }
+        if (k <= 2) {
+          float2 d4[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) d4[e] = (e < (1 << k)) ? ldm(m + e) : czero();
+          if (MODE == MODE_FWD) {
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+              int idx = idx_t;
+#pragma unroll
+              for (int ri = 0; ri < R; ++ri)
+                if ((r >> ri) & 1) idx ^= dbit[ri];
+              const float2 d = (idx == 0) ? d4[0] : (idx == 1) ? d4[1] : (idx == 2) ? d4[2] : d4[3];
+              v[r] = cmul(d, v[r]);
+            }
+          } else if (MODE == MODE_BWD) {
+            float2 acc[4] = {czero(), czero(), czero(), czero()};
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+              int idx = idx_t;
+#pragma unroll
+              for (int ri = 0; ri < R; ++ri)
+                if ((r >> ri) & 1) idx ^= dbit[ri];
+              const float2 d = cconj((idx == 0) ? d4[0] : (idx == 1) ? d4[1] : (idx == 2) ? d4[2] : d4[3]);
+              const float2 y = cmul(d, v[r]);
+              v[r] = y;
+              const float2 u = w[r];
+              const float2 g = make_float2(fmaf(u.x, y.x, u.y * y.y), fmaf(u.y, y.x, -u.x * y.y));
+              acc[0].x += (idx == 0) ? g.x : 0.f; acc[0].y += (idx == 0) ? g.y : 0.f;
+              acc[1].x += (idx == 1) ? g.x : 0.f; acc[1].y += (idx == 1) ? g.y : 0.f;
+              acc[2].x += (idx == 2) ? g.x : 0.f; acc[2].y += (idx == 2) ? g.y : 0.f;
+              acc[3].x += (idx == 3) ? g.x : 0.f; acc[3].y += (idx == 3) ? g.y : 0.f;
+              w[r] = cmul(d, u);
+            }
+            if (op.slot >= 0) {
+              for (int e = 0; e < (1 << k); ++e) {
+                const float2 t = warp_sum(acc[e], nl);
+                if (lane == 0) sm_slot[warp * A.max_slots + op.slot + e] = t;
+              }
+            }
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < NR; ++r) {
+            int idx = idx_t;
+#pragma unroll
+            for (int ri = 0; ri < R; ++ri)
+              if ((r >> ri) & 1) idx ^= dbit[ri];
+            if (MODE == MODE_FWD) {
+              v[r] = cmul(ldm(m + idx), v[r]);
+            } else if (MODE == MODE_BWD) {
+              const float2 d = cconj(ldm(m + idx));
+              v[r] = cmul(d, v[r]);
+              w[r] = cmul(d, w[r]);
+            }
+          }
+        }
+      } else if (kind == OP_EXPECT) {
+        // sign bits: fixed part parity and register bits inside zmask
+        const int sbase = __popc(gthr & op.zmask) & 1;
+        int zr = 0;
+#pragma unroll
+        for (int ri = 0; ri < R; ++ri)
+          if (ly.rg[ri] & op.zmask) zr |= 1 << ri;
+        if (MODE == MODE_MEAS) {
+          float2 acc = dispatch_expect<R>(op.xreg, v, sbase, zr);
+          acc = cmul(ypow(op.nY), acc);
+          acc = warp_sum(acc, nl);
+          if (lane == 0) sm_slot[warp * A.max_slots + op.slot] = acc;
+        } else if (MODE == MODE_PACC) {
+          const float c = A.coef[b * A.coef_stride + op.mat_off];
+          const float2 y = ypow(op.nY);
+          const float2 cf = make_float2(c * y.x, c * y.y);
+          dispatch_pacc<R>(op.xreg, v, w, cf, sbase, zr);
+        }
+      }
+    }
+
+    // ---- flush accumulator slots of this stage (fixed order over warps)
+    if ((MODE == MODE_BWD || MODE == MODE_MEAS) && S.nslots > 0) {
+      __syncthreads();
+      for (int e = S.slot_out_begin + tid; e < S.slot_out_end; e += nthreads) {
+        const SlotOut so = A.prog.slot_out[e];
+        float2 t = czero();
+        for (int q = 0; q < nwarps; ++q) {
+          const float2 x = sm_slot[q * A.max_slots + so.slot];
+          t.x += x.x;
+          t.y += x.y;
+        }
+        A.partial[(size_t(b) * A.part_stride + so.out_off) * ntiles + tile] = t;
+      }
+      __syncthreads();
+    }
+    prev = s;
+  }
+
+  // ---- write the tile back
+  if (STORE_PSI || STORE_MU) {
+    if (live) {
+      const DevStage& S = A.prog.stages[prev];
+      if (S.lanes_low) {
+        if (STORE_PSI) regs_to_global<R>(v, psi, base, ly);
+        if (STORE_MU) regs_to_global<R>(w, mu, base, ly);
+      } else {
+        if (STORE_PSI) regs_to_smem<R>(v, sm_psi, ly);
+        if (STORE_MU) regs_to_smem<R>(w, sm_mu, ly);
+        __syncthreads();
+        if (STORE_PSI) tile_store_smem(sm_psi, psi, base, runs, L, tid, nthreads);
+        if (STORE_MU) tile_store_smem(sm_mu, mu, base, runs, L, tid, nthreads);
+      }
+    } else if (in_smem) {
+      if (STORE_PSI) tile_store_smem(sm_psi, psi, base, runs, L, tid, nthreads);
+      if (STORE_MU) tile_store_smem(sm_mu, mu, base, runs, L, tid, nthreads);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- launchers
+template <int MODE, int R>
+static cudaError_t launch_one(const PassArgs& a, int L, int64_t batch, cudaStream_t st) {
+  const int nthreads = 1 << (L - R);
+  const bool has_mu = (MODE == MODE_BWD || MODE == MODE_PACC);
+  const int nwarps = (nthreads + 31) / 32;
+  const size_t smem = size_t(has_mu ? 2 : 1) * (size_t(1) << L) * sizeof(float2) +
+                      size_t(nwarps) * a.max_slots * sizeof(float2);
+  if (nthreads > kMaxThreads) return cudaErrorInvalidValue;
+  // the opt-in shared-memory size is a per-device function attribute: raise
+  // it once per device to the largest size seen
+  static int attr_smem[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 64 && attr_smem[dev] < (int)smem) {
+    e = cudaFuncSetAttribute(pass_kernel<MODE, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_smem[dev] = (int)smem;
+  }
+  const uint32_t ntiles = 1u << (a.n - L);
+  for (int64_t b0 = 0; b0 < batch; b0 += 65535) {
+    const int64_t nb = (batch - b0) < 65535 ? (batch - b0) : 65535;
+    PassArgs aa = a;
+    const size_t len = size_t(1) << a.n;
+    aa.psi = a.psi + b0 * len;
+    if (aa.mu) aa.mu = a.mu + b0 * len;
+    if (aa.mats) aa.mats = a.mats + b0 * a.mat_stride;
+    if (aa.coef) aa.coef = a.coef + b0 * a.coef_stride;
+    if (aa.partial) aa.partial = a.partial + size_t(b0) * a.part_stride * ntiles;
+    dim3 grid(ntiles, (unsigned)nb);
+    count_launch();
+    pass_kernel<MODE, R><<<grid, nthreads, smem, st>>>(aa);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_pass(int mode, int R, const PassArgs& a, int L, int64_t batch, cudaStream_t st) {
+  if (mode == MODE_FWD && R == 4) return launch_one<MODE_FWD, 4>(a, L, batch, st);
+  if (mode == MODE_BWD && R == 4) return launch_one<MODE_BWD, 4>(a, L, batch, st);
+  if (mode == MODE_MEAS && R == 4) return launch_one<MODE_MEAS, 4>(a, L, batch, st);
+  if (mode == MODE_PACC && R == 4) return launch_one<MODE_PACC, 4>(a, L, batch, st);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace tcg

@@ -1,0 +1,500 @@
+// plan.cpp — host planner.  Cuts an ordered gate list into HBM passes (each a
+// set of L local index bits, one CTA per 2^L-amplitude tile) and each pass
+// into register stages (R register bits per thread), then flattens the result
+// into the device program the pass kernels read.
+//
+// The reference has no counterpart: it contracts a tensor network with an
+// opt_einsum greedy path (tensorcircuit/cons.py:523-631).  What must agree is
+// the result, i.e. gates are applied in circuit order on the big-endian state
+// (tensorcircuit/basecircuit.py:120-245).
+#include "plan.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+namespace tcg {
+
+namespace {
+
+inline int popc64(uint64_t v) { return __builtin_popcountll(v); }
+
+uint64_t gate_mask(const PGate& g) {
+  uint64_t m = 0;
+  for (int i = 0; i < g.k; ++i) m |= 1ull << g.gbits[i];
+  return m;
+}
+
+// phys-bank position a tile bit flips under the smem swizzle
+// phys(j) = j ^ (((j >> 5) ^ (j >> 10)) & 31)  (see pass.cu)
+inline int bankpos(int t) { return t < 5 ? t : (t < 10 ? t - 5 : t - 10); }
+
+struct StageDraft {
+  bool smem = false;
+  uint32_t rset = 0;  // tile-bit mask of register bits
+  std::vector<int> ops;  // indices into the pass op drafts
+  int slots = 0;
+};
+
+struct OpDraft {
+  int kind;
+  int k;
+  int gbits[6];
+  int64_t mat_off;
+  int64_t grad_off;
+  // term ops
+  uint64_t x = 0, z = 0;
+  int term = -1;
+};
+
+// Complete a stage: pad the register set, choose thread-bit order, encode ops.
+int emit_stage(Program* P, DevPass& dp, const StageDraft& sd,
+               const std::vector<OpDraft>& od, const int* tile_of_gbit,
+               int L, int R, bool prefer_high_pad) {
+  DevStage st;
+  std::memset(&st, 0, sizeof(st));
+  st.op_begin = (int)P->ops.size();
+  st.slot_out_begin = (int)P->slot_out.size();
+  if (sd.smem) {
+    st.smem_stage = 1;
+    st.R = 0;
+    st.nthread_bits = 0;
+    for (int oi : sd.ops) {
+      const OpDraft& o = od[oi];
+      DevOp d;
+      std::memset(&d, 0, sizeof(d));
+      d.kind = OP_DENSEK;
+      d.k = o.k;
+      for (int i = 0; i < o.k; ++i) d.p[i] = tile_of_gbit[o.gbits[i]];
+      d.slot = -1;
+      d.mat_off = o.mat_off;
+      d.grad_off = -1;
+      P->ops.push_back(d);
+    }
+    st.op_end = (int)P->ops.size();
+    st.slot_out_end = (int)P->slot_out.size();
+    P->stages.push_back(st);
+    return TCG_OK;
+  }
+  // pad register set to exactly R bits
+  uint32_t rset = sd.rset;
+  auto pad_from = [&](int lo, int hi) {
+    for (int t = lo; t < hi && popc64(rset) < R; ++t)
+      if (!(rset >> t & 1)) rset |= 1u << t;
+  };
+  if (prefer_high_pad) {
+    pad_from(std::min(kLo, L), L);
+    pad_from(0, L);
+  } else {
+    pad_from(0, L);
+  }
+  if (popc64(rset) != R) return TCG_ERR_INVALID_ARG;
+  st.R = R;
+  int ri = 0;
+  for (int t = 0; t < L; ++t)
+    if (rset >> t & 1) st.reg_tile[ri++] = t;
+  // thread bits
+  std::vector<int> tb;
+  for (int t = 0; t < L; ++t)
+    if (!(rset >> t & 1)) tb.push_back(t);
+  st.nthread_bits = (int)tb.size();
+  std::vector<int> order;
+  bool low_ok = (int)tb.size() >= std::min(kLo, L - R);
+  for (int i = 0; i < std::min(kLo, (int)tb.size()); ++i)
+    if (tb[i] != i) low_ok = false;
+  if (low_ok) {
+    order = tb;
+    st.lanes_low = 1;
+  } else {
+    std::vector<int> left = tb;
+    int nl = std::min(5, (int)tb.size());
+    for (int i = 0; i < nl; ++i) {
+      int pick = -1;
+      if (i < 4)
+        for (size_t c = 0; c < left.size(); ++c)
+          if (bankpos(left[c]) == i) { pick = (int)c; break; }
+      if (pick < 0) pick = 0;
+      order.push_back(left[pick]);
+      left.erase(left.begin() + pick);
+    }
+    for (int t : left) order.push_back(t);
+    st.lanes_low = 0;
+  }
+  for (size_t i = 0; i < order.size(); ++i) st.thr_tile[i] = order[i];
+  // register position of each tile bit
+  int regpos_of_tile[32];
+  for (int i = 0; i < 32; ++i) regpos_of_tile[i] = -1;
+  for (int i = 0; i < R; ++i) regpos_of_tile[st.reg_tile[i]] = i;
+  int slot = 0;
+  for (int oi : sd.ops) {
+    const OpDraft& o = od[oi];
+    DevOp d;
+    std::memset(&d, 0, sizeof(d));
+    d.slot = -1;
+    d.grad_off = -1;
+    d.mat_off = o.mat_off;
+    d.k = o.k;
+    if (o.kind == OP_EXPECT) {
+      d.kind = OP_EXPECT;
+      int xr = 0;
+      for (int b = 0; b < 64; ++b)
+        if (o.x >> b & 1) {
+          int rp = regpos_of_tile[tile_of_gbit[b]];
+          if (rp < 0) return TCG_ERR_INVALID_ARG;
+          xr |= 1 << rp;
+        }
+      d.xreg = xr;
+      d.zmask = (uint32_t)o.z;
+      d.nY = popc64(o.x & o.z);
+      d.mat_off = o.term;
+      d.slot = slot;
+      SlotOut so;
+      so.slot = slot;
+      so.pad = 0;
+      so.out_off = o.term;
+      P->slot_out.push_back(so);
+      slot += 1;
+    } else if (o.kind == TCG_GATE_DIAG) {
+      d.kind = OP_DIAG;
+      for (int i = 0; i < o.k; ++i) d.p[i] = o.gbits[i];
+      if (o.grad_off >= 0) {
+        d.grad_off = o.grad_off;
+        d.slot = slot;
+        int E = 1 << o.k;
+        for (int e = 0; e < E; ++e) {
+          SlotOut so;
+          so.slot = slot + e;
+          so.pad = 0;
+          so.out_off = o.grad_off + e;
+          P->slot_out.push_back(so);
+        }
+        slot += E;
+      }
+    } else {  // dense on registers
+      if (o.k == 1) d.kind = OP_DENSE1;
+      else if (o.k == 2) d.kind = OP_DENSE2;
+      else return TCG_ERR_INVALID_ARG;
+      for (int i = 0; i < o.k; ++i) {
+        int rp = regpos_of_tile[tile_of_gbit[o.gbits[i]]];
+        if (rp < 0) return TCG_ERR_INVALID_ARG;
+        d.p[i] = rp;
+      }
+      if (o.grad_off >= 0) {
+        d.grad_off = o.grad_off;
+        d.slot = slot;
+        int E = 1 << (2 * o.k);
+        for (int e = 0; e < E; ++e) {
+          SlotOut so;
+          so.slot = slot + e;
+          so.pad = 0;
+          so.out_off = o.grad_off + e;
+          P->slot_out.push_back(so);
+        }
+        slot += E;
+      }
+    }
+    P->ops.push_back(d);
+  }
+  st.nslots = slot;
+  P->max_slots = std::max(P->max_slots, slot);
+  st.op_end = (int)P->ops.size();
+  st.slot_out_end = (int)P->slot_out.size();
+  P->stages.push_back(st);
+  return TCG_OK;
+}
+
+// Common tail: build DevPass for local set S (global-bit mask) and op drafts,
+// splitting the pass ops into stages.
+int emit_pass(Program* P, int n, int L, int R, uint64_t S,
+              const std::vector<OpDraft>& od, int max_slots) {
+  DevPass dp;
+  std::memset(&dp, 0, sizeof(dp));
+  dp.L = L;
+  int tile_of_gbit[64];
+  for (int i = 0; i < 64; ++i) tile_of_gbit[i] = -1;
+  int ti = 0, ni = 0;
+  for (int b = 0; b < n; ++b) {
+    if (S >> b & 1) {
+      dp.lbits[ti] = b;
+      tile_of_gbit[b] = ti++;
+    } else {
+      dp.nlbits[ni++] = b;
+    }
+  }
+  if (ti != L) return TCG_ERR_INVALID_ARG;
+  dp.nnonlocal = ni;
+  int lo = std::min(kLo, L);
+  dp.runs_off = (int)P->runs.size();
+  int nruns = 1 << (L - lo);
+  for (int r = 0; r < nruns; ++r) {
+    uint32_t off = 0;
+    for (int i = lo; i < L; ++i)
+      if (r >> (i - lo) & 1) off |= 1u << dp.lbits[i];
+    P->runs.push_back(off);
+  }
+  dp.stage_begin = (int)P->stages.size();
+  // stage drafting
+  std::vector<StageDraft> drafts;
+  StageDraft cur;
+  auto close = [&]() {
+    if (!cur.ops.empty()) drafts.push_back(cur);
+    cur = StageDraft();
+  };
+  for (size_t oi = 0; oi < od.size(); ++oi) {
+    const OpDraft& o = od[oi];
+    if (o.kind == OP_EXPECT) {
+      uint32_t tb = 0;
+      for (int b = 0; b < n; ++b)
+        if (o.x >> b & 1) tb |= 1u << tile_of_gbit[b];
+      uint32_t need = tb & ~cur.rset;
+      if (popc64(cur.rset | need) <= R && cur.slots + 1 <= max_slots) {
+        cur.rset |= need;
+      } else {
+        close();
+        cur.rset = tb;
+      }
+      cur.ops.push_back((int)oi);
+      cur.slots += 1;
+      continue;
+    }
+    int E = 0;
+    if (o.grad_off >= 0) E = (o.kind == TCG_GATE_DIAG) ? (1 << o.k) : (1 << (2 * o.k));
+    if (o.kind == TCG_GATE_DIAG) {
+      if (o.grad_off >= 0 && o.k > 2) return TCG_ERR_UNSUPPORTED;
+      if (cur.smem || cur.slots + E > max_slots) close();
+      cur.ops.push_back((int)oi);
+      cur.slots += E;
+      continue;
+    }
+    // dense
+    if (o.k > 2 || o.k > R) {
+      if (o.grad_off >= 0) return TCG_ERR_UNSUPPORTED;
+      if (!cur.smem) close();
+      cur.smem = true;
+      cur.ops.push_back((int)oi);
+      continue;
+    }
+    if (cur.smem) close();
+    uint32_t tb = 0;
+    for (int i = 0; i < o.k; ++i) tb |= 1u << tile_of_gbit[o.gbits[i]];
+    uint32_t need = tb & ~cur.rset;
+    if (popc64(cur.rset | need) <= R && cur.slots + E <= max_slots) {
+      cur.rset |= need;
+    } else {
+      close();
+      cur.rset = tb;
+    }
+    cur.ops.push_back((int)oi);
+    cur.slots += E;
+  }
+  close();
+  if (drafts.empty()) {  // a pass with no ops still needs a layout
+    StageDraft e;
+    drafts.push_back(e);
+  }
+  for (size_t s = 0; s < drafts.size(); ++s) {
+    bool edge = (s == 0) || (s + 1 == drafts.size());
+    int rc = emit_stage(P, dp, drafts[s], od, tile_of_gbit, L, R, edge || true);
+    if (rc != TCG_OK) return rc;
+  }
+  dp.stage_end = (int)P->stages.size();
+  P->passes.push_back(dp);
+  return TCG_OK;
+}
+
+void finish_entries(Program* P) {
+  std::vector<int64_t> e;
+  for (const SlotOut& so : P->slot_out) e.push_back(so.out_off);
+  std::sort(e.begin(), e.end());
+  e.erase(std::unique(e.begin(), e.end()), e.end());
+  P->entries = e;
+}
+
+}  // namespace
+
+int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
+                       bool reverse, int max_slots, Program* out) {
+  Program& P = *out;
+  P.n = n;
+  L = std::min(L, n);
+  P.L = L;
+  P.R = R;
+  if (R > L) return TCG_ERR_INVALID_ARG;
+  int lo = std::min(kLo, L);
+  std::vector<int> rem;
+  for (size_t i = 0; i < gates.size(); ++i) rem.push_back((int)i);
+  if (reverse) std::reverse(rem.begin(), rem.end());
+  int64_t nout = 0;
+  for (const PGate& g : gates)
+    if (g.grad_off >= 0) {
+      int64_t E = (g.kind == TCG_GATE_DIAG) ? (1 << g.k) : (1 << (2 * g.k));
+      nout = std::max(nout, g.grad_off + E);
+    }
+  P.nout = nout;
+  if (rem.empty()) {
+    // identity circuit: one pass with no ops keeps the launch path uniform
+    uint64_t S = 0;
+    for (int b = 0; b < L; ++b) S |= 1ull << b;
+    std::vector<OpDraft> none;
+    return emit_pass(&P, n, L, R, S, none, max_slots);
+  }
+  while (!rem.empty()) {
+    uint64_t S = (lo >= 64) ? ~0ull : ((1ull << lo) - 1);
+    uint64_t blocked = 0;
+    std::vector<int> taken, left;
+    for (int gi : rem) {
+      const PGate& g = gates[gi];
+      uint64_t bits = gate_mask(g);
+      if (bits & blocked) {
+        blocked |= bits;
+        left.push_back(gi);
+        continue;
+      }
+      uint64_t need = (g.kind == TCG_GATE_DENSE) ? (bits & ~S) : 0;
+      if (popc64(S | need) <= L) {
+        S |= need;
+        taken.push_back(gi);
+      } else {
+        blocked |= bits;
+        left.push_back(gi);
+      }
+    }
+    if (taken.empty()) return TCG_ERR_INVALID_ARG;  // cannot happen: L >= lo + 6
+    // pad S to L bits: prefer bits the next gates need
+    for (int gi : left) {
+      if (popc64(S) >= L) break;
+      const PGate& g = gates[gi];
+      if (g.kind != TCG_GATE_DENSE) continue;
+      uint64_t need = gate_mask(g) & ~S;
+      if (popc64(S | need) <= L) S |= need;
+    }
+    for (int b = 0; b < n && popc64(S) < L; ++b) S |= 1ull << b;
+    std::vector<OpDraft> od;
+    for (int gi : taken) {
+      const PGate& g = gates[gi];
+      OpDraft o;
+      o.kind = g.kind;
+      o.k = g.k;
+      for (int i = 0; i < 6; ++i) o.gbits[i] = (i < g.k) ? g.gbits[i] : 0;
+      o.mat_off = g.mat_off;
+      o.grad_off = g.grad_off;
+      od.push_back(o);
+    }
+    int rc = emit_pass(&P, n, L, R, S, od, max_slots);
+    if (rc != TCG_OK) return rc;
+    rem.swap(left);
+  }
+  finish_entries(&P);
+  return TCG_OK;
+}
+
+int build_term_program(int n, const std::vector<tcg_pauli>& terms, int L, int R,
+                       int max_slots, Program* out, std::vector<int>* direct) {
+  Program& P = *out;
+  P.n = n;
+  L = std::min(L, n);
+  P.L = L;
+  P.R = R;
+  P.nout = (int64_t)terms.size();
+  int lo = std::min(kLo, L);
+  std::vector<int> rem;
+  for (size_t t = 0; t < terms.size(); ++t) {
+    if (popc64(terms[t].xmask) > 2) direct->push_back((int)t);  // register path: <= 2 X/Y bits
+    else rem.push_back((int)t);
+  }
+  // group equal / overlapping X masks next to each other
+  std::stable_sort(rem.begin(), rem.end(), [&](int a, int b) {
+    return terms[a].xmask < terms[b].xmask;
+  });
+  while (!rem.empty()) {
+    uint64_t S = (1ull << lo) - 1;
+    std::vector<int> taken, left;
+    for (int t : rem) {
+      uint64_t need = terms[t].xmask & ~S;
+      if (popc64(S | need) <= L) {
+        S |= need;
+        taken.push_back(t);
+      } else {
+        left.push_back(t);
+      }
+    }
+    for (int b = 0; b < n && popc64(S) < L; ++b) S |= 1ull << b;
+    std::vector<OpDraft> od;
+    for (int t : taken) {
+      OpDraft o;
+      std::memset(&o, 0, sizeof(o));
+      o.kind = OP_EXPECT;
+      o.k = popc64(terms[t].xmask);
+      o.x = terms[t].xmask;
+      o.z = terms[t].zmask;
+      o.term = t;
+      o.grad_off = -1;
+      od.push_back(o);
+    }
+    int rc = emit_pass(&P, n, L, R, S, od, max_slots);
+    if (rc != TCG_OK) return rc;
+    rem.swap(left);
+  }
+  finish_entries(&P);
+  return TCG_OK;
+}
+
+int program_device_view(Program* p, ProgramView* view) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(p->mu);
+  auto it = p->dev.find(dev);
+  if (it != p->dev.end()) {
+    *view = it->second.view;
+    return TCG_OK;
+  }
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t o_pass = 0;
+  size_t o_stage = al(o_pass + p->passes.size() * sizeof(DevPass));
+  size_t o_op = al(o_stage + p->stages.size() * sizeof(DevStage));
+  size_t o_so = al(o_op + p->ops.size() * sizeof(DevOp));
+  size_t o_runs = al(o_so + p->slot_out.size() * sizeof(SlotOut));
+  size_t o_ent = al(o_runs + p->runs.size() * sizeof(uint32_t));
+  size_t total = al(o_ent + p->entries.size() * sizeof(int64_t)) + 256;
+  std::vector<char> host(total, 0);
+  if (!p->passes.empty()) std::memcpy(host.data() + o_pass, p->passes.data(), p->passes.size() * sizeof(DevPass));
+  if (!p->stages.empty()) std::memcpy(host.data() + o_stage, p->stages.data(), p->stages.size() * sizeof(DevStage));
+  if (!p->ops.empty()) std::memcpy(host.data() + o_op, p->ops.data(), p->ops.size() * sizeof(DevOp));
+  if (!p->slot_out.empty()) std::memcpy(host.data() + o_so, p->slot_out.data(), p->slot_out.size() * sizeof(SlotOut));
+  if (!p->runs.empty()) std::memcpy(host.data() + o_runs, p->runs.data(), p->runs.size() * sizeof(uint32_t));
+  if (!p->entries.empty()) std::memcpy(host.data() + o_ent, p->entries.data(), p->entries.size() * sizeof(int64_t));
+  void* d = nullptr;
+  if (cudaMalloc(&d, total) != cudaSuccess) return TCG_ERR_OOM;
+  if (cudaMemcpy(d, host.data(), total, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return TCG_ERR_CUDA;
+  }
+  Program::DevCopy c;
+  c.base = d;
+  char* b = (char*)d;
+  c.view.passes = (const DevPass*)(b + o_pass);
+  c.view.stages = (const DevStage*)(b + o_stage);
+  c.view.ops = (const DevOp*)(b + o_op);
+  c.view.slot_out = (const SlotOut*)(b + o_so);
+  c.view.runs = (const uint32_t*)(b + o_runs);
+  c.view.entries = (const int64_t*)(b + o_ent);
+  c.view.nentries = (int64_t)p->entries.size();
+  p->dev[dev] = c;
+  *view = c.view;
+  return TCG_OK;
+}
+
+void program_free(Program* p) {
+  std::lock_guard<std::mutex> lk(p->mu);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (auto& kv : p->dev) {
+    cudaSetDevice(kv.first);
+    cudaFree(kv.second.base);
+  }
+  cudaSetDevice(cur);
+  p->dev.clear();
+}
+
+}  // namespace tcg

@@ -1,0 +1,85 @@
+// plan.h — host-side planner: gate list -> passes -> stages -> device program.
+#pragma once
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tcgb300.h"
+#include "engine.h"
+
+namespace tcg {
+
+// One direction of a plan (forward, backward, or a Pauli-term measurement),
+// flattened into the arrays the kernels read.
+struct Program {
+  int n = 0;
+  int L = 0;                 // tile bits of every pass
+  int R = 0;                 // register bits of the kernel it targets
+  std::vector<DevPass> passes;
+  std::vector<DevStage> stages;
+  std::vector<DevOp> ops;
+  std::vector<SlotOut> slot_out;
+  std::vector<uint32_t> runs;
+  std::vector<int64_t> entries;  // distinct accumulator outputs (sorted)
+  int max_slots = 0;         // largest stage slot count
+  int64_t nout = 0;          // per-circuit accumulator outputs (complex entries)
+
+  // device copy, one per CUDA device, uploaded on first use
+  struct DevCopy { void* base = nullptr; ProgramView view{}; };
+  std::map<int, DevCopy> dev;
+  std::mutex mu;
+};
+
+struct PlanOpts {
+  int tile_bits_fwd = 12;  // 2^(12-4) = 256 threads per CTA
+  int tile_bits_bwd = 12;
+  int max_stage_slots = 64;
+};
+
+// A planned gate (global-bit form).
+struct PGate {
+  int kind;            // TCG_GATE_DENSE / TCG_GATE_DIAG
+  int k;
+  int gbits[TCG_MAX_GATE_QUBITS];  // global index bits, first = sub-index MSB
+  int64_t mat_off;
+  int64_t grad_off;
+};
+
+// Build a gate program for `gates` in execution order (`reverse` for the
+// adjoint sweep: passes/stages are laid out in the order they execute).
+int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
+                       bool reverse, int max_slots, Program* out);
+
+// Build a measurement program for Pauli terms (global-bit masks).  Terms whose
+// X/Y bits cannot fit the register layout are returned in `direct`.
+int build_term_program(int n, const std::vector<tcg_pauli>& terms, int L, int R,
+                       int max_slots, Program* out, std::vector<int>* direct);
+
+// Upload (once per device) and return the device view.
+int program_device_view(Program* p, ProgramView* view);
+void program_free(Program* p);
+
+}  // namespace tcg
+
+struct tcg_plan {
+  int n = 0;
+  int ngates = 0;
+  int64_t grad_entries = 0;   // max grad_off + entries over gates
+  bool has_grad = false;
+  tcg::Program fwd;
+  tcg::Program bwd;
+};
+
+struct tcg_mplan {
+  int n = 0;
+  int nterms = 0;
+  std::vector<tcg_pauli> terms;
+  tcg::Program prog;
+  std::vector<int> direct;    // terms run by the plain kernel
+  // device copies of terms[] and direct[] per device
+  struct Dev { void* base = nullptr; tcg_pauli* terms = nullptr; int* direct = nullptr; int64_t* direct_entries = nullptr; };
+  std::map<int, Dev> dev;
+  std::mutex mu;
+};

@@ -1,0 +1,112 @@
+"""Known-answer cases transcribed from the reference's own test-suite.
+
+Each case gives the circuit (gate list in the oracle's ``(name, qubits,
+params)`` form, plus optional ``inputs``), the queried quantity and the value
+the reference's test asserts, with the reference file:line it comes from.
+The values are copied from the assertions in those test files (read as
+text; the reference cannot be imported in this environment).  Both the CPU
+oracle (tests/test_oracle_kats.py) and the GPU engine
+(tests/test_gpu_kats.py) are checked against them.
+"""
+
+import numpy as np
+
+S2 = 1 / np.sqrt(2)
+
+KATS = [
+    # tests/test_circuit.py:21-44 -- gate leg order / big-endian layout
+    dict(id="unitary01_amp2", src="tests/test_circuit.py:23-28", n=2,
+         ops=[("any", (0, 1), {"unitary": np.arange(16).reshape(4, 4)})],
+         query=("amp", 2), expect=8.0, atol=0.0),
+    dict(id="unitary10_amp2", src="tests/test_circuit.py:29-36", n=2,
+         ops=[("any", (1, 0), {"unitary": np.arange(16).reshape(4, 4)})],
+         query=("amp", 2), expect=4.0, atol=0.0),
+    dict(id="unitary0_amp2", src="tests/test_circuit.py:37-42", n=2,
+         ops=[("any", (0,), {"unitary": np.arange(4).reshape(2, 2)})],
+         query=("amp", 2), expect=2.0, atol=0.0),
+    # tests/test_circuit.py:47-53 -- amplitude
+    dict(id="x_amp10", src="tests/test_circuit.py:49-51", n=2, ops=[("x", (0,), {})],
+         query=("bitstring", "10"), expect=1.0, atol=1e-7),
+    dict(id="x_cnot_amp11", src="tests/test_circuit.py:49-53", n=2,
+         ops=[("x", (0,), {}), ("cnot", (0, 1), {})],
+         query=("bitstring", "11"), expect=1.0, atol=1e-7),
+    # tests/test_circuit.py:64-68 -- iswap on identity inputs (2n-leg inputs)
+    dict(id="iswap_eye", src="tests/test_circuit.py:64-68", n=2, inputs=np.eye(4).reshape(-1),
+         ops=[("iswap", (0, 1), {})], query=("state4x4",),
+         expect=np.array([[1, 0, 0, 0], [0, 0, 1j, 0], [0, 1j, 0, 0], [0, 0, 0, 1]]), atol=1e-5),
+    # tests/test_circuit.py:71-77 -- controlled rotation
+    dict(id="crx_z0", src="tests/test_circuit.py:71-77", n=2,
+         ops=[("x", (1,), {}), ("crx", (1, 0), {"theta": 0.3})],
+         query=("expect_ops", [("z", [0])]), expect=0.95533645, atol=1e-5),
+    # tests/test_circuit.py:80-84 -- adjoint gate
+    dict(id="x_sd_state", src="tests/test_circuit.py:80-84", n=1,
+         ops=[("x", (0,), {}), ("sd", (0,), {})], query=("state",),
+         expect=np.array([0.0, -1.0j]), atol=1e-6),
+    # tests/test_circuit.py:405-413 -- X (x) Y on identity inputs
+    dict(id="xy_eye", src="tests/test_circuit.py:405-413", n=2, inputs=np.eye(4).reshape(-1),
+         ops=[("x", (0,), {}), ("y", (1,), {})], query=("state4x4",),
+         expect=np.kron(np.array([[0, 1], [1, 0]]), np.array([[0, -1j], [1j, 0]])), atol=1e-4),
+    # tests/test_circuit.py:416-429 -- expectation_ps forms
+    dict(id="ps_zz", src="tests/test_circuit.py:418-421", n=2, ops=[("x", (0,), {})],
+         query=("ps", dict(z=[0, 1])), expect=-1.0, atol=1e-5),
+    dict(id="ps_xz", src="tests/test_circuit.py:423-426", n=2, ops=[("h", (0,), {})],
+         query=("ps", dict(z=[1], x=[0])), expect=1.0, atol=1e-5),
+    dict(id="ps_codes", src="tests/test_circuit.py:427-428", n=2, ops=[("h", (0,), {})],
+         query=("ps", dict(ps=[1, 3])), expect=1.0, atol=1e-5),
+    dict(id="ps_overrides", src="tests/test_circuit.py:429", n=2, ops=[("h", (0,), {})],
+         query=("ps", dict(z=[1, 2], ps=[1, 3])), expect=1.0, atol=1e-5),
+    # tests/test_circuit.py:432-440 -- probability
+    dict(id="hh_prob", src="tests/test_circuit.py:432-440", n=2,
+         ops=[("h", (0,), {}), ("h", (1,), {})], query=("prob",),
+         expect=np.array([1, 1, 1, 1]) / 4, atol=1e-5),
+    # tests/test_circuit.py:1278-1281 -- Y sign
+    dict(id="y_sign", src="tests/test_circuit.py:1278-1281", n=1, inputs=S2 * np.array([-1, 1.0j]),
+         ops=[], query=("ps", dict(y=[0])), expect=-1.0, atol=1e-5),
+    # tests/test_circuit.py:1373-1381 -- negative indices
+    dict(id="minus_x0", src="tests/test_circuit.py:1373-1377", n=3,
+         ops=[("h", (-2,), {}), ("h", (0,), {})], query=("ps", dict(x=[0])), expect=1.0, atol=1e-5),
+    dict(id="minus_x1", src="tests/test_circuit.py:1378", n=3,
+         ops=[("h", (-2,), {}), ("h", (0,), {})], query=("ps", dict(x=[1])), expect=1.0, atol=1e-5),
+    dict(id="minus_xm1", src="tests/test_circuit.py:1379", n=3,
+         ops=[("h", (-2,), {}), ("h", (0,), {})], query=("ps", dict(x=[-1])), expect=0.0, atol=1e-5),
+    dict(id="minus_zm2", src="tests/test_circuit.py:1380", n=3,
+         ops=[("h", (-2,), {}), ("h", (0,), {})], query=("ps", dict(z=[-2])), expect=0.0, atol=1e-5),
+    # tests/test_circuit.py:1384-1390 -- Y expectation on a given input
+    dict(id="sexpps_y", src="tests/test_circuit.py:1385-1390", n=1, inputs=S2 * np.array([1.0, 1.0j]),
+         ops=[], query=("ps", dict(y=[0])), expect=1.0, atol=1e-5),
+    # abstractcircuit.py docstring of expectation_ps (:1221-1225)
+    dict(id="doc_xh", src="tensorcircuit/abstractcircuit.py:1221-1225", n=2,
+         ops=[("x", (0,), {}), ("h", (1,), {})], query=("ps", dict(x=[1], z=[0])), expect=-1.0, atol=1e-5),
+]
+
+# tests/test_circuit.py:1392-1406 -- a 4-qubit circuit whose sampled and
+# exact Pauli expectations must agree (exact within 1e-5, 81920 shots
+# within 0.01); the value itself is not asserted by the reference.
+SEXPPS_CIRCUIT = dict(
+    src="tests/test_circuit.py:1392-1406", n=4,
+    ops=[("h", (0,), {}), ("cnot", (0, 1), {}), ("rx", (1,), {"theta": 0.3}), ("rz", (2,), {"theta": -1.2}),
+         ("ccnot", (2, 3, 1), {}), ("rzz", (0, 3), {"theta": 0.5}), ("ry", (3,), {"theta": 2.2}),
+         ("s", (1,), {}), ("td", (2,), {})],
+    term=dict(x=[1], y=[0], z=[2, 3]), shots=81920, shot_tol=0.01,
+)
+
+# tests/test_gates.py:147-156 -- rxx/ryy/rzz equal exp1 with half angle
+RXX_EQUIV = dict(
+    src="tests/test_gates.py:147-156", n=3,
+    ops_a=[("rxx", (0, 1), {"theta": 1.0}), ("ryy", (0, 2), {"theta": 0.5}), ("rzz", (0, 1), {"theta": -0.5})],
+    ops_b=[("exp1", (0, 1), {"theta": 0.5, "unitary": np.kron([[0, 1], [1, 0]], [[0, 1], [1, 0]])}),
+           ("exp1", (0, 2), {"theta": 0.25, "unitary": np.kron([[0, -1j], [1j, 0]], [[0, -1j], [1j, 0]])}),
+           ("exp1", (0, 1), {"theta": -0.25, "unitary": np.diag([1, -1, -1, 1])})],
+    atol=1e-5,
+)
+
+# tests/test_backends.py:283-291 -- probability_sample histogram
+PROB_SAMPLE = dict(src="tests/test_backends.py:283-291",
+                   p=np.array([0.05] * 8 + [0.2, 0.4], dtype=np.float32), shots=10000, atol=200)
+
+# tests/test_backends.py:426-476 -- vvag self-consistency (torch backend)
+VVAG = dict(src="tests/test_backends.py:426-476", n=4, nlayers=3, batch=8, atol=1e-4)
+
+# tests/test_quantum.py:495-502 -- ps2xyz / xyz2ps
+PS_XYZ = dict(src="tests/test_quantum.py:495-502",
+              xyz={"x": [1], "z": [2]}, ps=[0, 1, 3], ps6=[0, 1, 3, 0, 0, 0])

@@ -1,0 +1,44 @@
+"""CPU: the C-ABI library builds, loads and exports every symbol that
+include/tcgb300.h declares; host-only entry points behave."""
+
+import ctypes
+import os
+import re
+
+from tensorcircuit_gb300 import _native as nat
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    with open(os.path.join(ROOT, "include", "tcgb300.h")) as fh:
+        src = fh.read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(tcg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = nat.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+    bound = {n for n, _, _ in nat.SIGNATURES}
+    assert set(names) == bound, set(names) ^ bound
+
+
+def test_status_strings_and_version():
+    lib = nat.load()
+    assert lib.tcg_abi_version() == 1
+    assert lib.tcg_status_string(0) == b"ok"
+    assert b"twice" in lib.tcg_status_string(2)
+
+
+def test_host_side_errors_without_gpu():
+    lib = nat.load()
+    h = ctypes.c_void_p()
+    assert lib.tcg_plan_create(3, None, 0, None, ctypes.byref(h)) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_forward(None, None, 1, None, 0, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_sample(None, 10, 1, None, 0, 1, None, None, 0, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_sample_scratch_bytes(10, 2) >= 2 * 8 * 1024
+    assert lib.tcg_launch_count() == 0

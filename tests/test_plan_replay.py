@@ -1,0 +1,172 @@
+"""CPU: replay the engine's device programs (planner output) and check them
+against the complex128 oracle -- forward states, adjoint cotangents and
+Pauli measurements -- plus the index invariants every kernel launch relies
+on.  No GPU needed: plans are built by the native library on the host."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import statevector as sv
+from tests.plan_emulator import Replay
+from tensorcircuit_gb300 import _native as nat
+from tensorcircuit_gb300 import circuit as cmod
+from tensorcircuit_gb300 import engine as eng
+from tensorcircuit_gb300 import templates
+
+ONE_Q = ["x", "y", "z", "h", "s", "t", "sd", "td", "wroot"]
+ONE_Q_P = ["rx", "ry", "rz", "phase"]
+TWO_Q = ["cnot", "cz", "swap", "cy", "ox", "oy", "oz"]
+TWO_Q_P = ["rxx", "ryy", "rzz", "crx", "cry", "crz", "cphase", "orx", "ory", "orz", "iswap"]
+
+
+def random_gate_list(n, ngates, rng, allow3=True):
+    gl = []
+    for _ in range(ngates):
+        r = rng.random()
+        if r < 0.25:
+            gl.append((str(rng.choice(ONE_Q)), (int(rng.integers(n)),), {}))
+        elif r < 0.5:
+            gl.append((str(rng.choice(ONE_Q_P)), (int(rng.integers(n)),), {"theta": float(rng.uniform(0, 6.3))}))
+        elif r < 0.65:
+            q = rng.choice(n, 2, replace=False)
+            gl.append((str(rng.choice(TWO_Q)), (int(q[0]), int(q[1])), {}))
+        elif r < 0.85:
+            q = rng.choice(n, 2, replace=False)
+            gl.append((str(rng.choice(TWO_Q_P)), (int(q[0]), int(q[1])), {"theta": float(rng.uniform(0, 6.3))}))
+        elif r < 0.95 or not allow3:
+            q = rng.choice(n, 2, replace=False)
+            u = templates.haar_unitary(4, rng)
+            gl.append(("any", (int(q[0]), int(q[1])), {"unitary": u}))
+        else:
+            q = rng.choice(n, 3, replace=False)
+            gl.append((str(rng.choice(["toffoli", "fredkin"])), tuple(int(x) for x in q), {}))
+    return gl
+
+
+def build_host(n, gl):
+    """Record a gate list on a Circuit and build plan + matrices on the CPU."""
+    c = cmod.Circuit(n)
+    templates.apply_gate_list(c, gl)
+    n_eng = max(n, nat.MIN_QUBITS)
+    entry = cmod._build_entry(n_eng, c._ops)
+    blocks = []
+    if entry.const_np is not None:
+        blocks.append(torch.as_tensor(entry.const_np))
+    for gkey, idx, E in entry.groups:
+        b = cmod._group_block(gkey, c._ops, idx, torch.device("cpu")).to(torch.complex64)
+        blocks.append(b.reshape(-1))
+    mats = torch.cat(blocks).numpy() if blocks else np.zeros(1, np.complex64)
+    return c, entry, mats, n_eng
+
+
+def oracle_cotangents(n, gl, mu_out):
+    """Reference cotangent of every gate matrix entry, d Re<mu|psi_out>."""
+    psis = [sv.run_circuit(n, [])]
+    for g in gl:
+        psis.append(sv.run_circuit(n, [g], psis[-1]))
+    out = [None] * len(gl)
+    mu = mu_out.astype(np.complex128)
+    for i in reversed(range(len(gl))):
+        name, q, p = gl[i]
+        q = [int(x) % n for x in q]
+        m = sv.gate_matrix(name, **p)
+        k = len(q)
+        # M_ab = sum_rest mu[a, rest] conj(psi_in[b, rest])
+        rest = [a for a in range(n) if a not in q]
+        mt = np.transpose(mu.reshape([2] * n), q + rest).reshape(1 << k, -1)
+        pt = np.transpose(psis[i].reshape([2] * n), q + rest).reshape(1 << k, -1)
+        out[i] = mt @ pt.conj().T
+        mu = sv.apply_matrix(mu, m.conj().T, q, n)
+    return out, mu
+
+
+@pytest.mark.parametrize("n,ngates,seed", [(6, 40, 0), (7, 60, 1), (9, 80, 2), (13, 60, 3), (14, 70, 4),
+                                           (15, 50, 5)])
+def test_forward_program_replay_matches_oracle(n, ngates, seed):
+    rng = np.random.default_rng(seed)
+    gl = random_gate_list(n, ngates, rng)
+    c, entry, mats, n_eng = build_host(n, gl)
+    assert n_eng == n
+    prog = nat.debug_program(entry.plan.handle, 0)
+    psi0 = np.zeros(1 << n, np.complex128)
+    psi0[0] = 1
+    got = Replay(prog, n).forward(psi0, mats)
+    want = sv.run_circuit(n, gl)
+    np.testing.assert_allclose(got, want, atol=2e-5)
+
+
+@pytest.mark.parametrize("n,ngates,seed", [(6, 30, 10), (8, 50, 11), (13, 40, 12), (14, 40, 13)])
+def test_backward_program_replay_matches_oracle(n, ngates, seed):
+    rng = np.random.default_rng(seed)
+    gl = random_gate_list(n, ngates, rng, allow3=True)
+    c, entry, mats, n_eng = build_host(n, gl)
+    psi_out = sv.run_circuit(n, gl)
+    mu_out = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    prog = nat.debug_program(entry.plan.handle, 1)
+    nout = max(1, mats.size)
+    psi_in, mu_in, grads = Replay(prog, n).backward(psi_out, mu_out, mats, nout)
+    want_cot, want_mu = oracle_cotangents(n, gl, mu_out)
+    e0 = np.zeros(1 << n)
+    e0[0] = 1
+    np.testing.assert_allclose(psi_in, e0, atol=2e-5)
+    np.testing.assert_allclose(mu_in, want_mu, atol=1e-4)
+    # compare the cotangents of gates that carry a gradient slot (the random
+    # lists never contain the identity, so engine ops and list entries align)
+    assert len(entry.gates_c) == len(gl)
+    for gi, (kind, qubits, mat_off, grad_off) in enumerate(entry.gates_c):
+        if grad_off < 0:
+            continue
+        cot = want_cot[gi]
+        want = np.diag(cot) if kind == nat.TCG_GATE_DIAG else cot.reshape(-1)
+        got = grads[grad_off:grad_off + want.size]
+        np.testing.assert_allclose(got, want, atol=1e-3, rtol=1e-4)
+
+
+@pytest.mark.parametrize("n,seed", [(6, 0), (10, 1), (14, 2)])
+def test_measure_program_replay_matches_oracle(n, seed):
+    rng = np.random.default_rng(seed)
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    psi /= np.linalg.norm(psi)
+    terms = []
+    specs = []
+    for _ in range(30):
+        k = int(rng.integers(0, 4))
+        q = rng.choice(n, min(n, 1 + k + int(rng.integers(0, 3))), replace=False)
+        kinds = rng.integers(1, 4, size=len(q))
+        x = [int(a) for a, b in zip(q, kinds) if b == 1]
+        y = [int(a) for a, b in zip(q, kinds) if b == 2]
+        z = [int(a) for a, b in zip(q, kinds) if b == 3]
+        specs.append(dict(x=x, y=y, z=z))
+        terms.append(eng.pauli_masks(n, x, y, z))
+    tp = eng.TermPlan(n, tuple(terms))
+    prog = nat.debug_program(tp.handle, 2)
+    got = Replay(prog, n).measure(psi, len(terms))
+    direct = set()
+    for t, (xm, zm) in enumerate(terms):
+        if bin(xm).count("1") > 2:
+            direct.add(t)
+    for t, s in enumerate(specs):
+        if t in direct:
+            assert got[t] == 0  # handled by the plain kernel, not the program
+            continue
+        np.testing.assert_allclose(got[t], sv.expectation_ps(psi, n, **s), atol=1e-10)
+
+
+def test_plan_errors_map_to_reference_exceptions():
+    with pytest.raises(AssertionError):
+        eng.GatePlan(6, [(nat.TCG_GATE_DENSE, (1, 1), 0, -1)], 16)
+    with pytest.raises(ValueError):
+        eng.GatePlan(6, [(nat.TCG_GATE_DENSE, (7,), 0, -1)], 4)
+    with pytest.raises(NotImplementedError):
+        eng.GatePlan(6, [(nat.TCG_GATE_DENSE, (0, 1, 2), 0, 0)], 64)
+
+
+def test_hea_plan_pass_counts():
+    """The n=20 hardware-efficient ansatz fits in a few HBM passes."""
+    n, nl = 20, 8
+    c = cmod.Circuit(n)
+    templates.apply_hea(c, n, nl, np.zeros(templates.hea_nparams(n, nl)))
+    entry = cmod._build_entry(n, c._ops)
+    assert entry.plan.npasses <= 8
+    assert entry.plan.ngates == 312
