@@ -198,6 +198,19 @@ int tcg_debug_program(const void* plan, int32_t which, const void** arrays,
  * (all entry points, all devices). */
 int64_t tcg_launch_count(void);
 
+/* Specialised kernels (no reference counterpart).  A plan direction whose
+ * kernels have run twice is translated into straight-line CUDA for its exact
+ * gate layout and compiled once with NVRTC for sm_103a (environment variable
+ * TCG_JIT: 0 = never, 1 = from the first call, unset = after two calls;
+ * cubins are cached under TCG_JIT_CACHE or ~/.cache/tcgb300).  This reports
+ * state (0 not built, 1 built, -1 failed, in which case the generic kernels
+ * keep running) and copies into `text` (cap bytes) the compile log
+ * (what = 0, ptxas register report included) or the generated source
+ * (what = 1).  which/mode as for tcg_debug_program; mode 0 forward,
+ * 1 adjoint, 2 measure, 3 Pauli accumulate. */
+int tcg_debug_jit(const void* plan, int32_t which, int32_t mode, int32_t* state,
+                  char* text, int64_t cap, int32_t what);
+
 #ifdef __cplusplus
 }
 #endif

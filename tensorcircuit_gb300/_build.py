@@ -21,8 +21,23 @@ OBJDIR = os.path.join(HERE, "lib", "obj")
 LIBNAME = "libtcgb300.so"
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["pass.cu", "misc.cu", "api.cu", "plan.cpp"]
-HEADERS = ["engine.h", "kernels.h", "plan.h"]
+SOURCES = ["pass.cu", "misc.cu", "api.cu", "plan.cpp", "jit.cpp"]
+HEADERS = ["engine.h", "kernels.h", "plan.h", "jit.h", "jit_device.cuh"]
+
+
+def _write_jit_include() -> None:
+    """Embed jit_device.cuh in the library as a string literal
+    (lib/obj/jit_device.inc), the preamble NVRTC compiles with every
+    generated pass kernel."""
+    with open(os.path.join(CSRC, "jit_device.cuh")) as fh:
+        text = fh.read()
+    if ")TCGJIT" in text:
+        raise RuntimeError("jit_device.cuh must not contain the raw-string delimiter")
+    out = os.path.join(OBJDIR, "jit_device.inc")
+    body = 'R"TCGJIT(' + text + ')TCGJIT"\n'
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as fh:
+            fh.write(body)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -53,7 +68,7 @@ def _digest() -> str:
 def _compile(src: str, nvcc: str, verbose: bool) -> str:
     obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+           "-I", INCLUDE, "-I", OBJDIR, "-c", os.path.join(CSRC, src), "-o", obj]
     if src.endswith(".cpp"):
         cmd[1:1] = ["-x", "cu"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -74,10 +89,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if fh.read().strip() == dig:
                 return lib_path()
     nvcc = nvcc_path()
+    _write_jit_include()
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, nvcc, verbose), SOURCES))
     tmp = lib_path() + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -81,6 +81,7 @@ SIGNATURES = [
     ("tcg_inner_scratch_bytes", _SZ, [_I64, _I64]),
     ("tcg_inner", ctypes.c_int, [_P, _P, _I64, _I64, _P, _P, _SZ, _P]),
     ("tcg_launch_count", _I64, []),
+    ("tcg_debug_jit", ctypes.c_int, [_P, _I32, _I32, ctypes.POINTER(_I32), ctypes.c_char_p, _I64, _I32]),
     ("tcg_debug_program", ctypes.c_int, [_P, _I32, ctypes.POINTER(_P), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
 ]
 
@@ -108,6 +109,17 @@ class DevOp(ctypes.Structure):
 
 class SlotOut(ctypes.Structure):
     _fields_ = [("slot", ctypes.c_int32), ("pad", ctypes.c_int32), ("out_off", ctypes.c_int64)]
+
+
+def jit_info(handle: Any, which: int, mode: int, what: int = 0, cap: int = 1 << 22) -> "tuple[int, str]":
+    """(state, text) of a plan direction's specialised kernels: state 0 not
+    built, 1 built, -1 failed; text = compile log (what=0) or generated
+    source (what=1)."""
+    lib = load()
+    st = ctypes.c_int32(0)
+    buf = ctypes.create_string_buffer(cap)
+    check(lib.tcg_debug_jit(handle, which, mode, ctypes.byref(st), buf, cap, what), "debug_jit")
+    return st.value, buf.value.decode(errors="replace")
 
 
 def debug_program(handle: Any, which: int) -> dict:

@@ -185,7 +185,7 @@ def _stack_scalars(vals: Sequence[Any], dev: torch.device) -> torch.Tensor:
         if np.iscomplexobj(arr):
             return torch.as_tensor(arr.astype(np.complex64), device=dev)
         return torch.as_tensor(arr.astype(np.float32), device=dev)
-    cplx = any((isinstance(v, torch.Tensor) and v.is_complex()) or np.iscomplexobj(v) for v in vals)
+    cplx = any(v.is_complex() if isinstance(v, torch.Tensor) else np.iscomplexobj(v) for v in vals)
     dt = torch.complex64 if cplx else torch.float32
     ts = []
     for v in vals:

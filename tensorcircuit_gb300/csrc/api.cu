@@ -70,6 +70,48 @@ int mplan_device(tcg_mplan* p, tcg_mplan::Dev* out) {
 
 constexpr uint32_t kDirectBlocks = 304;
 
+// Runs every pass of a program direction: the specialised kernels when the
+// JIT policy selects them for this plan (see jit.cpp), else the generic
+// pass kernels of pass.cu.
+int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStream_t st) {
+  JitKernels* jk = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(P->jit_mu);
+    const int pol = jit_policy();
+    P->calls[mode] += 1;
+    if (pol == 1 || (pol == 2 && P->calls[mode] >= 3)) {
+      if (!P->jit[mode]) {
+        P->jit[mode].reset(new (std::nothrow) JitKernels());
+        if (P->jit[mode]) jit_build(*P, mode, R, P->jit[mode].get());
+      }
+      if (P->jit[mode] && !P->jit[mode]->failed) jk = P->jit[mode].get();
+    }
+  }
+  const uint32_t ntiles = 1u << (a.n - P->L);
+  if (jk) {
+    KParams_Host kp;
+    kp.psi = a.psi;
+    kp.mu = a.mu;
+    kp.mats = a.mats;
+    kp.mat_stride = a.mat_stride;
+    kp.partial = a.partial;
+    kp.part_stride = a.part_stride;
+    kp.coef = a.coef;
+    kp.coef_stride = a.coef_stride;
+    for (int ps = 0; ps < (int)P->passes.size(); ++ps) {
+      const int rc = cuda_rc(jit_launch(jk, ps, kp, ntiles, batch, a.n, st));
+      if (rc != TCG_OK) return rc;
+    }
+    return TCG_OK;
+  }
+  for (int ps = 0; ps < (int)P->passes.size(); ++ps) {
+    a.pass = ps;
+    const int rc = cuda_rc(launch_pass(mode, R, a, P->L, batch, st));
+    if (rc != TCG_OK) return rc;
+  }
+  return TCG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -180,12 +222,7 @@ int tcg_forward(const tcg_plan* plan, void* psi, int64_t batch, const void* mats
   a.mats = static_cast<const float2*>(mats);
   a.mat_stride = mat_stride;
   a.max_slots = 0;
-  for (int ps = 0; ps < (int)p->fwd.passes.size(); ++ps) {
-    a.pass = ps;
-    rc = cuda_rc(launch_pass(MODE_FWD, kRFwd, a, p->fwd.L, batch, as_stream(stream)));
-    if (rc != TCG_OK) return rc;
-  }
-  return TCG_OK;
+  return run_program(&p->fwd, MODE_FWD, kRFwd, a, batch, as_stream(stream));
 }
 
 size_t tcg_backward_scratch_bytes(const tcg_plan* plan, int64_t batch) {
@@ -218,11 +255,8 @@ int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch, const
   a.partial = static_cast<float2*>(scratch);
   a.part_stride = std::max<int64_t>(p->bwd.nout, 1);
   a.max_slots = std::max(p->bwd.max_slots, 1);
-  for (int ps = 0; ps < (int)p->bwd.passes.size(); ++ps) {
-    a.pass = ps;
-    rc = cuda_rc(launch_pass(MODE_BWD, kRBwd, a, p->bwd.L, batch, as_stream(stream)));
-    if (rc != TCG_OK) return rc;
-  }
+  rc = run_program(&p->bwd, MODE_BWD, kRBwd, a, batch, as_stream(stream));
+  if (rc != TCG_OK) return rc;
   if (plan->has_grad) {
     const uint32_t ntiles = 1u << (plan->n - p->bwd.L);
     rc = cuda_rc(launch_reduce_partials(a.partial, a.part_stride, ntiles, view.entries, view.nentries, batch,
@@ -307,11 +341,8 @@ int tcg_expect_pauli(const tcg_mplan* plan, const void* psi, int64_t batch, doub
     a.partial = part_tiles;
     a.part_stride = plan->nterms;
     a.max_slots = std::max(p->prog.max_slots, 1);
-    for (int ps = 0; ps < (int)p->prog.passes.size(); ++ps) {
-      a.pass = ps;
-      rc = cuda_rc(launch_pass(MODE_MEAS, kRFwd, a, p->prog.L, batch, st));
-      if (rc != TCG_OK) return rc;
-    }
+    rc = run_program(&p->prog, MODE_MEAS, kRFwd, a, batch, st);
+    if (rc != TCG_OK) return rc;
     rc = cuda_rc(launch_reduce_partials(part_tiles, plan->nterms, ntiles, view.entries, view.nentries, batch,
                                         nullptr, 0, out, plan->nterms, st));
     if (rc != TCG_OK) return rc;
@@ -348,11 +379,8 @@ int tcg_pauli_accumulate(const tcg_mplan* plan, const void* psi, void* mu, int64
     a.coef = coef;
     a.coef_stride = coef_stride;
     a.max_slots = 0;
-    for (int ps = 0; ps < (int)p->prog.passes.size(); ++ps) {
-      a.pass = ps;
-      rc = cuda_rc(launch_pass(MODE_PACC, kRFwd, a, p->prog.L, batch, st));
-      if (rc != TCG_OK) return rc;
-    }
+    rc = run_program(&p->prog, MODE_PACC, kRFwd, a, batch, st);
+    if (rc != TCG_OK) return rc;
   }
   if (!p->direct.empty())
     rc = cuda_rc(launch_direct_pacc(static_cast<const float2*>(psi), static_cast<float2*>(mu), plan->n, batch,
@@ -390,6 +418,29 @@ int tcg_inner(const void* a, const void* b, int64_t len, int64_t batch, double* 
   if (!scratch || scratch_bytes < tcg_inner_scratch_bytes(len, batch)) return TCG_ERR_SCRATCH;
   return cuda_rc(launch_inner(static_cast<const float2*>(a), static_cast<const float2*>(b), len, batch, out,
                               scratch, as_stream(stream)));
+}
+
+int tcg_debug_jit(const void* plan, int32_t which, int32_t mode, int32_t* state, char* text, int64_t cap,
+                  int32_t what) {
+  if (!plan || !state || mode < 0 || mode > 3) return TCG_ERR_INVALID_ARG;
+  Program* p = nullptr;
+  if (which == 0) p = &static_cast<tcg_plan*>(const_cast<void*>(plan))->fwd;
+  else if (which == 1) p = &static_cast<tcg_plan*>(const_cast<void*>(plan))->bwd;
+  else if (which == 2) p = &static_cast<tcg_mplan*>(const_cast<void*>(plan))->prog;
+  else return TCG_ERR_INVALID_ARG;
+  std::string s;
+  {
+    std::lock_guard<std::mutex> lk(p->jit_mu);
+    *state = !p->jit[mode] ? 0 : (p->jit[mode]->failed ? -1 : 1);
+    if (what == 0 && p->jit[mode]) s = p->jit[mode]->log;
+  }
+  if (what == 1) s = jit_source(*p, mode, mode == MODE_BWD ? kRBwd : kRFwd);
+  if (text && cap > 0) {
+    const size_t n = std::min<size_t>(s.size(), size_t(cap - 1));
+    std::memcpy(text, s.data(), n);
+    text[n] = 0;
+  }
+  return TCG_OK;
 }
 
 int tcg_debug_program(const void* plan, int32_t which, const void** arrays, int64_t* counts, int64_t* sizes) {

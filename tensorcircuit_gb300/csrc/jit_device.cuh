@@ -1,0 +1,377 @@
+// jit_device.cuh — device helpers for the specialised pass kernels.
+//
+// The specialiser (jit.cpp) turns a planned pass into straight-line CUDA that
+// calls these helpers with compile-time register positions, so every register
+// index is a constant and no op descriptor is read at run time.  This header
+// is compiled by NVRTC together with the generated code (it is embedded in the
+// library as a string) and must stay self-contained: no host headers.
+#pragma once
+
+typedef unsigned int u32;
+typedef unsigned long long u64;
+
+struct KParams {
+  float2* psi;
+  float2* mu;
+  const float2* mats;
+  long long mat_stride;
+  float2* partial;
+  long long part_stride;
+  const float* coef;
+  long long coef_stride;
+};
+
+namespace tk {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+// a * conj(b) + c
+__device__ __forceinline__ float2 cfmac(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.y, b.x, fmaf(-a.x, b.y, c.y)));
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 czero() { return make_float2(0.f, 0.f); }
+__device__ __forceinline__ float2 cone() { return make_float2(1.f, 0.f); }
+__device__ __forceinline__ float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 ld(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ u32 swz(u32 j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31u); }
+__device__ __forceinline__ float2 sel2(u32 i, float2 a, float2 b) { return i ? b : a; }
+__device__ __forceinline__ float2 sel4(u32 i, float2 a, float2 b, float2 c, float2 d) {
+  return (i & 2u) ? ((i & 1u) ? d : c) : ((i & 1u) ? b : a);
+}
+
+// ------------------------------------------------------------------ dense
+template <int NR, int P>
+__device__ __forceinline__ void dense1(float2 (&v)[NR], float2 m0, float2 m1, float2 m2, float2 m3) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    if (r & (1 << P)) continue;
+    const int r1 = r | (1 << P);
+    const float2 x0 = v[r], x1 = v[r1];
+    v[r] = cfma(m0, x0, cmul(m1, x1));
+    v[r1] = cfma(m2, x0, cmul(m3, x1));
+  }
+}
+
+template <int NR, int P, bool G>
+__device__ __forceinline__ void dense1_bwd(float2 (&v)[NR], float2 (&w)[NR], float2 a0, float2 a1, float2 a2,
+                                           float2 a3, float2 (&acc)[4]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    if (r & (1 << P)) continue;
+    const int r1 = r | (1 << P);
+    const float2 x0 = v[r], x1 = v[r1];
+    const float2 y0 = cfma(a0, x0, cmul(a1, x1));
+    const float2 y1 = cfma(a2, x0, cmul(a3, x1));
+    v[r] = y0;
+    v[r1] = y1;
+    const float2 u0 = w[r], u1 = w[r1];
+    if (G) {
+      acc[0] = cfmac(u0, y0, acc[0]);
+      acc[1] = cfmac(u0, y1, acc[1]);
+      acc[2] = cfmac(u1, y0, acc[2]);
+      acc[3] = cfmac(u1, y1, acc[3]);
+    }
+    w[r] = cfma(a0, u0, cmul(a1, u1));
+    w[r1] = cfma(a2, u0, cmul(a3, u1));
+  }
+}
+
+template <int NR, int P0, int P1>
+__device__ __forceinline__ void dense2(float2 (&v)[NR], const float2 (&m)[16]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    if (r & ((1 << P0) | (1 << P1))) continue;
+    const int i0 = r, i1 = r | (1 << P1), i2 = r | (1 << P0), i3 = r | (1 << P0) | (1 << P1);
+    const float2 x0 = v[i0], x1 = v[i1], x2 = v[i2], x3 = v[i3];
+    v[i0] = cfma(m[0], x0, cfma(m[1], x1, cfma(m[2], x2, cmul(m[3], x3))));
+    v[i1] = cfma(m[4], x0, cfma(m[5], x1, cfma(m[6], x2, cmul(m[7], x3))));
+    v[i2] = cfma(m[8], x0, cfma(m[9], x1, cfma(m[10], x2, cmul(m[11], x3))));
+    v[i3] = cfma(m[12], x0, cfma(m[13], x1, cfma(m[14], x2, cmul(m[15], x3))));
+  }
+}
+
+template <int NR, int P0, int P1, bool G>
+__device__ __forceinline__ void dense2_bwd(float2 (&v)[NR], float2 (&w)[NR], const float2 (&a)[16],
+                                           float2 (&acc)[16]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    if (r & ((1 << P0) | (1 << P1))) continue;
+    const int idx[4] = {r, r | (1 << P1), r | (1 << P0), r | (1 << P0) | (1 << P1)};
+    float2 y[4], u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      y[i] = cfma(a[4 * i], v[idx[0]], cfma(a[4 * i + 1], v[idx[1]], cfma(a[4 * i + 2], v[idx[2]],
+                                                                          cmul(a[4 * i + 3], v[idx[3]]))));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      v[idx[i]] = y[i];
+      u[i] = w[idx[i]];
+    }
+    if (G) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[4 * i + j] = cfmac(u[i], y[j], acc[4 * i + j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      w[idx[i]] = cfma(a[4 * i], u[0], cfma(a[4 * i + 1], u[1], cfma(a[4 * i + 2], u[2], cmul(a[4 * i + 3], u[3]))));
+  }
+}
+
+// k-qubit dense gate applied in place on the shared-memory tile (tile bits
+// tb[0..K-1], tb[0] = sub-index MSB); adj applies M^H.
+template <int K>
+__device__ __forceinline__ void denseK_smem(float2* tile, int L, const int* tb, const float2* m, bool adj, u32 tid,
+                                            u32 nthreads) {
+  constexpr int D = 1 << K;
+  const u32 ngroups = 1u << (L - K);
+  int srt[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) srt[i] = tb[i];
+#pragma unroll
+  for (int i = 0; i < K; ++i)
+#pragma unroll
+    for (int j = 0; j + 1 < K - i; ++j)
+      if (srt[j] > srt[j + 1]) {
+        const int t = srt[j];
+        srt[j] = srt[j + 1];
+        srt[j + 1] = t;
+      }
+  for (u32 g = tid; g < ngroups; g += nthreads) {
+    u32 j0 = g;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const u32 lowm = (1u << srt[i]) - 1u;
+      j0 = ((j0 & ~lowm) << 1) | (j0 & lowm);
+    }
+    float2 x[D];
+#pragma unroll
+    for (int s = 0; s < D; ++s) {
+      u32 j = j0;
+#pragma unroll
+      for (int i = 0; i < K; ++i)
+        if ((s >> (K - 1 - i)) & 1) j |= 1u << tb[i];
+      x[s] = tile[swz(j)];
+    }
+#pragma unroll
+    for (int s = 0; s < D; ++s) {
+      float2 y = czero();
+#pragma unroll 8
+      for (int t = 0; t < D; ++t) {
+        const float2 e = adj ? cconj(ld(m + t * D + s)) : ld(m + s * D + t);
+        y = cfma(e, x[t], y);
+      }
+      u32 j = j0;
+#pragma unroll
+      for (int i = 0; i < K; ++i)
+        if ((s >> (K - 1 - i)) & 1) j |= 1u << tb[i];
+      tile[swz(j)] = y;
+    }
+  }
+}
+
+// ----------------------------------------------------------------- diagonal
+// A k<=2 diagonal op whose sub-index bits come from register positions RB0,
+// RB1 (or -1: the bit is the run-time value t0 / t1 of this thread).  The
+// factor table e[] is selected once per thread; per amplitude the factor is a
+// compile-time pick.
+template <int RB0, int RB1>
+__device__ __forceinline__ int dsub(int r) {
+  return ((RB0 >= 0 ? ((r >> RB0) & 1) : 0) << 1) | (RB1 >= 0 ? ((r >> RB1) & 1) : 0);
+}
+
+template <int NR, int RB0, int RB1>
+__device__ __forceinline__ void diag2(float2 (&v)[NR], const float2* d, u32 t0, u32 t1, bool conj) {
+  float2 e[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const u32 b0 = RB0 >= 0 ? u32((s >> 1) & 1) : t0;
+    const u32 b1 = RB1 >= 0 ? u32(s & 1) : t1;
+    float2 x = ld(d + ((b0 << 1) | b1));
+    e[s] = conj ? cconj(x) : x;
+  }
+#pragma unroll
+  for (int r = 0; r < NR; ++r) v[r] = cmul(e[dsub<RB0, RB1>(r)], v[r]);
+}
+
+template <int NR, int RB0, int RB1, bool G>
+__device__ __forceinline__ void diag2_bwd(float2 (&v)[NR], float2 (&w)[NR], const float2* d, u32 t0, u32 t1,
+                                          float2 (&acc)[4]) {
+  float2 e[4], g[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const u32 b0 = RB0 >= 0 ? u32((s >> 1) & 1) : t0;
+    const u32 b1 = RB1 >= 0 ? u32(s & 1) : t1;
+    e[s] = cconj(ld(d + ((b0 << 1) | b1)));
+    g[s] = czero();
+  }
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const int s = dsub<RB0, RB1>(r);
+    const float2 y = cmul(e[s], v[r]);
+    v[r] = y;
+    if (G) g[s] = cfmac(w[r], y, g[s]);
+    w[r] = cmul(e[s], w[r]);
+  }
+  if (G) {
+    // bin s holds sub-index (b0(s) << 1 | b1(s)); move to output entries
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const u32 b0 = RB0 >= 0 ? u32((s >> 1) & 1) : t0;
+      const u32 b1 = RB1 >= 0 ? u32(s & 1) : t1;
+      const u32 o = (b0 << 1) | b1;
+      const bool live = (RB0 >= 0 || ((s >> 1) & 1) == 0) && (RB1 >= 0 || (s & 1) == 0);
+      if (live) {
+        acc[0] = (o == 0) ? make_float2(acc[0].x + g[s].x, acc[0].y + g[s].y) : acc[0];
+        acc[1] = (o == 1) ? make_float2(acc[1].x + g[s].x, acc[1].y + g[s].y) : acc[1];
+        acc[2] = (o == 2) ? make_float2(acc[2].x + g[s].x, acc[2].y + g[s].y) : acc[2];
+        acc[3] = (o == 3) ? make_float2(acc[3].x + g[s].x, acc[3].y + g[s].y) : acc[3];
+      }
+    }
+  }
+}
+
+// 1-qubit diagonal: same with a single sub-index bit
+template <int NR, int RB>
+__device__ __forceinline__ void diag1(float2 (&v)[NR], const float2* d, u32 t, bool conj) {
+  float2 e0 = ld(d + (RB >= 0 ? 0u : t)), e1 = ld(d + (RB >= 0 ? 1u : t));
+  if (conj) {
+    e0 = cconj(e0);
+    e1 = cconj(e1);
+  }
+#pragma unroll
+  for (int r = 0; r < NR; ++r) v[r] = cmul((RB >= 0 && ((r >> RB) & 1)) ? e1 : e0, v[r]);
+}
+
+template <int NR, int RB, bool G>
+__device__ __forceinline__ void diag1_bwd(float2 (&v)[NR], float2 (&w)[NR], const float2* d, u32 t,
+                                          float2 (&acc)[4]) {
+  const float2 e0 = cconj(ld(d + (RB >= 0 ? 0u : t))), e1 = cconj(ld(d + (RB >= 0 ? 1u : t)));
+  float2 g0 = czero(), g1 = czero();
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const bool hi = RB >= 0 && ((r >> RB) & 1);
+    const float2 y = cmul(hi ? e1 : e0, v[r]);
+    v[r] = y;
+    if (G) {
+      if (hi) g1 = cfmac(w[r], y, g1);
+      else g0 = cfmac(w[r], y, g0);
+    }
+    w[r] = cmul(hi ? e1 : e0, w[r]);
+  }
+  if (G) {
+    if (RB >= 0) {
+      acc[0] = g0;
+      acc[1] = g1;
+    } else {
+      acc[0] = t ? czero() : g0;
+      acc[1] = t ? g0 : czero();
+    }
+  }
+}
+
+// ----------------------------------------------------------------- Pauli terms
+// sum_r conj(v[r]) (-1)^{popc(r & ZR)} v[r ^ X]  (the run-time sign of the
+// thread's fixed bits is applied by the caller)
+template <int NR, int X, int ZR>
+__device__ __forceinline__ float2 expect(const float2 (&v)[NR]) {
+  float2 acc = czero();
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const float2 t = v[r ^ X];
+    const float cx = fmaf(v[r].x, t.x, v[r].y * t.y);
+    const float cy = fmaf(v[r].x, t.y, -v[r].y * t.x);
+    if (__builtin_popcount(r & ZR) & 1) {
+      acc.x -= cx;
+      acc.y -= cy;
+    } else {
+      acc.x += cx;
+      acc.y += cy;
+    }
+  }
+  return acc;
+}
+
+template <int NR, int X, int ZR>
+__device__ __forceinline__ void pacc(const float2 (&v)[NR], float2 (&w)[NR], float2 cf) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const float2 c = (__builtin_popcount(r & ZR) & 1) ? cneg(cf) : cf;
+    w[r] = cfma(c, v[r ^ X], w[r]);
+  }
+}
+
+// (-i)^nY
+__device__ __forceinline__ float2 ypow(int nY) {
+  return (nY & 3) == 0 ? make_float2(1.f, 0.f)
+       : (nY & 3) == 1 ? make_float2(0.f, -1.f)
+       : (nY & 3) == 2 ? make_float2(-1.f, 0.f) : make_float2(0.f, 1.f);
+}
+
+// ----------------------------------------------------------------- reductions
+// Sum E complex values (E a power of two <= 16) over the NL lanes of a warp.
+// Returns this lane's total and sets `entry` to the entry it holds, or -1 if
+// another lane writes that entry.  Full warps use a transpose-reduce (each
+// step keeps half of the entries and sends the other half to the partner
+// lane), which costs E + log2(32) shuffle pairs instead of E * log2(32).
+template <int E, int NL>
+__device__ __forceinline__ float2 warp_reduce(float2 (&a)[E], int lane, int& entry) {
+  constexpr unsigned FULL = NL >= 32 ? 0xffffffffu : ((1u << NL) - 1u);
+  if (E == 1 || NL < 32) {
+    // plain butterfly per entry; lane e returns entry e
+    entry = lane < E ? lane : -1;
+    float2 mine = czero();
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      float2 x = a[e];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        if (o < NL) {
+          x.x += __shfl_xor_sync(FULL, x.x, o);
+          x.y += __shfl_xor_sync(FULL, x.y, o);
+        }
+      }
+      if (lane == e) mine = x;
+    }
+    return mine;
+  } else {
+    // halve the entry set at each step: keep the half selected by the lane
+    // bit, send the other half; lane l ends with entry l >> (5 - log2 E)
+    constexpr int M = E == 2 ? 1 : E == 4 ? 2 : E == 8 ? 3 : E == 16 ? 4 : 5;
+    entry = (lane & ((32 >> M) - 1)) == 0 ? (lane >> (5 - M)) : -1;
+    float2 b[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) b[e] = a[e];
+    int cnt = E;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      if (cnt > 1) {
+        const int h = cnt >> 1;
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int e = 0; e < E / 2; ++e) {
+          if (e < h) {
+            const float2 keep = up ? b[e + h] : b[e];
+            const float2 send = up ? b[e] : b[e + h];
+            const float rx = __shfl_xor_sync(FULL, send.x, o);
+            const float ry = __shfl_xor_sync(FULL, send.y, o);
+            b[e] = make_float2(keep.x + rx, keep.y + ry);
+          }
+        }
+        cnt = h;
+      } else {
+        b[0].x += __shfl_xor_sync(FULL, b[0].x, o);
+        b[0].y += __shfl_xor_sync(FULL, b[0].y, o);
+      }
+    }
+    return b[0];
+  }
+}
+
+}  // namespace tk

@@ -30,6 +30,19 @@ struct PassArgs {
   int max_slots;
 };
 
+// Argument block of the specialised (generated) pass kernels; the same
+// layout as KParams in jit_device.cuh.
+struct KParams_Host {
+  float2* psi;
+  float2* mu;
+  const float2* mats;
+  long long mat_stride;
+  float2* partial;
+  long long part_stride;
+  const float* coef;
+  long long coef_stride;
+};
+
 // every kernel launch of the library increments this counter
 void count_launch(int64_t n = 1);
 int64_t launch_count();

@@ -6,8 +6,11 @@
 #include <string>
 #include <vector>
 
+#include <memory>
+
 #include "../../include/tcgb300.h"
 #include "engine.h"
+#include "jit.h"
 
 namespace tcg {
 
@@ -30,6 +33,11 @@ struct Program {
   struct DevCopy { void* base = nullptr; ProgramView view{}; };
   std::map<int, DevCopy> dev;
   std::mutex mu;
+
+  // specialised kernels per mode (jit.cpp), built on demand
+  std::unique_ptr<JitKernels> jit[4];
+  int calls[4] = {0, 0, 0, 0};
+  std::mutex jit_mu;
 };
 
 struct PlanOpts {

@@ -196,11 +196,19 @@ C64 = torch.complex64
 
 
 def _c(x: torch.Tensor) -> torch.Tensor:
-    return x.to(C64) if not x.is_complex() else x.to(C64)
+    return x.to(torch.complex128)
+
+
+def _hi(theta: torch.Tensor) -> torch.Tensor:
+    """Parameters are evaluated in double precision and the finished matrix
+    entries rounded to complex64 once: fp32 cos/sin leave each gate ~1e-7
+    away from unitary, and the adjoint sweep (uncompute through G^H) would
+    compound that over forward + backward."""
+    return theta.to(torch.complex128) if theta.is_complex() else theta.to(torch.float64)
 
 
 def _cs(theta: torch.Tensor, scale: float) -> Tuple[torch.Tensor, torch.Tensor]:
-    t = theta * scale
+    t = _hi(theta) * scale
     return torch.cos(t), torch.sin(t)
 
 
@@ -226,11 +234,12 @@ def build_rz(theta: torch.Tensor) -> torch.Tensor:  # diagonal
 
 
 def build_phase(theta: torch.Tensor) -> torch.Tensor:  # diagonal
-    e = torch.exp(J * _c(theta))
+    e = torch.exp(J * _c(_hi(theta)))
     return torch.stack([torch.ones_like(e), e], -1)
 
 
 def build_r(theta: torch.Tensor, alpha: torch.Tensor, phi: torch.Tensor) -> torch.Tensor:
+    theta, alpha, phi = _hi(theta), _hi(alpha), _hi(phi)
     ct, st = _c(torch.cos(theta)), _c(torch.sin(theta))
     ca, sa = _c(torch.cos(alpha)), _c(torch.sin(alpha))
     cp, sp = _c(torch.cos(phi)), _c(torch.sin(phi))
@@ -243,8 +252,8 @@ def build_r(theta: torch.Tensor, alpha: torch.Tensor, phi: torch.Tensor) -> torc
 def build_u(theta: torch.Tensor, phi: torch.Tensor, lbd: torch.Tensor) -> torch.Tensor:
     c, s = _cs(theta, 0.5)
     c, s = _c(c), _c(s)
-    ephi = torch.exp(J * _c(phi))
-    elbd = torch.exp(J * _c(lbd))
+    ephi = torch.exp(J * _c(_hi(phi)))
+    elbd = torch.exp(J * _c(_hi(lbd)))
     return torch.stack([c, -elbd * s, ephi * s, ephi * elbd * c], -1)
 
 
@@ -260,24 +269,24 @@ def build_iswap(theta: torch.Tensor) -> torch.Tensor:
 
 def build_exp1_dense(theta: torch.Tensor, unitary: torch.Tensor, half: bool) -> torch.Tensor:
     """``cos(t) I - i sin(t) U``; unitary [G, d, d] or [d, d]."""
-    t = theta * 0.5 if half else theta
+    t = _hi(theta) * 0.5 if half else _hi(theta)
     c, s = _c(torch.cos(t)), _c(torch.sin(t))
     u = _c(unitary)
     d = u.shape[-1]
-    eye = torch.eye(d, dtype=C64, device=u.device)
+    eye = torch.eye(d, dtype=torch.complex128, device=u.device)
     m = c[..., None, None] * eye - J * s[..., None, None] * u
     return m.reshape(m.shape[:-2] + (d * d,))
 
 
 def build_exp1_diag(theta: torch.Tensor, udiag: torch.Tensor, half: bool) -> torch.Tensor:
-    t = theta * 0.5 if half else theta
+    t = _hi(theta) * 0.5 if half else _hi(theta)
     c, s = _c(torch.cos(t)), _c(torch.sin(t))
     return c[..., None] - J * s[..., None] * _c(udiag)
 
 
 def build_exp_dense(theta: torch.Tensor, unitary: torch.Tensor) -> torch.Tensor:
     u = _c(unitary)
-    m = torch.linalg.matrix_exp(-J * _c(theta)[..., None, None] * u)
+    m = torch.linalg.matrix_exp(-J * _c(_hi(theta))[..., None, None] * u)
     d = u.shape[-1]
     return m.reshape(m.shape[:-2] + (d * d,))
 
@@ -285,7 +294,7 @@ def build_exp_dense(theta: torch.Tensor, unitary: torch.Tensor) -> torch.Tensor:
 def controlled_dense(m: torch.Tensor, d: int, ctrl_first_one: bool = True) -> torch.Tensor:
     """Embed U (entries [G, d*d]) as [[I, 0], [0, U]] (or [[U, 0], [0, I]])."""
     u = m.reshape(m.shape[:-1] + (d, d))
-    eye = torch.eye(d, dtype=C64, device=m.device).expand(u.shape)
+    eye = torch.eye(d, dtype=m.dtype, device=m.device).expand(u.shape)
     zero = torch.zeros_like(u)
     if ctrl_first_one:
         top = torch.cat([eye, zero], -1)
