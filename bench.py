@@ -157,7 +157,9 @@ def run_gb300_arm(args, rank, world):
         c = templates.apply_hea(tc.Circuit(n), n, nl, p)
         return templates.energy(c, terms)
 
-    vvag = K.vvag(f, argnums=0, vectorized_argnums=0)
+    # the reference's idiom (e.g. examples/bp_validation.py:55): K.jit(K.vvag(f));
+    # jit captures the step into a CUDA graph after its eager warm-up calls
+    vvag = K.jit(K.vvag(f, argnums=0, vectorized_argnums=0))
     params_host = torch.from_numpy(_workload_params()).pin_memory()
     params = params_host.to(dev)
 
@@ -165,14 +167,22 @@ def run_gb300_arm(args, rank, world):
         if world > 1:
             torch.distributed.barrier()
 
-    for _ in range(max(args.warmup, 1)):
+    # warm-up: the jit wrapper runs 3 eager calls, then captures the graph;
+    # every warm-up call is untimed
+    warmup = max(args.warmup, 5)
+    for _ in range(warmup):
         v, g = vvag(params)
     torch.cuda.synchronize()
+    # engine kernels per step: count the launches of one eager step (graph
+    # replays launch the same kernels without passing through the host code)
+    l0 = lib.tcg_launch_count()
+    K.vvag(f, argnums=0, vectorized_argnums=0)(params)
+    torch.cuda.synchronize()
+    launches_per_step = lib.tcg_launch_count() - l0
 
     # ---- device-resident value
     barrier()
     torch.cuda.synchronize()
-    l0 = lib.tcg_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
         ev0.record()
@@ -180,7 +190,7 @@ def run_gb300_arm(args, rank, world):
             v, g = vvag(params)
         ev1.record()
         torch.cuda.synchronize()
-    launches = (lib.tcg_launch_count() - l0) // args.steps
+    launches = launches_per_step * args.steps
     ms = ev0.elapsed_time(ev1) / args.steps
     barrier()
 
@@ -285,7 +295,7 @@ def run_gb300_arm(args, rank, world):
         cpu = cpu_reference(steps=1, warmup=0)
     line = {
         "metric": METRIC, "value": circ_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n_qubits": n, "layers": nl, "params": int(params.shape[1]),
                    "batch_per_gpu": BATCH, "parallelism": "replicas" if world > 1 else "single",
@@ -301,6 +311,7 @@ def run_gb300_arm(args, rank, world):
         "e2e": {"value": circ_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
+        "gpu_launches_per_step": int(launches_per_step),
     }
     print(json.dumps(line), flush=True)
 

@@ -97,6 +97,8 @@ class _PlanEntry:
                  gates_c: Optional[List[Any]] = None) -> None:
         self.plan = plan
         self.gates_c = gates_c or []  # (kind, qubits, mat_off, grad_off) per gate
+        # Pauli terms the last circuit of this structure asked for, in order
+        self.last_terms: Optional[List[Tuple[int, int]]] = None
         self.const_np = const_block
         self.const_dev: Dict[int, torch.Tensor] = {}
         self.groups = groups  # (gkey, op indices, E)
@@ -185,6 +187,14 @@ def _stack_scalars(vals: Sequence[Any], dev: torch.device) -> torch.Tensor:
         if np.iscomplexobj(arr):
             return torch.as_tensor(arr.astype(np.complex64), device=dev)
         return torch.as_tensor(arr.astype(np.float32), device=dev)
+    if all(isinstance(v, torch.Tensor) for v in vals):
+        v0 = vals[0]
+        if all(v.dtype == v0.dtype and v.device == v0.device and v.dim() == 0 for v in vals) and \
+                v0.dtype in (torch.float32, torch.float64, torch.complex64, torch.complex128):
+            # one stack op; no per-parameter casts (each torch op costs tens of
+            # microseconds under torch.func transforms)
+            t = torch.stack(list(vals))
+            return t if t.device == dev else t.to(dev)
     cplx = any(v.is_complex() if isinstance(v, torch.Tensor) else np.iscomplexobj(v) for v in vals)
     dt = torch.complex64 if cplx else torch.float32
     ts = []
@@ -264,6 +274,11 @@ class Circuit:
         self._extra_qir: List[Dict[str, Any]] = []
         self._ops: List[_Op] = []
         self._cache: Optional[Tuple[Any, ...]] = None
+        # Pauli terms requested from this circuit's state, in order; the next
+        # circuit with the same structure uses the list as its prediction
+        self._req_terms: List[Tuple[int, int]] = []
+        self._pred_terms: Optional[List[Tuple[int, int]]] = None
+        self._term_batch: Optional[torch.Tensor] = None
 
     # ------------------------------------------------------------------ gates
     def _norm_index(self, index: Sequence[int]) -> Tuple[int, ...]:
@@ -279,6 +294,9 @@ class Circuit:
         self._qir.append(ir)
         self._ops.append(op)
         self._cache = None
+        self._req_terms = []
+        self._pred_terms = None
+        self._term_batch = None
 
     def _apply_const(self, name: str, index: Sequence[int], ir_extra: Optional[Dict[str, Any]] = None) -> None:
         idx = self._norm_index(index)
@@ -430,6 +448,10 @@ class Circuit:
             psi0 = inp
         run = eng.Run(entry.plan, n_eng)
         psi_eng, anchor = eng.StateFn.apply(mats, psi0, run)
+        self._req_terms = []
+        self._term_batch = None
+        self._pred_terms = entry.last_terms
+        entry.last_terms = self._req_terms
         psi = psi_eng if pad == 0 else psi_eng.reshape(psi_eng.shape[:-1] + (N, 1 << pad))[..., 0]
         self._cache = (psi, psi_eng, anchor, run, n_eng)
         return self._cache  # type: ignore
@@ -497,6 +519,27 @@ class Circuit:
             x, y, z = d.get("x", None), d.get("y", None), d.get("z", None)
         _, psi_eng, anchor, run, n_eng = self._engine_state()
         term = self._pauli_term(x or [], y or [], z or [], n_eng)
+        return self._expect_pauli(term)
+
+    def _expect_pauli(self, term: Tuple[int, int]) -> Tensor:
+        """<P> for one Pauli term (masks over the engine's index bits).
+
+        VQE-style code asks a circuit for the same list of terms every step
+        (one ``expectation_ps`` per Hamiltonian term, as in the reference's
+        benchmarks/scripts/vqe_tc.py:75-81).  The first request evaluates every
+        term the previous circuit of this structure asked for in ONE
+        measurement plan (a few reads of the state instead of one read per
+        term); a request returns a slice of that batch only when it is exactly
+        the predicted term at that position, otherwise it is evaluated on its
+        own."""
+        _, psi_eng, anchor, run, n_eng = self._engine_state()
+        i = len(self._req_terms)
+        self._req_terms.append(term)
+        pred = self._pred_terms
+        if pred is not None and len(pred) > 1 and i < len(pred) and pred[i] == term:
+            if self._term_batch is None:
+                self._term_batch = eng.ExpectFn.apply(psi_eng, anchor, tuple(pred), run)
+            return self._term_batch[..., i]
         return eng.ExpectFn.apply(psi_eng, anchor, (term,), run)[..., 0]
 
     def expectation_ps_batch(self, terms: Sequence[Dict[str, Sequence[int]]]) -> Tensor:
@@ -545,8 +588,7 @@ class Circuit:
                 general.append((op, idx))
         psi, psi_eng, anchor, run, n_eng = self._engine_state()
         if not general:
-            term = eng.pauli_masks(n_eng, xs, ys, zs)
-            return eng.ExpectFn.apply(psi_eng, anchor, (term,), run)[..., 0]
+            return self._expect_pauli(eng.pauli_masks(n_eng, xs, ys, zs))
         # general operators: phi = O psi through a forward sweep on a copy
         c = Circuit(n, inputs=psi)
         for op, idx in general:

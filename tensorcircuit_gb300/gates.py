@@ -326,6 +326,21 @@ class Family:
         return (1 << self.nq) if self.diag else (1 << (2 * self.nq))
 
 
+_DEV_CONSTS: Dict[Tuple[str, str], torch.Tensor] = {}
+
+
+def device_const(name: str, m: np.ndarray, device: torch.device) -> torch.Tensor:
+    """A constant matrix on ``device``, copied from the host once; later
+    uses (including under CUDA-graph capture, where a host-to-device copy is
+    not allowed) reuse the device copy."""
+    key = (name, str(device))
+    t = _DEV_CONSTS.get(key)
+    if t is None:
+        t = torch.as_tensor(np.array(m, dtype=np.complex128), device=device)
+        _DEV_CONSTS[key] = t
+    return t
+
+
 def _ctrl(f: Callable[..., torch.Tensor], base_nq: int, diag: bool, one: bool) -> Callable[..., torch.Tensor]:
     d = 1 << base_nq
 
@@ -345,11 +360,11 @@ FAMILIES: Dict[str, Family] = {
     "u": Family("u", 1, False, [("theta", 0.0), ("phi", 0.0), ("lbd", 0.0)], build_u),
     "iswap": Family("iswap", 2, False, [("theta", 1.0)], build_iswap),
     "rxx": Family("rxx", 2, False, [("theta", 0.0)],
-                  lambda t: build_exp1_dense(t, torch.as_tensor(_xx_matrix, dtype=C64, device=t.device), True)),
+                  lambda t: build_exp1_dense(t, device_const("xx", _xx_matrix, t.device), True)),
     "ryy": Family("ryy", 2, False, [("theta", 0.0)],
-                  lambda t: build_exp1_dense(t, torch.as_tensor(_yy_matrix, dtype=C64, device=t.device), True)),
+                  lambda t: build_exp1_dense(t, device_const("yy", _yy_matrix, t.device), True)),
     "rzz": Family("rzz", 2, True, [("theta", 0.0)],
-                  lambda t: build_exp1_diag(t, torch.as_tensor(np.diag(_zz_matrix).copy(), dtype=C64, device=t.device), True)),
+                  lambda t: build_exp1_diag(t, device_const("zzdiag", np.diag(_zz_matrix), t.device), True)),
     "crx": Family("crx", 2, False, [("theta", 0.0)], _ctrl(build_rx, 1, False, True)),
     "cry": Family("cry", 2, False, [("theta", 0.0)], _ctrl(build_ry, 1, False, True)),
     "crz": Family("crz", 2, True, [("theta", 0.0)], _ctrl(build_rz, 1, True, True)),

@@ -310,3 +310,47 @@ def test_large_state_properties(tc):
     assert abs(back[0].item() - 1.0) < 1e-4
     zz = c.expectation_ps(z=[0, n - 1]).real.item()
     assert -1.0001 <= zz <= 1.0001
+
+
+def test_backend_jit_graph_replay_matches_eager(tc):
+    """K.jit(K.vvag(f)) captures a CUDA graph after its warm-up calls; every
+    replay must use the new inputs and agree with the eager call."""
+    from tensorcircuit_gb300 import templates
+
+    K_ = tc.set_backend("pytorch")
+    n, nl, B = 11, 2, 6
+    terms = templates.tfim_terms(n, -1.0, -1.0)
+
+    def f(p):
+        c = templates.apply_hea(tc.Circuit(n), n, nl, p)
+        return templates.energy(c, terms)
+
+    eager = K_.vvag(f)
+    jitted = K_.jit(K_.vvag(f))
+    rng = np.random.default_rng(9)
+    for it in range(7):
+        p = torch.tensor(rng.uniform(0, 2 * np.pi, (B, templates.hea_nparams(n, nl))), dtype=torch.float32,
+                         device="cuda")
+        v1, g1 = jitted(p)
+        v0, g0 = eager(p)
+        np.testing.assert_allclose(v1.cpu().numpy(), v0.cpu().numpy(), atol=1e-6)
+        np.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=1e-5)
+    ent = list(jitted.cache.values())[0]
+    assert ent["graph"] is not None and not ent["failed"]
+
+
+def test_expectation_batching_follows_requests(tc):
+    """Repeated circuits of one structure batch their expectation_ps calls;
+    a request that differs from the predicted sequence is still exact."""
+    from tensorcircuit_gb300 import templates
+
+    n = 8
+    gl = templates.hea_gate_list(n, 2, np.linspace(0.1, 2.0, templates.hea_nparams(n, 2)))
+    psi = sv.run_circuit(n, gl)
+    seqs = [[{"z": [0, 1]}, {"x": [3]}, {"y": [2], "z": [5]}],
+            [{"z": [0, 1]}, {"x": [3]}, {"y": [2], "z": [5]}],
+            [{"z": [0, 1]}, {"x": [4]}, {"y": [2], "z": [5]}, {"x": [7]}]]
+    for seq in seqs:
+        c = templates.apply_gate_list(tc.Circuit(n), gl)
+        for s in seq:
+            np.testing.assert_allclose(c.expectation_ps(**s).item(), sv.expectation_ps(psi, n, **s), atol=2e-5)
