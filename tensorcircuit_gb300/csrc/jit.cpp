@@ -60,27 +60,43 @@ bool same_layout(const Layout& a, const Layout& b) {
     if (a.thr_tile[i] != b.thr_tile[i]) return false;
   return true;
 }
+// Host mirror of the op record the generated kernels read from constant
+// memory (one per op; the kind and compile-time register positions live in
+// the signature `sig`, the rest are run-time operands).
+struct OpRec {
+  long long off;  // matrix offset (gates) or term / coefficient index (Pauli)
+  int sig;        // index of the compiled body
+  int slot;       // first accumulator slot, -1 = none
+  int g0, g1;     // global bits of a diagonal op's sub-index (run-time part)
+  unsigned zm;    // Pauli Z/Y mask (global bits)
+  int ny;         // number of Y factors
+  int zr;         // register-position mask of the Z/Y bits
+  int pad;
+};
 
 class Gen {
  public:
   Gen(const Program& P, int mode, int R) : P_(P), mode_(mode), R_(R) {}
 
-  std::string source() {
-    std::ostringstream& o = os_;
+  // Returns false when the op tables do not fit the 64 KiB constant bank.
+  bool source(std::string* out) {
+    std::ostringstream o;
     o << "// generated by the tcgb300 plan specialiser: n=" << P_.n << " mode=" << mode_ << "\n";
-    for (size_t p = 0; p < P_.passes.size(); ++p) pass(int(p));
-    return o.str();
+    o << "struct OpRec { long long off; int sig; int slot; int g0; int g1; unsigned zm; int ny; int zr; int pad; };\n";
+    size_t cbytes = 0;
+    for (size_t p = 0; p < P_.passes.size(); ++p) cbytes += pass(o, int(p));
+    *out = o.str();
+    return cbytes <= 60 * 1024;
   }
 
  private:
   const Program& P_;
   int mode_, R_;
-  std::ostringstream os_;
-  // per-pass state
   const DevPass* dp_ = nullptr;
   int L_ = 0, NT_ = 0, NR_ = 0, NL_ = 0, NW_ = 0, MS_ = 1;
   bool has_mu_ = false;
-  Layout cur_;
+  std::map<std::string, int> sig_id_;
+  std::vector<std::string> sig_body_;
 
   bool fwd() const { return mode_ == MODE_FWD; }
   bool bwd() const { return mode_ == MODE_BWD; }
@@ -100,47 +116,55 @@ class Gen {
       if ((r >> i) & 1) o |= gbit(l.reg_tile[i]);
     return o;
   }
-  // register position holding global bit g in layout l, or -1
   int regpos(const Layout& l, int g) const {
     for (int i = 0; i < l.R; ++i)
       if (dp_->lbits[l.reg_tile[i]] == g) return i;
     return -1;
   }
 
-  void layout_code(const Layout& l) {
-    std::ostringstream& o = os_;
-    o << "  jt = 0u; gt = 0u;\n";
+  int sig(const std::string& body) {
+    auto it = sig_id_.find(body);
+    if (it != sig_id_.end()) return it->second;
+    const int id = (int)sig_body_.size();
+    sig_id_[body] = id;
+    sig_body_.push_back(body);
+    return id;
+  }
+
+  // ------------------------------------------------------------ data moves
+  void layout_code(std::ostream& o, const Layout& l) {
+    o << "      jt = 0u; gt = 0u;\n";
     for (int i = 0; i < l.nthr; ++i)
-      o << "  jt |= ((tid >> " << i << ") & 1u) << " << l.thr_tile[i] << "; gt |= ((tid >> " << i
+      o << "      jt |= ((tid >> " << i << ") & 1u) << " << l.thr_tile[i] << "; gt |= ((tid >> " << i
         << ") & 1u) << " << dp_->lbits[l.thr_tile[i]] << ";\n";
-    o << "  sjt = swz(jt);\n";
+    o << "      sjt = swz(jt);\n";
   }
-  void regs_from_smem(const Layout& l, bool mu) {
+  void regs_from_smem(std::ostream& o, const Layout& l, bool mu) {
     for (int r = 0; r < NR_; ++r) {
-      os_ << "  v[" << r << "] = smp[sjt ^ " << host_swz(tr(l, r)) << "u];";
-      if (mu) os_ << " w[" << r << "] = smu[sjt ^ " << host_swz(tr(l, r)) << "u];";
-      os_ << "\n";
+      o << "      v[" << r << "] = smp[sjt ^ " << host_swz(tr(l, r)) << "u];";
+      if (mu) o << " w[" << r << "] = smu[sjt ^ " << host_swz(tr(l, r)) << "u];";
+      o << "\n";
     }
   }
-  void regs_to_smem(const Layout& l, bool psi, bool mu) {
+  void regs_to_smem(std::ostream& o, const Layout& l, bool psi, bool mu) {
     for (int r = 0; r < NR_; ++r) {
-      if (psi) os_ << "  smp[sjt ^ " << host_swz(tr(l, r)) << "u] = v[" << r << "];";
-      if (mu) os_ << " smu[sjt ^ " << host_swz(tr(l, r)) << "u] = w[" << r << "];";
-      os_ << "\n";
+      if (psi) o << "      smp[sjt ^ " << host_swz(tr(l, r)) << "u] = v[" << r << "];";
+      if (mu) o << " smu[sjt ^ " << host_swz(tr(l, r)) << "u] = w[" << r << "];";
+      o << "\n";
     }
   }
-  void regs_from_global(const Layout& l, bool mu) {
+  void regs_from_global(std::ostream& o, const Layout& l, bool mu) {
     for (int r = 0; r < NR_; ++r) {
-      os_ << "  v[" << r << "] = S[gt + " << gr(l, r) << "u];";
-      if (mu) os_ << " w[" << r << "] = U[gt + " << gr(l, r) << "u];";
-      os_ << "\n";
+      o << "      v[" << r << "] = S[gt + " << gr(l, r) << "u];";
+      if (mu) o << " w[" << r << "] = U[gt + " << gr(l, r) << "u];";
+      o << "\n";
     }
   }
-  void regs_to_global(const Layout& l, bool psi, bool mu) {
+  void regs_to_global(std::ostream& o, const Layout& l, bool psi, bool mu) {
     for (int r = 0; r < NR_; ++r) {
-      if (psi) os_ << "  S[gt + " << gr(l, r) << "u] = v[" << r << "];";
-      if (mu) os_ << " U[gt + " << gr(l, r) << "u] = w[" << r << "];";
-      os_ << "\n";
+      if (psi) o << "  S[gt + " << gr(l, r) << "u] = v[" << r << "];";
+      if (mu) o << " U[gt + " << gr(l, r) << "u] = w[" << r << "];";
+      o << "\n";
     }
   }
   std::string off_expr() const {
@@ -149,20 +173,18 @@ class Gen {
     for (int q = kLo; q < L_; ++q) e << " | (((j >> " << q << ") & 1u) << " << dp_->lbits[q] << ")";
     return e.str();
   }
-  void staged_load(bool psi, bool mu) {
-    std::ostringstream& o = os_;
-    o << "  for (u32 i = tid; i < " << (1u << (L_ - 1)) << "u; i += " << NT_ << "u) {\n";
-    o << "    const u32 j = 2u * i; const u32 off = " << off_expr() << ";\n";
+  void staged_load(std::ostream& o, bool psi, bool mu) {
+    o << "      for (u32 i = tid; i < " << (1u << (L_ - 1)) << "u; i += " << NT_ << "u) {\n";
+    o << "        const u32 j = 2u * i; const u32 off = " << off_expr() << ";\n";
     if (psi)
-      o << "    { const float4 q = *reinterpret_cast<const float4*>(S + off); smp[swz(j)] = "
+      o << "        { const float4 q = *reinterpret_cast<const float4*>(S + off); smp[swz(j)] = "
            "make_float2(q.x, q.y); smp[swz(j + 1u)] = make_float2(q.z, q.w); }\n";
     if (mu)
-      o << "    { const float4 q = *reinterpret_cast<const float4*>(U + off); smu[swz(j)] = "
+      o << "        { const float4 q = *reinterpret_cast<const float4*>(U + off); smu[swz(j)] = "
            "make_float2(q.x, q.y); smu[swz(j + 1u)] = make_float2(q.z, q.w); }\n";
-    o << "  }\n";
+    o << "      }\n";
   }
-  void staged_store(bool psi, bool mu) {
-    std::ostringstream& o = os_;
+  void staged_store(std::ostream& o, bool psi, bool mu) {
     o << "  for (u32 i = tid; i < " << (1u << (L_ - 1)) << "u; i += " << NT_ << "u) {\n";
     o << "    const u32 j = 2u * i; const u32 off = " << off_expr() << ";\n";
     if (psi)
@@ -174,93 +196,94 @@ class Gen {
     o << "  }\n";
   }
 
-  void reduce_to_slot(int E, const char* arr, int slot) {
-    os_ << "    { int ent; const float2 t = warp_reduce<" << E << ", " << NL_ << ">(" << arr
-        << ", lane, ent); if (ent >= 0) sms[warp * " << MS_ << " + " << slot << " + ent] = t; }\n";
+  std::string reduce(int E, const char* arr) const {
+    std::ostringstream o;
+    o << " { int ent; const float2 t = warp_reduce<" << E << ", " << NL_ << ">(" << arr
+      << ", lane, ent); if (ent >= 0) sms[warp * " << MS_ << " + op.slot + ent] = t; }";
+    return o.str();
   }
 
-  void op_code(const DevOp& op) {
-    std::ostringstream& o = os_;
-    const Layout& l = cur_;
-    o << "  {\n";
+  // Body (signature) and record of one register-stage op.  Returns false
+  // for ops without a shared body (wide diagonals): their code goes
+  // straight into the stage's case.
+  void op_sig(const DevOp& op, const Layout& l, OpRec* rec, bool* usesC) {
+    std::memset(rec, 0, sizeof(*rec));
+    rec->off = op.mat_off;
+    rec->slot = op.slot;
+    std::ostringstream b;
     if (op.kind == OP_DENSE1) {
-      o << "    const float2* m = Mt + " << op.mat_off << "ll;\n";
       if (fwd()) {
-        o << "    dense1<" << NR_ << ", " << op.p[0] << ">(v, ld(m), ld(m + 1), ld(m + 2), ld(m + 3));\n";
+        b << "const float2* m = Mt + op.off; dense1<" << NR_ << ", " << op.p[0]
+          << ">(v, ld(m), ld(m + 1), ld(m + 2), ld(m + 3));";
       } else {
         const bool G = op.slot >= 0;
-        o << "    float2 acc[4] = {czero(), czero(), czero(), czero()};\n";
-        o << "    dense1_bwd<" << NR_ << ", " << op.p[0] << ", " << (G ? "true" : "false")
-          << ">(v, w, cconj(ld(m)), cconj(ld(m + 2)), cconj(ld(m + 1)), cconj(ld(m + 3)), acc);\n";
-        if (G) reduce_to_slot(4, "acc", op.slot);
+        b << "const float2* m = Mt + op.off; float2 acc[4] = {czero(), czero(), czero(), czero()}; dense1_bwd<"
+          << NR_ << ", " << op.p[0] << ", " << (G ? "true" : "false")
+          << ">(v, w, cconj(ld(m)), cconj(ld(m + 2)), cconj(ld(m + 1)), cconj(ld(m + 3)), acc);";
+        if (G) b << reduce(4, "acc");
       }
     } else if (op.kind == OP_DENSE2) {
-      o << "    const float2* m = Mt + " << op.mat_off << "ll;\n";
       if (fwd()) {
-        o << "    float2 mm[16];\n#pragma unroll\n    for (int e = 0; e < 16; ++e) mm[e] = ld(m + e);\n";
-        o << "    dense2<" << NR_ << ", " << op.p[0] << ", " << op.p[1] << ">(v, mm);\n";
+        b << "const float2* m = Mt + op.off; float2 mm[16];\n#pragma unroll\n for (int e = 0; e < 16; ++e) mm[e] = "
+             "ld(m + e); dense2<"
+          << NR_ << ", " << op.p[0] << ", " << op.p[1] << ">(v, mm);";
       } else {
         const bool G = op.slot >= 0;
-        o << "    float2 a[16];\n#pragma unroll\n    for (int i = 0; i < 4; ++i)\n#pragma unroll\n"
-             "      for (int j = 0; j < 4; ++j) a[4 * i + j] = cconj(ld(m + 4 * j + i));\n";
-        o << "    float2 acc[16];\n#pragma unroll\n    for (int e = 0; e < 16; ++e) acc[e] = czero();\n";
-        o << "    dense2_bwd<" << NR_ << ", " << op.p[0] << ", " << op.p[1] << ", " << (G ? "true" : "false")
-          << ">(v, w, a, acc);\n";
-        if (G) reduce_to_slot(16, "acc", op.slot);
+        b << "const float2* m = Mt + op.off; float2 a[16];\n#pragma unroll\n for (int i = 0; i < 4; ++i)\n#pragma "
+             "unroll\n for (int j = 0; j < 4; ++j) a[4 * i + j] = cconj(ld(m + 4 * j + i)); float2 acc[16];\n"
+             "#pragma unroll\n for (int e = 0; e < 16; ++e) acc[e] = czero(); dense2_bwd<"
+          << NR_ << ", " << op.p[0] << ", " << op.p[1] << ", " << (G ? "true" : "false") << ">(v, w, a, acc);";
+        if (G) b << reduce(16, "acc");
       }
     } else if (op.kind == OP_DIAG) {
       const int k = op.k;
       int rb[6];
       for (int i = 0; i < k; ++i) rb[i] = regpos(l, op.p[i]);
-      o << "    const float2* d = Mt + " << op.mat_off << "ll;\n";
+      rec->g0 = op.p[0];
+      rec->g1 = k > 1 ? op.p[1] : 0;
+      const char* t0 = "((gthr >> op.g0) & 1u)";
+      const char* t1 = "((gthr >> op.g1) & 1u)";
       if (k <= 2) {
-        std::ostringstream t0, t1;
-        t0 << "((gthr >> " << op.p[0] << ") & 1u)";
-        if (k == 2) t1 << "((gthr >> " << op.p[1] << ") & 1u)";
+        const bool scalar = (k == 1) ? rb[0] < 0 : (rb[0] < 0 && rb[1] < 0);
         if (fwd()) {
-          bool scalar = (k == 1) ? rb[0] < 0 : (rb[0] < 0 && rb[1] < 0);
           if (scalar) {
-            if (k == 1) o << "    C = cmul(C, ld(d + " << t0.str() << "));\n";
-            else o << "    C = cmul(C, ld(d + ((" << t0.str() << " << 1) | " << t1.str() << ")));\n";
-            uses_c_ = true;
+            if (k == 1) b << "C = cmul(C, ld(Mt + op.off + " << t0 << "));";
+            else b << "C = cmul(C, ld(Mt + op.off + ((" << t0 << " << 1) | " << t1 << ")));";
+            *usesC = true;
           } else if (k == 1) {
-            o << "    diag1<" << NR_ << ", " << rb[0] << ">(v, d, " << t0.str() << ", false);\n";
+            b << "diag1<" << NR_ << ", " << rb[0] << ">(v, Mt + op.off, " << t0 << ", false);";
           } else {
-            o << "    diag2<" << NR_ << ", " << rb[0] << ", " << rb[1] << ">(v, d, " << t0.str() << ", "
-              << t1.str() << ", false);\n";
+            b << "diag2<" << NR_ << ", " << rb[0] << ", " << rb[1] << ">(v, Mt + op.off, " << t0 << ", " << t1
+              << ", false);";
           }
-        } else {  // BWD
+        } else {
           const bool G = op.slot >= 0;
-          o << "    float2 acc[4] = {czero(), czero(), czero(), czero()};\n";
+          b << "float2 acc[4] = {czero(), czero(), czero(), czero()}; ";
           if (k == 1) {
-            o << "    diag1_bwd<" << NR_ << ", " << rb[0] << ", " << (G ? "true" : "false") << ">(v, w, d, "
-              << t0.str() << ", acc);\n";
-            if (G) {
-              o << "    float2 a2[2] = {acc[0], acc[1]};\n";
-              reduce_to_slot(2, "a2", op.slot);
-            }
+            b << "diag1_bwd<" << NR_ << ", " << rb[0] << ", " << (G ? "true" : "false") << ">(v, w, Mt + op.off, "
+              << t0 << ", acc);";
+            if (G) b << " float2 a2[2] = {acc[0], acc[1]};" << reduce(2, "a2");
           } else {
-            o << "    diag2_bwd<" << NR_ << ", " << rb[0] << ", " << rb[1] << ", " << (G ? "true" : "false")
-              << ">(v, w, d, " << t0.str() << ", " << t1.str() << ", acc);\n";
-            if (G) reduce_to_slot(4, "acc", op.slot);
+            b << "diag2_bwd<" << NR_ << ", " << rb[0] << ", " << rb[1] << ", " << (G ? "true" : "false")
+              << ">(v, w, Mt + op.off, " << t0 << ", " << t1 << ", acc);";
+            if (G) b << reduce(4, "acc");
           }
         }
       } else {
-        // wide diagonal (no gradient): run-time part of the index once,
-        // register part per amplitude as a literal
-        o << "    const u32 rt = 0u";
+        // wide diagonal (no gradient): literal per-op code
+        b << "const float2* d = Mt + " << op.mat_off << "ll; const u32 rt = 0u";
         for (int i = 0; i < k; ++i)
-          if (rb[i] < 0) o << " | (((gthr >> " << op.p[i] << ") & 1u) << " << (k - 1 - i) << ")";
-        o << ";\n";
+          if (rb[i] < 0) b << " | (((gthr >> " << op.p[i] << ") & 1u) << " << (k - 1 - i) << ")";
+        b << ";";
         for (int r = 0; r < NR_; ++r) {
           uint32_t c = 0;
           for (int i = 0; i < k; ++i)
             if (rb[i] >= 0 && ((r >> rb[i]) & 1)) c |= 1u << (k - 1 - i);
           if (fwd()) {
-            o << "    v[" << r << "] = cmul(ld(d + (rt | " << c << "u)), v[" << r << "]);\n";
+            b << " v[" << r << "] = cmul(ld(d + (rt | " << c << "u)), v[" << r << "]);";
           } else {
-            o << "    { const float2 e = cconj(ld(d + (rt | " << c << "u))); v[" << r << "] = cmul(e, v[" << r
-              << "]); w[" << r << "] = cmul(e, w[" << r << "]); }\n";
+            b << " { const float2 e = cconj(ld(d + (rt | " << c << "u))); v[" << r << "] = cmul(e, v[" << r
+              << "]); w[" << r << "] = cmul(e, w[" << r << "]); }";
           }
         }
       }
@@ -268,42 +291,26 @@ class Gen {
       int zr = 0;
       for (int i = 0; i < l.R; ++i)
         if (gbit(l.reg_tile[i]) & op.zmask) zr |= 1 << i;
+      rec->zm = op.zmask;
+      rec->ny = op.nY;
+      rec->zr = zr;
       if (meas()) {
-        o << "    float2 acc = expect<" << NR_ << ", " << op.xreg << ", " << zr << ">(v);\n";
-        o << "    if (__popc(gthr & " << op.zmask << "u) & 1) acc = cneg(acc);\n";
-        o << "    acc = cmul(ypow(" << op.nY << "), acc);\n";
-        o << "    float2 a1[1] = {acc};\n";
-        reduce_to_slot(1, "a1", op.slot);
+        b << "float2 acc = expectz<" << NR_ << ", " << op.xreg
+          << ">(v, op.zr); if (__popc(gthr & op.zm) & 1) acc = cneg(acc); acc = cmul(ypow(op.ny), acc); "
+             "float2 a1[1] = {acc};"
+          << reduce(1, "a1");
       } else {
-        o << "    float2 cf = cmul(ypow(" << op.nY << "), make_float2(kp.coef[b * kp.coef_stride + " << op.mat_off
-          << "ll], 0.f));\n";
-        o << "    if (__popc(gthr & " << op.zmask << "u) & 1) cf = cneg(cf);\n";
-        o << "    pacc<" << NR_ << ", " << op.xreg << ", " << zr << ">(v, w, cf);\n";
+        b << "float2 cf = cmul(ypow(op.ny), make_float2(kp.coef[b * kp.coef_stride + op.off], 0.f)); if "
+             "(__popc(gthr & op.zm) & 1) cf = cneg(cf); paccz<"
+          << NR_ << ", " << op.xreg << ">(v, w, cf, op.zr);";
       }
     }
-    o << "  }\n";
+    rec->sig = sig(b.str());
   }
 
-  void flush_slots(const DevStage& S) {
-    std::ostringstream& o = os_;
-    o << "  __syncthreads();\n";
-    const uint64_t ntiles = 1ull << (P_.n - L_);
-    for (int e = S.slot_out_begin; e < S.slot_out_end; ++e) {
-      const SlotOut& so = P_.slot_out[e];
-      const int te = (e - S.slot_out_begin) % NT_;
-      o << "  if (tid == " << te << "u) { float2 t = czero();";
-      for (int q = 0; q < NW_; ++q)
-        o << " { const float2 x = sms[" << q * MS_ + so.slot << "]; t.x += x.x; t.y += x.y; }";
-      o << " kp.partial[((unsigned long long)b * kp.part_stride + " << so.out_off << "ull) * " << ntiles
-        << "ull + tile] = t; }\n";
-    }
-    o << "  __syncthreads();\n";
-  }
-
-  bool uses_c_ = false;
-
-  void pass(int pi) {
-    std::ostringstream& o = os_;
+  // ------------------------------------------------------------------ pass
+  // Emits one kernel; returns the constant-memory bytes its tables use.
+  size_t pass(std::ostringstream& out, int pi) {
     dp_ = &P_.passes[pi];
     L_ = dp_->L;
     NR_ = 1 << R_;
@@ -312,106 +319,160 @@ class Gen {
     NW_ = (NT_ + 31) / 32;
     MS_ = P_.max_slots > 0 ? P_.max_slots : 1;
     has_mu_ = bwd() || pacc();
+    sig_id_.clear();
+    sig_body_.clear();
     const bool store_psi = fwd() || bwd();
     const bool store_mu = has_mu_;
     const uint64_t N = 1ull << P_.n;
     const uint32_t TILE = 1u << L_;
-    // two CTAs per SM (<= 128 registers at 256 threads) so one CTA's tile
-    // load overlaps the other's arithmetic; the adjoint kernel keeps psi and
-    // mu live and gets the whole register file
-    o << "\nextern \"C\" __global__ void __launch_bounds__(" << NT_ << ", " << (bwd() ? 1 : 2) << ") tcgk_" << pi
-      << "(KParams kp) {\n";
-    o << "  using namespace tk;\n";
-    o << "  extern __shared__ __align__(16) float2 smem[];\n";
-    o << "  const u32 tid = threadIdx.x;\n  const int lane = (int)(tid & 31u);\n  const int warp = (int)(tid >> 5);\n";
-    o << "  (void)lane; (void)warp;\n";
-    o << "  const u32 tile = blockIdx.x;\n  const long long b = (long long)blockIdx.y;\n";
-    o << "  u32 base = 0u;\n";
-    for (int i = 0; i < dp_->nnonlocal; ++i) o << "  base |= ((tile >> " << i << ") & 1u) << " << dp_->nlbits[i] << ";\n";
-    o << "  float2* __restrict__ S = kp.psi + (unsigned long long)b * " << N << "ull + base;\n";
-    if (has_mu_) o << "  float2* __restrict__ U = kp.mu + (unsigned long long)b * " << N << "ull + base;\n";
-    if (fwd() || bwd()) o << "  const float2* __restrict__ Mt = kp.mats + b * kp.mat_stride;\n";
-    o << "  float2* const smp = smem;\n";
-    if (has_mu_) o << "  float2* const smu = smem + " << TILE << ";\n";
-    o << "  float2* const sms = smem + " << (has_mu_ ? 2 : 1) * TILE << ";\n  (void)sms;\n";
-    o << "  float2 v[" << NR_ << "];\n";
-    if (has_mu_) o << "  float2 w[" << NR_ << "];\n";
-    o << "  u32 jt = 0u, gt = 0u, sjt = 0u;\n  (void)jt; (void)sjt;\n";
+    const uint64_t ntiles = 1ull << (P_.n - L_);
+
+    std::vector<OpRec> recs;
+    std::vector<int> so;  // slot, out pairs
+    std::ostringstream cases;  // stage-entry code, one case per stage
     bool live = false, in_smem = false;
-    for (int s = dp_->stage_begin; s < dp_->stage_end; ++s) {
-      const DevStage& S = P_.stages[s];
-      o << "  // stage " << s << "\n";
+    Layout cur;
+    const int NS = dp_->stage_end - dp_->stage_begin;
+    for (int si = 0; si < NS; ++si) {
+      const DevStage& S = P_.stages[dp_->stage_begin + si];
+      const int ob = (int)recs.size();
+      bool usesC = false;
+      std::ostringstream c;
       if (S.smem_stage) {
         if (live) {
-          regs_to_smem(cur_, true, has_mu_);
+          regs_to_smem(c, cur, true, has_mu_);
           live = false;
         } else if (!in_smem) {
-          staged_load(true, has_mu_);
+          staged_load(c, true, has_mu_);
         }
         in_smem = true;
-        o << "  __syncthreads();\n";
+        c << "      __syncthreads();\n";
         for (int oi = S.op_begin; oi < S.op_end; ++oi) {
           const DevOp& op = P_.ops[oi];
-          o << "  { const int tb[6] = {" << op.p[0] << ", " << op.p[1] << ", " << op.p[2] << ", " << op.p[3] << ", "
-            << op.p[4] << ", " << op.p[5] << "};\n";
+          c << "      { const int tb[6] = {" << op.p[0] << ", " << op.p[1] << ", " << op.p[2] << ", " << op.p[3]
+            << ", " << op.p[4] << ", " << op.p[5] << "};\n";
           if (fwd() || bwd())
-            o << "    denseK_smem<" << op.k << ">(smp, " << L_ << ", tb, Mt + " << op.mat_off << "ll, "
+            c << "        denseK_smem<" << op.k << ">(smp, " << L_ << ", tb, Mt + " << op.mat_off << "ll, "
               << (bwd() ? "true" : "false") << ", tid, " << NT_ << ");\n";
           if (bwd())
-            o << "    denseK_smem<" << op.k << ">(smu, " << L_ << ", tb, Mt + " << op.mat_off << "ll, true, tid, "
-              << NT_ << ");\n";
-          o << "  }\n  __syncthreads();\n";
+            c << "        denseK_smem<" << op.k << ">(smu, " << L_ << ", tb, Mt + " << op.mat_off
+              << "ll, true, tid, " << NT_ << ");\n";
+          c << "      }\n      __syncthreads();\n";
         }
-        continue;
-      }
-      const Layout nl = layout_of(S);
-      if (!live) {
-        cur_ = nl;
-        layout_code(cur_);
-        if (in_smem) {
-          regs_from_smem(cur_, has_mu_);
-          o << "  __syncthreads();\n";
-        } else if (cur_.lanes_low) {
-          regs_from_global(cur_, has_mu_);
-        } else {
-          staged_load(true, has_mu_);
-          o << "  __syncthreads();\n";
-          regs_from_smem(cur_, has_mu_);
-          o << "  __syncthreads();\n";
+      } else {
+        const Layout nl = layout_of(S);
+        if (!live) {
+          cur = nl;
+          layout_code(c, cur);
+          if (in_smem) {
+            regs_from_smem(c, cur, has_mu_);
+            c << "      __syncthreads();\n";
+          } else if (cur.lanes_low) {
+            regs_from_global(c, cur, has_mu_);
+          } else {
+            staged_load(c, true, has_mu_);
+            c << "      __syncthreads();\n";
+            regs_from_smem(c, cur, has_mu_);
+            c << "      __syncthreads();\n";
+          }
+          live = true;
+          in_smem = false;
+        } else if (!same_layout(cur, nl)) {
+          regs_to_smem(c, cur, true, has_mu_);
+          c << "      __syncthreads();\n";
+          cur = nl;
+          layout_code(c, cur);
+          regs_from_smem(c, cur, has_mu_);
+          c << "      __syncthreads();\n";
         }
-        live = true;
-        in_smem = false;
-      } else if (!same_layout(cur_, nl)) {
-        regs_to_smem(cur_, true, has_mu_);
-        o << "  __syncthreads();\n";
-        cur_ = nl;
-        layout_code(cur_);
-        regs_from_smem(cur_, has_mu_);
-        o << "  __syncthreads();\n";
+        for (int oi = S.op_begin; oi < S.op_end; ++oi) {
+          OpRec r;
+          op_sig(P_.ops[oi], cur, &r, &usesC);
+          recs.push_back(r);
+        }
       }
-      o << "  {\n  const u32 gthr = base | gt; (void)gthr;\n  float2 C = cone(); (void)C;\n";
-      uses_c_ = false;
-      for (int oi = S.op_begin; oi < S.op_end; ++oi) op_code(P_.ops[oi]);
-      if (uses_c_) {
-        o << "#pragma unroll\n  for (int r = 0; r < " << NR_ << "; ++r) v[r] = cmul(C, v[r]);\n";
+      const int oe = (int)recs.size();
+      const int sob = (int)so.size() / 2;
+      if (bwd() || meas()) {
+        for (int e = S.slot_out_begin; e < S.slot_out_end; ++e) {
+          so.push_back(P_.slot_out[e].slot);
+          so.push_back((int)P_.slot_out[e].out_off);
+        }
       }
-      o << "  }\n";
-      if ((bwd() || meas()) && S.nslots > 0) flush_slots(S);
+      const int soe = (int)so.size() / 2;
+      cases << "    case " << si << ": {\n" << c.str() << "      ob = " << ob << "; oe = " << oe << "; sob = " << sob
+            << "; soe = " << soe << "; useC = " << (usesC ? "true" : "false") << ";\n    } break;\n";
     }
+
+    // constant tables
+    out << "\n__constant__ OpRec OPS_" << pi << "[" << std::max<size_t>(recs.size(), 1) << "] = {";
+    if (recs.empty()) out << "{0, 0, -1, 0, 0, 0u, 0, 0, 0}";
+    for (size_t i = 0; i < recs.size(); ++i) {
+      const OpRec& r = recs[i];
+      out << (i ? ", " : "") << "{" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
+          << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", 0}";
+    }
+    out << "};\n";
+    out << "__constant__ int SO_" << pi << "[" << std::max<size_t>(so.size(), 2) << "] = {";
+    if (so.empty()) out << "0, 0";
+    for (size_t i = 0; i < so.size(); ++i) out << (i ? ", " : "") << so[i];
+    out << "};\n";
+
+    // kernel
+    out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", " << (bwd() ? 1 : 2) << ") tcgk_" << pi
+        << "(KParams kp) {\n";
+    out << "  using namespace tk;\n  extern __shared__ __align__(16) float2 smem[];\n";
+    out << "  const u32 tid = threadIdx.x;\n  const int lane = (int)(tid & 31u);\n  const int warp = (int)(tid >> 5);\n";
+    out << "  (void)lane; (void)warp;\n  const u32 tile = blockIdx.x;\n  const long long b = (long long)blockIdx.y;\n";
+    out << "  u32 base = 0u;\n";
+    for (int i = 0; i < dp_->nnonlocal; ++i)
+      out << "  base |= ((tile >> " << i << ") & 1u) << " << dp_->nlbits[i] << ";\n";
+    out << "  float2* __restrict__ S = kp.psi + (unsigned long long)b * " << N << "ull + base;\n";
+    if (has_mu_) out << "  float2* __restrict__ U = kp.mu + (unsigned long long)b * " << N << "ull + base;\n";
+    if (fwd() || bwd()) out << "  const float2* __restrict__ Mt = kp.mats + b * kp.mat_stride;\n";
+    out << "  float2* const smp = smem;\n";
+    if (has_mu_) out << "  float2* const smu = smem + " << TILE << ";\n";
+    out << "  float2* const sms = smem + " << (has_mu_ ? 2 : 1) * TILE << ";\n  (void)sms;\n";
+    out << "  float2 v[" << NR_ << "];\n";
+    if (has_mu_) out << "  float2 w[" << NR_ << "];\n";
+    out << "  u32 jt = 0u, gt = 0u, sjt = 0u;\n  (void)jt; (void)sjt;\n";
+    out << "#pragma unroll 1\n  for (int s = 0; s < " << NS << "; ++s) {\n";
+    out << "    int ob = 0, oe = 0, sob = 0, soe = 0; bool useC = false;\n";
+    out << "    switch (s) {\n" << cases.str() << "    default: break;\n    }\n";
+    out << "    const u32 gthr = base | gt; (void)gthr;\n    float2 C = cone(); (void)C;\n";
+    out << "#pragma unroll 1\n    for (int o = ob; o < oe; ++o) {\n      const OpRec op = OPS_" << pi << "[o];\n";
+    out << "      switch (op.sig) {\n";
+    for (size_t i = 0; i < sig_body_.size(); ++i)
+      out << "        case " << i << ": { " << sig_body_[i] << " } break;\n";
+    out << "        default: break;\n      }\n    }\n";
+    out << "    if (useC) {\n#pragma unroll\n      for (int r = 0; r < " << NR_ << "; ++r) v[r] = cmul(C, v[r]);\n    }\n";
+    if (bwd() || meas()) {
+      out << "    if (soe > sob) {\n      __syncthreads();\n";
+      out << "      for (int e = sob + (int)tid; e < soe; e += " << NT_ << ") {\n";
+      out << "        const int slot = SO_" << pi << "[2 * e], outo = SO_" << pi << "[2 * e + 1];\n";
+      out << "        float2 t = czero();\n";
+      out << "        for (int q = 0; q < " << NW_ << "; ++q) { const float2 x = sms[q * " << MS_
+          << " + slot]; t.x += x.x; t.y += x.y; }\n";
+      out << "        kp.partial[((unsigned long long)b * kp.part_stride + (unsigned long long)outo) * " << ntiles
+          << "ull + tile] = t;\n      }\n      __syncthreads();\n    }\n";
+    }
+    out << "  }\n";
     if (store_psi || store_mu) {
       if (live) {
-        if (cur_.lanes_low) {
-          regs_to_global(cur_, store_psi, store_mu);
+        if (cur.lanes_low) {
+          regs_to_global(out, cur, store_psi, store_mu);
         } else {
-          regs_to_smem(cur_, store_psi, store_mu);
-          o << "  __syncthreads();\n";
-          staged_store(store_psi, store_mu);
+          std::ostringstream tmp;
+          regs_to_smem(tmp, cur, store_psi, store_mu);
+          out << tmp.str() << "  __syncthreads();\n";
+          staged_store(out, store_psi, store_mu);
         }
       } else if (in_smem) {
-        staged_store(store_psi, store_mu);
+        staged_store(out, store_psi, store_mu);
       }
     }
-    o << "}\n";
+    out << "}\n";
+    return recs.size() * sizeof(OpRec) + so.size() * sizeof(int);
   }
 };
 
@@ -501,7 +562,9 @@ int jit_policy() {
 
 std::string jit_source(const Program& P, int mode, int R) {
   Gen g(P, mode, R);
-  return g.source();
+  std::string s;
+  g.source(&s);
+  return s;
 }
 
 bool jit_build(const Program& P, int mode, int R, JitKernels* out) {
@@ -511,7 +574,15 @@ bool jit_build(const Program& P, int mode, int R, JitKernels* out) {
     out->log = "NVRTC not found";
     return false;
   }
-  const std::string body = jit_source(P, mode, R);
+  std::string body;
+  {
+    Gen g(P, mode, R);
+    if (!g.source(&body)) {
+      out->failed = true;
+      out->log = "op tables exceed the constant bank";
+      return false;
+    }
+  }
   const std::string src = std::string(kJitDevice) + "\n" + body;
   const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo", "--ptxas-options=-v"};
   const int nopt = 4;

@@ -307,6 +307,31 @@ __device__ __forceinline__ void pacc(const float2 (&v)[NR], float2 (&w)[NR], flo
   }
 }
 
+// the same with the register sign mask zr known only at run time
+template <int NR, int X>
+__device__ __forceinline__ float2 expectz(const float2 (&v)[NR], int zr) {
+  float2 acc = czero();
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const float2 t = v[r ^ X];
+    const float cx = fmaf(v[r].x, t.x, v[r].y * t.y);
+    const float cy = fmaf(v[r].x, t.y, -v[r].y * t.x);
+    const bool neg = __popc(r & zr) & 1;
+    acc.x += neg ? -cx : cx;
+    acc.y += neg ? -cy : cy;
+  }
+  return acc;
+}
+
+template <int NR, int X>
+__device__ __forceinline__ void paccz(const float2 (&v)[NR], float2 (&w)[NR], float2 cf, int zr) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const float2 c = (__popc(r & zr) & 1) ? cneg(cf) : cf;
+    w[r] = cfma(c, v[r ^ X], w[r]);
+  }
+}
+
 // (-i)^nY
 __device__ __forceinline__ float2 ypow(int nY) {
   return (nY & 3) == 0 ? make_float2(1.f, 0.f)
