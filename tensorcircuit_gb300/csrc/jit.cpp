@@ -35,6 +35,12 @@ const char kJitDevice[] =
 
 inline uint32_t host_swz(uint32_t j) { return j ^ (((j >> 5) ^ (j >> 10)) & 31u); }
 
+// tcgkF_<pass> forward, tcgkB_ adjoint, tcgkM_ measure, tcgkP_ Pauli accumulate
+std::string kernel_name(int mode, int pass) {
+  const char m = mode == MODE_FWD ? 'F' : mode == MODE_BWD ? 'B' : mode == MODE_MEAS ? 'M' : 'P';
+  return std::string("tcgk") + m + "_" + std::to_string(pass);
+}
+
 struct Layout {
   int R = 0, nthr = 0;
   int reg_tile[6] = {0};
@@ -419,7 +425,8 @@ class Gen {
     out << "};\n";
 
     // kernel
-    out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", " << (bwd() ? 1 : 2) << ") tcgk_" << pi
+    out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", " << (bwd() ? 1 : 2) << ") "
+        << kernel_name(mode_, pi)
         << "(KParams kp) {\n";
     out << "  using namespace tk;\n  extern __shared__ __align__(16) float2 smem[];\n";
     out << "  const u32 tid = threadIdx.x;\n  const int lane = (int)(tid & 31u);\n  const int warp = (int)(tid >> 5);\n";
@@ -636,7 +643,7 @@ bool jit_build(const Program& P, int mode, int R, JitKernels* out) {
   const bool has_mu = (mode == MODE_BWD || mode == MODE_PACC);
   for (size_t p = 0; p < P.passes.size(); ++p) {
     cudaKernel_t k;
-    const std::string nm = "tcgk_" + std::to_string(p);
+    const std::string nm = kernel_name(mode, int(p));
     if (cudaLibraryGetKernel(&k, out->lib, nm.c_str()) != cudaSuccess) {
       cudaGetLastError();
       out->failed = true;
