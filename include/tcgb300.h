@@ -44,7 +44,8 @@ enum {
   TCG_ERR_UNSUPPORTED = 3,   /* valid request this engine does not implement */
   TCG_ERR_CUDA = 4,          /* a CUDA runtime call failed */
   TCG_ERR_SCRATCH = 5,       /* caller-provided scratch is too small */
-  TCG_ERR_OOM = 6            /* a host or device allocation failed */
+  TCG_ERR_OOM = 6,           /* a host or device allocation failed */
+  TCG_ERR_TOO_LARGE = 7      /* request exceeds a fixed internal capacity */
 };
 
 /* ---- gate program --------------------------------------------------------- */
@@ -145,6 +146,22 @@ size_t tcg_expect_scratch_bytes(const tcg_mplan* plan, int64_t batch);
 int tcg_expect_pauli(const tcg_mplan* plan, const void* psi, int64_t batch,
                      double* out, void* scratch, size_t scratch_bytes,
                      void* stream);
+
+/* Allocation-free Pauli expectations.  No counterpart in the reference: it
+ * exists for callers that cannot allocate device memory -- code running while
+ * a stream is captured into a CUDA graph (cudaMalloc is refused there), hosts
+ * whose device memory lives in a pool this ABI cannot reach, and loops that
+ * cannot afford cudaMalloc's implicit synchronisation.  Same result as
+ * tcg_expect_pauli (out[b][t] = <psi_b|P_t|psi_b>, complex128) without a plan
+ * and without any allocation: the partial sums go to a fixed 8 MiB device
+ * array inside the library.  Limits: nterms <= 64, batch <= 65535 and
+ * batch * nterms <= 6898; larger requests return TCG_ERR_TOO_LARGE.  The
+ * first call on each device looks up the array's device address (make it
+ * before any stream capture).  All calls share the array: calls that overlap
+ * on the GPU (different streams, no ordering between them) race. */
+int tcg_expect_pauli_noalloc(const void* psi, int32_t nqubits, int64_t batch,
+                             const tcg_pauli* terms, int32_t nterms, double* out,
+                             void* stream);
 
 /* Cotangent seed for Pauli observables: mu[b] += sum_t coef[b][t] P_t psi[b]
  * (coef real fp32, coef_stride floats per circuit).  With coef = 2 Re(g_t)

@@ -19,6 +19,7 @@ TCG_ERR_UNSUPPORTED = 3
 TCG_ERR_CUDA = 4
 TCG_ERR_SCRATCH = 5
 TCG_ERR_OOM = 6
+TCG_ERR_TOO_LARGE = 7
 
 TCG_GATE_DENSE = 0
 TCG_GATE_DIAG = 1
@@ -75,6 +76,7 @@ SIGNATURES = [
     ("tcg_expect_scratch_bytes", _SZ, [_P, _I64]),
     ("tcg_expect_pauli", ctypes.c_int, [_P, _P, _I64, _P, _P, _SZ, _P]),
     ("tcg_pauli_accumulate", ctypes.c_int, [_P, _P, _P, _I64, _P, _I64, _P]),
+    ("tcg_expect_pauli_noalloc", ctypes.c_int, [_P, _I32, _I64, ctypes.POINTER(TcgPauli), _I32, _P, _P]),
     ("tcg_sample_scratch_bytes", _SZ, [_I32, _I64]),
     ("tcg_sample", ctypes.c_int, [_P, _I32, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),
     ("tcg_probability", ctypes.c_int, [_P, _I64, _P, _P]),
@@ -180,7 +182,7 @@ def check(status: int, what: str = "") -> None:
         msg = "%s: %s" % (what, msg)
     if status == TCG_ERR_DUP_QUBIT:
         raise AssertionError(msg)
-    if status == TCG_ERR_INVALID_ARG:
+    if status in (TCG_ERR_INVALID_ARG, TCG_ERR_TOO_LARGE):
         raise ValueError(msg)
     if status == TCG_ERR_UNSUPPORTED:
         raise NotImplementedError(msg)

@@ -129,6 +129,9 @@ const char* tcg_status_string(int32_t s) {
     case TCG_ERR_CUDA: return "CUDA runtime error";
     case TCG_ERR_SCRATCH: return "scratch buffer too small";
     case TCG_ERR_OOM: return "allocation failed";
+    case TCG_ERR_TOO_LARGE:
+      return "request exceeds a fixed internal capacity (tcg_expect_pauli_noalloc: nterms <= 64, "
+             "batch <= 65535, batch * nterms <= 6898)";
     default: return "unknown status";
   }
 }

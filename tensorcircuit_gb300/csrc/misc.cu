@@ -37,7 +37,7 @@ __global__ void reduce_partials_kernel(const float2* __restrict__ partial, int64
   const int lane = threadIdx.x & 31;
   const int64_t b = blockIdx.y;
   if (ei >= nentries) return;
-  const int64_t e = entries[ei];
+  const int64_t e = entries ? entries[ei] : ei;  // null: entries 0 .. nentries-1
   const float2* p = partial + (size_t(b) * part_stride + e) * ntiles;
   double sx = 0.0, sy = 0.0;
   for (uint32_t t = lane; t < ntiles; t += 32) {
