@@ -225,7 +225,10 @@ def run_gb300_arm(args, rank, world):
     blocks = []
     for gkey, idx, E in entry.groups:
         th = params[:, [layout[i][2] for i in idx]]
-        blocks.append(G.FAMILIES[gkey[1]].build(th).reshape(BATCH, -1))
+        if gkey[0] == "prot":
+            blocks.append(G.build_prot(th, gkey[1]).reshape(BATCH, -1))
+        else:
+            blocks.append(G.FAMILIES[gkey[1]].build(th).reshape(BATCH, -1))
     mats = torch.cat(blocks, -1).to(torch.complex64).contiguous()
     M = mats.shape[-1]
     psi_out = torch.zeros(BATCH, N, dtype=torch.complex64, device=dev)
@@ -316,12 +319,160 @@ def run_gb300_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+BW_N, BW_DEPTH, BW_SEED, BW_USEED, BW_SHOTS = 28, 20, 3, 4, 1 << 20
+BW_METRIC = "gate-updates/s (n=28 Haar brick wall, depth 20; state, <Z0Z27>, <X13>, 2^20 samples)"
+BW_UNIT = "gate-updates/s"
+BW_WORKLOAD = "brickwall_n28_d20_haar"
+
+
+def _bw_inputs():
+    from tensorcircuit_gb300 import templates
+
+    gl = templates.brickwall_gate_list(BW_N, BW_DEPTH, BW_SEED)
+    u = np.random.default_rng(BW_USEED).random(BW_SHOTS, dtype=np.float32)
+    return gl, u
+
+
+def cpu_brickwall(n_cpu=22):
+    """Reference-algorithm restatement (per-gate tensordot, complex64) on the
+    host cores: the n=28 circuit holds 2 GiB states, so the bounded sample is
+    the same brick wall at ``n_cpu`` qubits, scaled to gate-updates/s of
+    n=28 by the amplitude count."""
+    from oracle import reference_algo as ra
+    from tensorcircuit_gb300 import templates
+
+    threads = len(os.sched_getaffinity(0))
+    gl = templates.brickwall_gate_list(n_cpu, BW_DEPTH, BW_SEED)
+    ra.run_gate_list(n_cpu, gl[:4], threads)
+    t0 = time.perf_counter()
+    ra.run_gate_list(n_cpu, gl, threads)
+    dt = time.perf_counter() - t0
+    scale = float(1 << (BW_N - n_cpu))
+    return {"value": len(gl) / dt / scale, "unit": BW_UNIT, "cores": threads, "kind": "port",
+            "sample": "brick wall depth %d at n=%d (%d gates, %.2f s; labelled torch restatement of the "
+                      "reference's per-gate tensordot), scaled by 2^%d amplitudes to n=%d" %
+                      (BW_DEPTH, n_cpu, len(gl), dt, BW_N - n_cpu, BW_N)}
+
+
+def run_brickwall(args, rank, world):
+    """Large single circuit: n=28 Haar brick wall (270 gates), then <Z0 Z27>,
+    <X13> and 2^20 samples from seeded uniforms, through the Circuit API."""
+    import torch
+
+    import tensorcircuit_gb300 as tc
+    from tensorcircuit_gb300 import _native, templates
+    from tensorcircuit_gb300 import circuit as cmod
+
+    tc.build()
+    lib = _native.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n = BW_N
+    gl, u_np = _bw_inputs()
+    u_host = torch.from_numpy(u_np).pin_memory()
+    u_dev = u_host.to(dev)
+
+    def step(u):
+        c = templates.apply_gate_list(tc.Circuit(n), gl)
+        zz = c.expectation_ps(z=[0, n - 1])
+        x13 = c.expectation_ps(x=[13])
+        s = c.sample(batch=BW_SHOTS, allow_state=True, status=u, format="sample_int")
+        return zz, x13, s
+
+    warmup = max(args.warmup, 3)
+    for _ in range(warmup):
+        out = step(u_dev)
+    torch.cuda.synchronize()
+    l0 = lib.tcg_launch_count()
+    step(u_dev)
+    torch.cuda.synchronize()
+    launches_per_step = lib.tcg_launch_count() - l0
+
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            out = step(u_dev)
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+
+    # end to end: uniforms from pinned host memory in, expectations and
+    # samples back to pinned host memory, every step
+    sh = torch.empty((BW_SHOTS,), dtype=torch.int64).pin_memory()
+    eh = torch.empty((2,), dtype=torch.complex64).pin_memory()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        u = u_host.to(dev, non_blocking=True)
+        zz, x13, s = step(u)
+        eh.copy_(torch.stack([zz.reshape(()), x13.reshape(())]), non_blocking=True)
+        sh.copy_(s, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+
+    # dominant kernel: the forward sweep of the cached plan, per pass
+    c = templates.apply_gate_list(tc.Circuit(n), gl)
+    entry = cmod._entries[cmod._struct_key(n, c._ops)]
+    plan = entry.plan
+    mats = entry.const_block(dev)
+    N = 1 << n
+    psi = torch.zeros(N, dtype=torch.complex64, device=dev)
+    st = int(torch.cuda.current_stream().cuda_stream)
+    reps = max(3, args.steps)
+    tot = 0.0
+    for r in range(reps + 1):
+        psi.zero_()
+        psi[0] = 1
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record()
+        _native.check(lib.tcg_forward(plan.handle, psi.data_ptr(), 1, mats.data_ptr(), mats.numel(), st))
+        f1.record()
+        torch.cuda.synchronize()
+        if r:
+            tot += f0.elapsed_time(f1)
+    ms_fwd = tot / reps
+    per_launch_s = ms_fwd / 1e3 / plan.npasses
+    achieved = 16.0 * N / per_launch_s / 1e9
+    peak, peak_kind = _peaks()
+    if rank != 0:
+        return
+    cpu = None if args.no_cpu else cpu_brickwall()
+    zz, x13, _ = out
+    line = {
+        "metric": BW_METRIC, "value": len(gl) / (ms / 1e3), "unit": BW_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": BW_WORKLOAD, "n_qubits": n, "depth": BW_DEPTH, "gates": len(gl),
+                   "shots": BW_SHOTS, "seed": BW_SEED, "uniform_seed": BW_USEED,
+                   "l2": "no flush: the 2 GiB state exceeds the 129 MB L2",
+                   "fwd_passes": plan.npasses, "zz_0_27": float(zz.real), "x_13": float(x13.real)},
+        "roofline": {"bound": "hbm", "kernel": "forward pass (tcg_forward, one launch per pass)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "alg_bytes_per_launch": 16.0 * N,
+                     "ms_forward": ms_fwd, "passes": plan.npasses,
+                     "amp_updates_per_s": len(gl) * N / (ms_fwd / 1e3),
+                     "gate_updates_per_s_forward": len(gl) / (ms_fwd / 1e3)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": len(gl) / (ms_e2e / 1e3), "unit": BW_UNIT, "h2d_bytes_per_step": BW_SHOTS * 4,
+                "d2h_bytes_per_step": BW_SHOTS * 8 + 16},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches_per_step * args.steps),
+        "gpu_launches_per_step": int(launches_per_step),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="hea", choices=["hea", "brickwall"],
+                    help="hea: n=20 HEA batched vvag (default); brickwall: n=28 Haar brick wall")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -335,7 +486,10 @@ def main():
         local = int(os.environ.get("LOCAL_RANK", "0"))
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
-    run_gb300_arm(args, rank, world)
+    if args.workload == "brickwall":
+        run_brickwall(args, rank, world)
+    else:
+        run_gb300_arm(args, rank, world)
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -50,21 +50,27 @@ enum {
 
 /* ---- gate program --------------------------------------------------------- */
 enum {
-  TCG_GATE_DENSE = 0, /* 2^nq x 2^nq matrix, row-major M[out, in]          */
-  TCG_GATE_DIAG = 1   /* diagonal gate: 2^nq entries d[idx]                  */
+  TCG_GATE_DENSE = 0,     /* 2^nq x 2^nq matrix, row-major M[out, in]        */
+  TCG_GATE_DIAG = 1,      /* diagonal gate: 2^nq entries d[idx]                */
+  TCG_GATE_PAULI_ROT = 2  /* cos(phi) I - i sin(phi) P for a Pauli string P  */
 };
 
 #define TCG_MAX_GATE_QUBITS 6
 
 typedef struct tcg_gate {
-  int32_t kind;                         /* TCG_GATE_DENSE or TCG_GATE_DIAG   */
+  int32_t kind;                         /* TCG_GATE_*                        */
   int32_t nq;                           /* 1 .. TCG_MAX_GATE_QUBITS          */
   int32_t qubits[TCG_MAX_GATE_QUBITS];  /* qubit indices, first = sub-index MSB */
+  int32_t pauli[TCG_MAX_GATE_QUBITS];   /* PAULI_ROT: 1=X 2=Y 3=Z per qubit  */
   int64_t mat_off;   /* complex64 offset of this gate's entries in the
-                        per-circuit matrix buffer (4^nq dense, 2^nq diag)  */
+                        per-circuit matrix buffer: 4^nq (dense), 2^nq
+                        (diagonal), or 1 = cos(phi) + i sin(phi) (Pauli
+                        rotation; rx(theta) is phi = theta/2, P = X)      */
   int64_t grad_off;  /* complex64 offset of this gate's cotangent in the
-                        per-circuit gradient buffer (same entry count as the
-                        matrix), or -1 when no gradient is wanted           */
+                        per-circuit gradient buffer, or -1 when no gradient
+                        is wanted.  Dense/diagonal: one entry per matrix
+                        entry (torch convention dL/dRe + i dL/dIm).  Pauli
+                        rotation: one entry, (dL/dphi, 0).                */
 } tcg_gate;
 
 typedef struct tcg_plan tcg_plan; /* opaque, host side; owns a small device

@@ -79,3 +79,19 @@ def vvag_hea(n: int, layout: Sequence[Tuple[str, Tuple[int, ...], int]],
     vg = torch.func.vmap(torch.func.grad_and_value(f))
     g, v = vg(torch.as_tensor(params, dtype=torch.float32))
     return v.numpy(), g.numpy()
+
+
+def run_gate_list(n: int, gl: Sequence[Tuple[str, Tuple[int, ...], Dict[str, Any]]], threads: int) -> torch.Tensor:
+    """Forward-only: constant-matrix gates (``any``/unitary, e.g. the Haar
+    brick wall) contracted one ``tensordot`` per gate in circuit order, the
+    reference's per-gate contraction on a complex64 state."""
+    torch.set_num_threads(threads)
+    psi = torch.zeros([2] * n, dtype=C64)
+    psi.view(-1)[0] = 1.0
+    for name, q, p in gl:
+        if name not in ("any", "unitary"):
+            raise NotImplementedError(name)
+        k = len(q)
+        g = torch.as_tensor(np.asarray(p["unitary"], dtype=np.complex64)).reshape([2] * (2 * k))
+        psi = _apply(psi, g, q)
+    return psi.reshape(-1)

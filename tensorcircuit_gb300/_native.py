@@ -23,6 +23,7 @@ TCG_ERR_TOO_LARGE = 7
 
 TCG_GATE_DENSE = 0
 TCG_GATE_DIAG = 1
+TCG_GATE_PAULI_ROT = 2
 MAX_GATE_QUBITS = 6
 MIN_QUBITS = 6
 
@@ -32,6 +33,7 @@ class TcgGate(ctypes.Structure):
         ("kind", ctypes.c_int32),
         ("nq", ctypes.c_int32),
         ("qubits", ctypes.c_int32 * MAX_GATE_QUBITS),
+        ("pauli", ctypes.c_int32 * MAX_GATE_QUBITS),
         ("mat_off", ctypes.c_int64),
         ("grad_off", ctypes.c_int64),
     ]

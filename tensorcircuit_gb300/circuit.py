@@ -32,6 +32,12 @@ _PAULI_1Q = {
 }
 
 
+def _is_complex(v: Any) -> bool:
+    if isinstance(v, torch.Tensor):
+        return v.is_complex()
+    return bool(np.iscomplexobj(v))
+
+
 def _is_seq(x: Any) -> bool:
     return isinstance(x, (list, tuple, range)) or (isinstance(x, np.ndarray) and x.ndim > 0)
 
@@ -118,6 +124,8 @@ _entries: Dict[Any, _PlanEntry] = {}
 
 
 def _group_key(op: _Op) -> Any:
+    if op.kind == "prot":
+        return ("prot", op.data[1])
     if op.kind == "fam":
         return ("fam", op.name)
     if op.kind == "any":
@@ -134,6 +142,8 @@ def _struct_key(n: int, ops: Sequence[_Op]) -> Any:
     for op in ops:
         if op.kind == "const":
             parts.append(("c", op.name, op.qubits))
+        elif op.kind == "prot":
+            parts.append((_group_key(op), op.qubits, op.data[2]))
         else:
             parts.append((_group_key(op), op.qubits))
     return (n, tuple(parts))
@@ -163,22 +173,34 @@ def _build_entry(n_eng: int, ops: Sequence[_Op]) -> _PlanEntry:
     mat_off: Dict[int, int] = dict(const_off)
     grad_off: Dict[int, int] = {}
     glist = []
+    prot_offs: List[int] = []
     for k in order:
         idx = groups[k]
-        E = (1 << ops[idx[0]].nq) if ops[idx[0]].diag else (1 << (2 * ops[idx[0]].nq))
+        op0 = ops[idx[0]]
+        if op0.kind == "prot":
+            E = 1
+        else:
+            E = (1 << op0.nq) if op0.diag else (1 << (2 * op0.nq))
         for j, i in enumerate(idx):
             mat_off[i] = off + j * E
-            if ops[i].nq <= 2:
+            if ops[i].nq <= 2 or ops[i].kind == "prot":
                 grad_off[i] = off + j * E
+            if ops[i].kind == "prot":
+                prot_offs.append(off + j * E)
         off += E * len(idx)
         glist.append((k, idx, E))
     gates_c = []
     for i, op in enumerate(ops):
-        kind = nat.TCG_GATE_DIAG if op.diag else nat.TCG_GATE_DENSE
-        gates_c.append((kind, op.qubits, mat_off[i], grad_off.get(i, -1)))
+        if op.kind == "prot":
+            gates_c.append((nat.TCG_GATE_PAULI_ROT, op.qubits, mat_off[i], grad_off.get(i, -1), op.data[2]))
+        else:
+            kind = nat.TCG_GATE_DIAG if op.diag else nat.TCG_GATE_DENSE
+            gates_c.append((kind, op.qubits, mat_off[i], grad_off.get(i, -1)))
     plan = eng.GatePlan(n_eng, gates_c, off)
     const_block = np.concatenate(const_mats) if const_mats else None
-    return _PlanEntry(plan, const_block, glist, off, gates_c)
+    entry = _PlanEntry(plan, const_block, glist, off, gates_c)
+    entry.prot_offs = np.asarray(prot_offs, dtype=np.int64)
+    return entry
 
 
 def _stack_scalars(vals: Sequence[Any], dev: torch.device) -> torch.Tensor:
@@ -220,6 +242,8 @@ def _stack_mats(vals: Sequence[Any], d: int, dev: torch.device) -> torch.Tensor:
 
 def _group_block(key: Any, ops: Sequence[_Op], idx: Sequence[int], dev: torch.device) -> torch.Tensor:
     kind = key[0]
+    if kind == "prot":
+        return gates.build_prot(_stack_scalars([ops[i].data[0] for i in idx], dev), key[1])
     if kind == "fam":
         fam = gates.FAMILIES[key[1]]
         args = []
@@ -323,7 +347,11 @@ class Circuit:
             if len(idx) != fam.nq:
                 raise ValueError("gate %s acts on %d qubits, got %d indices" % (name, fam.nq, len(idx)))
             data = tuple(vars.get(p, d) for p, d in fam.params)
-            self._record(_Op("fam", name, idx, data, fam.diag, fam.nq), ir)
+            if fam.pauli is not None and not _is_complex(data[0]):
+                codes = tuple(gates.PAULI_CODE[c] for c in fam.pauli)
+                self._record(_Op("prot", name, idx, (data[0], fam.scale, codes), False, fam.nq), ir)
+            else:
+                self._record(_Op("fam", name, idx, data, fam.diag, fam.nq), ir)
             return
         if name == "any":
             u = vars.get("unitary")
@@ -342,6 +370,15 @@ class Circuit:
             if un is not None and un.shape[0] != d:
                 raise ValueError("unitary size does not match %d qubits" % len(idx))
             if name == "exp1":
+                codes = _pauli_decompose(un) if un is not None else None
+                if codes is not None and any(c != 0 for c in codes) and \
+                        sum(c in (1, 2) for c in codes) <= 4 and not _is_complex(theta):
+                    # exp1 of a Pauli string: the engine's Pauli-rotation kind
+                    # (identity factors dropped)
+                    pq = tuple(q for q, c in zip(idx, codes) if c != 0)
+                    pc = tuple(c for c in codes if c != 0)
+                    self._record(_Op("prot", name, pq, (theta, 0.5 if half else 1.0, pc), False, len(pq)), ir)
+                    return
                 diag = un is not None and gates.is_diagonal(un)
                 self._record(_Op("exp1", name, idx, (theta, u if un is None else un, half), diag, len(idx)), ir)
             else:

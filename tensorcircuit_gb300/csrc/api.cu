@@ -18,7 +18,17 @@ constexpr int kAbiVersion = 1;
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
 int check_gate(int n, const tcg_gate& g) {
-  if (g.kind != TCG_GATE_DENSE && g.kind != TCG_GATE_DIAG) return TCG_ERR_INVALID_ARG;
+  if (g.kind != TCG_GATE_DENSE && g.kind != TCG_GATE_DIAG && g.kind != TCG_GATE_PAULI_ROT)
+    return TCG_ERR_INVALID_ARG;
+  if (g.kind == TCG_GATE_PAULI_ROT) {
+    if (g.nq < 1 || g.nq > TCG_MAX_GATE_QUBITS) return TCG_ERR_INVALID_ARG;
+    int nx = 0;
+    for (int i = 0; i < g.nq; ++i) {
+      if (g.pauli[i] < 1 || g.pauli[i] > 3) return TCG_ERR_INVALID_ARG;
+      nx += g.pauli[i] != 3;
+    }
+    if (nx > kRBwd) return TCG_ERR_UNSUPPORTED;  // X/Y qubits must fit the registers
+  }
   if (g.nq < 1 || g.nq > TCG_MAX_GATE_QUBITS) return TCG_ERR_INVALID_ARG;
   if (g.mat_off < 0) return TCG_ERR_INVALID_ARG;
   for (int i = 0; i < g.nq; ++i) {
@@ -26,7 +36,7 @@ int check_gate(int n, const tcg_gate& g) {
     for (int j = 0; j < i; ++j)
       if (g.qubits[i] == g.qubits[j]) return TCG_ERR_DUP_QUBIT;
   }
-  if (g.grad_off >= 0 && g.nq > 2) return TCG_ERR_UNSUPPORTED;
+  if (g.grad_off >= 0 && g.nq > 2 && g.kind != TCG_GATE_PAULI_ROT) return TCG_ERR_UNSUPPORTED;
   return TCG_OK;
 }
 
@@ -155,9 +165,16 @@ int tcg_plan_create(int32_t nqubits, const tcg_gate* gates, int32_t ngates, cons
     for (int q = 0; q < g.k; ++q) g.gbits[q] = nqubits - 1 - gates[i].qubits[q];
     g.mat_off = gates[i].mat_off;
     g.grad_off = gates[i].grad_off;
+    if (g.kind == TCG_GATE_PAULI_ROT) {
+      for (int q = 0; q < g.k; ++q) {
+        const uint64_t bit = 1ull << g.gbits[q];
+        if (gates[i].pauli[q] != 3) g.xmask |= bit;  // X or Y
+        if (gates[i].pauli[q] != 1) g.zmask |= bit;  // Z or Y
+      }
+    }
     if (g.grad_off >= 0) {
       has_grad = true;
-      const int64_t E = (g.kind == TCG_GATE_DIAG) ? (1 << g.k) : (1 << (2 * g.k));
+      const int64_t E = (g.kind == TCG_GATE_PAULI_ROT) ? 1 : (g.kind == TCG_GATE_DIAG) ? (1 << g.k) : (1 << (2 * g.k));
       grad_entries = std::max(grad_entries, g.grad_off + E);
     }
     pg.push_back(g);

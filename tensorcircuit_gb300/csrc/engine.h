@@ -30,7 +30,9 @@ enum OpKind : int32_t {
   OP_DIAG = 2,     // k-qubit diagonal on global bits gb[0..k-1] (gb[0] = MSB)
   OP_DENSEK = 3,   // k-qubit dense on tile bits tb[0..k-1], run on the smem tile
   OP_EXPECT = 4,   // Pauli term: acc += conj(psi[a]) s(a) psi[a ^ x]
-  OP_PACC = 5      // Pauli term: mu[a] += c s(a) psi[a ^ x]
+  OP_PACC = 5,     // Pauli term: mu[a] += c s(a) psi[a ^ x]
+  OP_PROT = 6      // Pauli rotation cos(phi) I - i sin(phi) P (X/Y bits in
+                   // registers: xreg; Z/Y global mask: zmask; nY)
 };
 
 // One device op, 48 bytes.

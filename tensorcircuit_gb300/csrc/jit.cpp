@@ -293,6 +293,22 @@ class Gen {
           }
         }
       }
+    } else if (op.kind == OP_PROT) {
+      int zr = 0;
+      for (int i = 0; i < l.R; ++i)
+        if (gbit(l.reg_tile[i]) & op.zmask) zr |= 1 << i;
+      rec->zm = op.zmask;
+      rec->ny = op.nY;
+      rec->zr = zr;
+      b << "const float2 cs = ld(Mt + op.off); const u32 sg = __popc(gthr & op.zm) & 1u; ";
+      if (fwd()) {
+        b << "prot<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, cs.x, cs.y, sg, false);";
+      } else {
+        const bool G = op.slot >= 0;
+        b << "float g = 0.f; prot_bwd<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ", "
+          << (G ? "true" : "false") << ">(v, w, cs.x, cs.y, sg, g);";
+        if (G) b << " float2 a1[1] = {make_float2(g, 0.f)};" << reduce(1, "a1");
+      }
     } else if (op.kind == OP_EXPECT) {
       int zr = 0;
       for (int i = 0; i < l.R; ++i)

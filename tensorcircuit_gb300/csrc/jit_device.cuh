@@ -277,6 +277,10 @@ __device__ __forceinline__ void diag1_bwd(float2 (&v)[NR], float2 (&w)[NR], cons
 }
 
 // ----------------------------------------------------------------- Pauli terms
+// population count usable in constant expressions (NVRTC has no
+// __builtin_popcount)
+__host__ __device__ constexpr int tk_popc(unsigned x) { return x ? int(x & 1u) + tk_popc(x >> 1) : 0; }
+
 // sum_r conj(v[r]) (-1)^{popc(r & ZR)} v[r ^ X]  (the run-time sign of the
 // thread's fixed bits is applied by the caller)
 template <int NR, int X, int ZR>
@@ -287,7 +291,7 @@ __device__ __forceinline__ float2 expect(const float2 (&v)[NR]) {
     const float2 t = v[r ^ X];
     const float cx = fmaf(v[r].x, t.x, v[r].y * t.y);
     const float cy = fmaf(v[r].x, t.y, -v[r].y * t.x);
-    if (__builtin_popcount(r & ZR) & 1) {
+    if (tk_popc(r & ZR) & 1) {
       acc.x -= cx;
       acc.y -= cy;
     } else {
@@ -302,7 +306,7 @@ template <int NR, int X, int ZR>
 __device__ __forceinline__ void pacc(const float2 (&v)[NR], float2 (&w)[NR], float2 cf) {
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
-    const float2 c = (__builtin_popcount(r & ZR) & 1) ? cneg(cf) : cf;
+    const float2 c = (tk_popc(r & ZR) & 1) ? cneg(cf) : cf;
     w[r] = cfma(c, v[r ^ X], w[r]);
   }
 }
@@ -337,6 +341,68 @@ __device__ __forceinline__ float2 ypow(int nY) {
   return (nY & 3) == 0 ? make_float2(1.f, 0.f)
        : (nY & 3) == 1 ? make_float2(0.f, -1.f)
        : (nY & 3) == 2 ? make_float2(-1.f, 0.f) : make_float2(0.f, 1.f);
+}
+
+// ----------------------------------------------------------------- Pauli rotations
+// G = c I - i s P with (P psi)[a] = (-i)^NY (-1)^{popc(a & zmask)} psi[a ^ x].
+// X: register mask of the X/Y bits; ZR: register mask of the Z/Y bits (the
+// rest of the Z/Y mask is folded into the thread sign `sgn`).
+// G psi [r] = c psi[r] + (-1)^{popc(r & ZR)} q psi[r ^ X],  q = -i s (-i)^NY (-1)^sgn;
+// G^H uses -q.
+template <int NY>
+__device__ __forceinline__ float2 ypowc() {
+  return (NY & 3) == 0 ? make_float2(1.f, 0.f)
+       : (NY & 3) == 1 ? make_float2(0.f, -1.f)
+       : (NY & 3) == 2 ? make_float2(-1.f, 0.f) : make_float2(0.f, 1.f);
+}
+
+template <int NR, int X, int ZR, int NY>
+__device__ __forceinline__ void prot(float2 (&v)[NR], float c, float s, u32 sgn, bool adj) {
+  float2 q = cmul(make_float2(0.f, -s), ypowc<NY>());
+  if (adj ^ (sgn != 0u)) q = cneg(q);
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const bool neg = tk_popc(r & ZR) & 1;
+    const float2 qr = neg ? cneg(q) : q;
+    if (X == 0) {
+      v[r] = cmul(make_float2(c + qr.x, qr.y), v[r]);
+    } else {
+      const int r2 = r ^ X;
+      if (r2 < r) continue;
+      const bool neg2 = tk_popc(r2 & ZR) & 1;
+      const float2 q2 = neg2 ? cneg(q) : q;
+      const float2 a = v[r], bb = v[r2];
+      v[r] = cfma(qr, bb, make_float2(c * a.x, c * a.y));
+      v[r2] = cfma(q2, a, make_float2(c * bb.x, c * bb.y));
+    }
+  }
+}
+
+// Adjoint step: g = Im <mu|P|psi> over this thread's amplitudes (psi, mu
+// after the gate), then psi <- G^H psi, mu <- G^H mu.
+template <int NR, int X, int ZR, int NY, bool G>
+__device__ __forceinline__ void prot_bwd(float2 (&v)[NR], float2 (&w)[NR], float c, float s, u32 sgn, float& g) {
+  if (G) {
+    float2 z = czero();
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      const float2 t = v[r ^ X];
+      const float cx = fmaf(w[r].x, t.x, w[r].y * t.y);   // conj(w) * t
+      const float cy = fmaf(w[r].x, t.y, -w[r].y * t.x);
+      if (tk_popc(r & ZR) & 1) {
+        z.x -= cx;
+        z.y -= cy;
+      } else {
+        z.x += cx;
+        z.y += cy;
+      }
+    }
+    float2 pt = ypowc<NY>();
+    if (sgn) pt = cneg(pt);
+    g = fmaf(pt.x, z.y, pt.y * z.x);  // Im(pt * z)
+  }
+  prot<NR, X, ZR, NY>(v, c, s, sgn, true);
+  prot<NR, X, ZR, NY>(w, c, s, sgn, true);
 }
 
 // ----------------------------------------------------------------- reductions

@@ -155,6 +155,29 @@ int emit_stage(Program* P, DevPass& dp, const StageDraft& sd,
       so.out_off = o.term;
       P->slot_out.push_back(so);
       slot += 1;
+    } else if (o.kind == TCG_GATE_PAULI_ROT) {
+      d.kind = OP_PROT;
+      int xr = 0;
+      for (int b = 0; b < 64; ++b)
+        if (o.x >> b & 1) {
+          int rp = regpos_of_tile[tile_of_gbit[b]];
+          if (rp < 0) return TCG_ERR_INVALID_ARG;
+          xr |= 1 << rp;
+        }
+      d.xreg = xr;
+      d.zmask = (uint32_t)o.z;
+      d.nY = popc64(o.x & o.z);
+      for (int i = 0; i < o.k; ++i) d.p[i] = o.gbits[i];
+      if (o.grad_off >= 0) {
+        d.grad_off = o.grad_off;
+        d.slot = slot;
+        SlotOut so;
+        so.slot = slot;
+        so.pad = 0;
+        so.out_off = o.grad_off;
+        P->slot_out.push_back(so);
+        slot += 1;
+      }
     } else if (o.kind == TCG_GATE_DIAG) {
       d.kind = OP_DIAG;
       for (int i = 0; i < o.k; ++i) d.p[i] = o.gbits[i];
@@ -258,6 +281,25 @@ int emit_pass(Program* P, int n, int L, int R, uint64_t S,
       cur.slots += 1;
       continue;
     }
+    if (o.kind == TCG_GATE_PAULI_ROT) {
+      // X/Y bits must be register bits; Z bits may be anywhere
+      const int E1 = o.grad_off >= 0 ? 1 : 0;
+      uint32_t tb = 0;
+      for (int b = 0; b < n; ++b)
+        if (o.x >> b & 1) tb |= 1u << tile_of_gbit[b];
+      if (popc64(tb) > R) return TCG_ERR_UNSUPPORTED;
+      if (cur.smem) close();
+      const uint32_t need = tb & ~cur.rset;
+      if (popc64(cur.rset | need) <= R && cur.slots + E1 <= max_slots) {
+        cur.rset |= need;
+      } else {
+        close();
+        cur.rset = tb;
+      }
+      cur.ops.push_back((int)oi);
+      cur.slots += E1;
+      continue;
+    }
     int E = 0;
     if (o.grad_off >= 0) E = (o.kind == TCG_GATE_DIAG) ? (1 << o.k) : (1 << (2 * o.k));
     if (o.kind == TCG_GATE_DIAG) {
@@ -328,7 +370,7 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
   int64_t nout = 0;
   for (const PGate& g : gates)
     if (g.grad_off >= 0) {
-      int64_t E = (g.kind == TCG_GATE_DIAG) ? (1 << g.k) : (1 << (2 * g.k));
+      int64_t E = (g.kind == TCG_GATE_PAULI_ROT) ? 1 : (g.kind == TCG_GATE_DIAG) ? (1 << g.k) : (1 << (2 * g.k));
       nout = std::max(nout, g.grad_off + E);
     }
   P.nout = nout;
@@ -351,7 +393,8 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
         left.push_back(gi);
         continue;
       }
-      uint64_t need = (g.kind == TCG_GATE_DENSE) ? (bits & ~S) : 0;
+      uint64_t need = (g.kind == TCG_GATE_DENSE) ? (bits & ~S)
+                    : (g.kind == TCG_GATE_PAULI_ROT) ? (g.xmask & ~S) : 0;
       if (popc64(S | need) <= L) {
         S |= need;
         taken.push_back(gi);
@@ -379,6 +422,8 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
       for (int i = 0; i < 6; ++i) o.gbits[i] = (i < g.k) ? g.gbits[i] : 0;
       o.mat_off = g.mat_off;
       o.grad_off = g.grad_off;
+      o.x = g.xmask;
+      o.z = g.zmask;
       od.push_back(o);
     }
     int rc = emit_pass(&P, n, L, R, S, od, max_slots);

@@ -48,11 +48,12 @@ struct PlanOpts {
 
 // A planned gate (global-bit form).
 struct PGate {
-  int kind;            // TCG_GATE_DENSE / TCG_GATE_DIAG
+  int kind;            // TCG_GATE_DENSE / TCG_GATE_DIAG / TCG_GATE_PAULI_ROT
   int k;
   int gbits[TCG_MAX_GATE_QUBITS];  // global index bits, first = sub-index MSB
   int64_t mat_off;
   int64_t grad_off;
+  uint64_t xmask = 0, zmask = 0;   // PAULI_ROT: X/Y and Z/Y global masks
 };
 
 // Build a gate program for `gates` in execution order (`reverse` for the

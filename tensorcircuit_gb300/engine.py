@@ -52,14 +52,19 @@ def _stream() -> int:
 class GatePlan:
     """A native gate plan plus its matrix-buffer layout."""
 
-    def __init__(self, n: int, gates: Sequence[Tuple[int, Tuple[int, ...], int, int]], nmat: int) -> None:
+    def __init__(self, n: int, gates: Sequence[Tuple[Any, ...]], nmat: int) -> None:
+        """gates: (kind, qubits, mat_off, grad_off[, pauli codes]) tuples."""
         lib = nat.load()
         arr = (nat.TcgGate * max(len(gates), 1))()
-        for i, (kind, qubits, mat_off, grad_off) in enumerate(gates):
+        for i, g in enumerate(gates):
+            kind, qubits, mat_off, grad_off = g[:4]
             arr[i].kind = kind
             arr[i].nq = len(qubits)
             for j, q in enumerate(qubits):
                 arr[i].qubits[j] = q
+            if len(g) > 4:
+                for j, c in enumerate(g[4]):
+                    arr[i].pauli[j] = c
             arr[i].mat_off = mat_off
             arr[i].grad_off = grad_off
         h = nat.ctypes.c_void_p()
@@ -73,6 +78,21 @@ class GatePlan:
         self.npasses = st.npasses
         self.nstages = st.nstages
         self.tile_bits = st.tile_bits
+        # matrix-buffer entries of Pauli rotations: the engine writes dL/dphi
+        # there, which the autograd glue turns into the e^{i phi} cotangent
+        self.prot_offs = [g[3] for g in gates if g[0] == nat.TCG_GATE_PAULI_ROT and g[3] >= 0]
+        self._prot_mask: Dict[Any, torch.Tensor] = {}
+
+    def prot_mask(self, device: torch.device) -> Optional[torch.Tensor]:
+        if not self.prot_offs:
+            return None
+        m = self._prot_mask.get(device)
+        if m is None:
+            h = torch.zeros(self.nmat, dtype=torch.bool)
+            h[self.prot_offs] = True
+            m = h.to(device)
+            self._prot_mask[device] = m
+        return m
 
     def __del__(self) -> None:
         try:
@@ -225,6 +245,11 @@ class StateFn(torch.autograd.Function):
         spec = tuple(terms)
         gm, gp0 = AdjointFn.apply(mats, psi, gpsi, gcoef, ctx.run, spec)
         gm = gm.sum_to_size(ctx.mats_shape) if gm.shape != ctx.mats_shape else gm
+        pm = ctx.run.plan.prot_mask(gm.device)
+        if pm is not None:
+            # Pauli rotation entries hold z = e^{i phi} and the sweep returned
+            # g = dL/dphi; the cotangent with Re(conj(c) dz/dphi) = g is c = i z g
+            gm = torch.where(pm, 1j * mats * gm.real, gm)
         gp0 = gp0.sum_to_size(ctx.psi0_shape) if gp0.shape != ctx.psi0_shape else gp0
         return gm, gp0, None
 

@@ -320,10 +320,26 @@ class Family:
         self.diag = diag
         self.params = list(params)
         self.build = build
+        # Pauli rotations cos(phi) I - i sin(phi) P, phi = scale * theta:
+        # the engine takes them as one entry exp(i phi) (see PROT_FAMILIES)
+        self.pauli: Optional[str] = None
+        self.scale = 1.0
 
     @property
     def entries(self) -> int:
+        if self.pauli is not None:
+            return 1
         return (1 << self.nq) if self.diag else (1 << (2 * self.nq))
+
+
+PAULI_CODE = {"x": 1, "y": 2, "z": 3}
+
+
+def build_prot(theta: torch.Tensor, scale: float) -> torch.Tensor:
+    """exp(i phi), phi = scale * theta, as [G, 1]: the engine's encoding of
+    cos(phi) I - i sin(phi) P (cos and sin evaluated in double precision)."""
+    phi = _hi(theta) * scale
+    return torch.exp(1j * _c(phi))[..., None]
 
 
 _DEV_CONSTS: Dict[Tuple[str, str], torch.Tensor] = {}
@@ -375,6 +391,12 @@ FAMILIES: Dict[str, Family] = {
     "ory": Family("ory", 2, False, [("theta", 0.0)], _ctrl(build_ry, 1, False, False)),
     "orz": Family("orz", 2, True, [("theta", 0.0)], _ctrl(build_rz, 1, True, False)),
 }
+
+# Families that are Pauli rotations exp(-i theta/2 P) (tensorcircuit/gates.py:
+# 579-636 rx/ry/rz, :825-865 rxx/ryy/rzz = exp1(PP, theta, half=True)).
+for _name, _p in [("rx", "x"), ("ry", "y"), ("rz", "z"), ("rxx", "xx"), ("ryy", "yy"), ("rzz", "zz")]:
+    FAMILIES[_name].pauli = _p
+    FAMILIES[_name].scale = 0.5
 
 # gate method names as in the reference (tensorcircuit/abstractcircuit.py:28-66)
 sgates = ["i", "x", "y", "z", "h", "t", "s", "td", "sd", "wroot"] + \

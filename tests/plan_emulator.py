@@ -10,7 +10,7 @@ tiles, in-range global offsets -- before anything runs on a GPU.
 
 import numpy as np
 
-OP_DENSE1, OP_DENSE2, OP_DIAG, OP_DENSEK, OP_EXPECT = 0, 1, 2, 3, 4
+OP_DENSE1, OP_DENSE2, OP_DIAG, OP_DENSEK, OP_EXPECT, OP_PACC, OP_PROT = 0, 1, 2, 3, 4, 5, 6
 
 
 def dep(v, bits):
@@ -148,6 +148,17 @@ class Replay:
 
     # ------------------------------------------------------------ op helpers
     @staticmethod
+    def _pauli(V, op, G, R):
+        """P V for the op's Pauli string: the X/Y bits are the register mask
+        xreg, the Y/Z bits the global mask zmask, phase i^nY."""
+        X = op.xreg
+        assert 0 <= X < (1 << R)
+        r = np.arange(1 << R)
+        src = G[:, r ^ X]
+        sgn = 1 - 2 * (_popc(src & op.zmask) & 1)
+        return (1j ** (op.nY % 4)) * sgn * V[:, r ^ X]
+
+    @staticmethod
     def _mat(op, mats, dim):
         return np.asarray(mats[op.mat_off:op.mat_off + dim * dim], dtype=np.complex128).reshape(dim, dim)
 
@@ -191,6 +202,12 @@ class Replay:
             for i in range(k):
                 idx |= ((G >> op.p[i]) & 1) << (k - 1 - i)
             V = V * d[idx]
+        elif op.kind == OP_PROT:
+            z = complex(mats[op.mat_off])
+            c, s = z.real, z.imag
+            if adj:
+                s = -s
+            V = c * V - 1j * s * self._pauli(V, op, G, R)
         else:
             raise AssertionError("unexpected op kind %d" % op.kind)
         return V
@@ -233,6 +250,12 @@ class Replay:
                 for e in range(1 << k):
                     grads[op.grad_off + e] += np.sum(g[idx == e])
             W = W * d[idx]
+        elif op.kind == OP_PROT:
+            # dG/dphi = -i P G, so dL/dphi = Im <mu| P |psi_out>
+            if op.slot >= 0:
+                grads[op.grad_off] += np.sum(np.conj(W) * self._pauli(V, op, G, R)).imag
+            V = self._apply(V, op, mats, G, R, adj=True)
+            W = self._apply(W, op, mats, G, R, adj=True)
         else:
             raise AssertionError("unexpected op kind %d" % op.kind)
         return V, W

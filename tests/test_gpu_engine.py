@@ -354,3 +354,54 @@ def test_expectation_batching_follows_requests(tc):
         c = templates.apply_gate_list(tc.Circuit(n), gl)
         for s in seq:
             np.testing.assert_allclose(c.expectation_ps(**s).item(), sv.expectation_ps(psi, n, **s), atol=2e-5)
+
+
+def test_pauli_rotation_forms_state_and_gradient(tc):
+    """exp1 on Pauli strings (identity factors dropped, Y factors, half
+    angles, far-apart qubits) and the rotation families run as the engine's
+    Pauli-rotation kind; states and adjoint gradients match the oracle."""
+    X, Y, Z, I2 = (np.array(m, dtype=np.complex128) for m in
+                   ([[0, 1], [1, 0]], [[0, -1j], [1j, 0]], [[1, 0], [0, -1]], np.eye(2)))
+    n = 9
+    spec = [
+        ("rx", (0,), {}), ("ry", (8,), {}), ("rz", (4,), {}),
+        ("rxx", (1, 7), {}), ("ryy", (2, 3), {}), ("rzz", (0, 8), {}),
+        ("exp1", (1, 5, 6), {"unitary": np.kron(np.kron(X, I2), Y), "half": False}),
+        ("exp1", (0, 3), {"unitary": np.kron(Y, Y), "half": True}),
+        ("exp1", (2, 4, 8), {"unitary": np.kron(np.kron(Z, X), Z)}),
+        ("h", (3,), None), ("cnot", (3, 6), None),
+        ("exp1", (6, 7, 2, 0), {"unitary": np.kron(np.kron(X, Y), np.kron(X, Y))}),
+    ]
+    rng = np.random.default_rng(41)
+    thetas = rng.uniform(0, 2 * np.pi, len(spec))
+    terms = [(0.7, {"x": [0], "z": [5]}), (-1.1, {"y": [3, 8]}), (0.4, {"z": [2]})]
+
+    def build(c, th):
+        for i, (name, q, kw) in enumerate(spec):
+            if kw is None:
+                getattr(c, name)(*q)
+            else:
+                getattr(c, name)(*q, theta=th[i], **kw)
+        return c
+
+    from tensorcircuit_gb300 import templates
+
+    c = build(tc.Circuit(n), torch.tensor(thetas, dtype=torch.float32, device="cuda"))
+    assert any(op.kind == "prot" for op in c._ops)
+    ops = []
+    for i, (name, q, kw) in enumerate(spec):
+        ops.append((name, q, {} if kw is None else dict(kw, theta=float(np.float32(thetas[i])))))
+    want = sv.run_circuit(n, ops)
+    np.testing.assert_allclose(c.state().cpu().numpy(), want, atol=2e-5)
+
+    K = tc.set_backend("pytorch")
+
+    def f(th):
+        return templates.energy(build(tc.Circuit(n), th), terms)
+
+    v, g = K.value_and_grad(f)(torch.tensor(thetas, dtype=torch.float32, device="cuda"))
+    pidx = [i if kw is not None else None for i, (_, _, kw) in enumerate(spec)]
+    ops0 = [(name, q, {} if kw is None else dict(kw, theta=0.0)) for name, q, kw in spec]
+    ve, ge = sv.value_and_grad_adjoint(n, ops0, pidx, thetas.astype(np.float32).astype(np.float64), terms)
+    assert abs(v.item() - ve) < 1e-5
+    np.testing.assert_allclose(g.cpu().numpy(), ge, atol=2e-5)

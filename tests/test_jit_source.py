@@ -1,7 +1,11 @@
 """CPU: the plan specialiser's generated kernels compile for sm_103a (with
 the same preamble NVRTC uses), for every op kind and all four modes, and fit
-the register budget without spilling.  Skipped when nvcc is absent."""
+the register budget without spilling -- with nvcc (for the register report)
+and with NVRTC itself, the compiler the engine runs (it accepts a narrower
+language: no compiler builtins such as __builtin_popcount).  Skipped when
+nvcc is absent."""
 
+import ctypes
 import os
 import re
 import shutil
@@ -35,11 +39,41 @@ def compile_source(src):
         return r.returncode, r.stdout + r.stderr
 
 
+def _nvrtc():
+    for name in ("libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    return None
+
+
+def compile_nvrtc(src):
+    """Compile as the engine does (csrc/jit.cpp: same options, same name)."""
+    lib = _nvrtc()
+    if lib is None:
+        pytest.skip("NVRTC not available")
+    full = (open(PREAMBLE).read() + "\n" + src).encode()
+    prog = ctypes.c_void_p()
+    assert lib.nvrtcCreateProgram(ctypes.byref(prog), full, b"tcg_pass.cu", 0, None, None) == 0
+    opts = [b"--gpu-architecture=sm_103a", b"--std=c++17", b"-lineinfo", b"--ptxas-options=-v"]
+    arr = (ctypes.c_char_p * len(opts))(*opts)
+    rc = lib.nvrtcCompileProgram(prog, len(opts), arr)
+    size = ctypes.c_size_t(0)
+    lib.nvrtcGetProgramLogSize(prog, ctypes.byref(size))
+    buf = ctypes.create_string_buffer(max(size.value, 1))
+    lib.nvrtcGetProgramLog(prog, buf)
+    lib.nvrtcDestroyProgram(ctypes.byref(prog))
+    return rc, buf.value.decode(errors="replace")
+
+
 def check_compiles(handle, which, mode):
     st, src = nat.jit_info(handle, which, mode, what=1)
     assert "tcgk" in src and "_0(" in src
     rc, log = compile_source(src)
     assert rc == 0, log[-3000:]
+    rc, nlog = compile_nvrtc(src)
+    assert rc == 0, nlog[-3000:]
     spills = [int(x) for x in re.findall(r"(\d+) bytes spill stores", log)]
     regs = [int(x) for x in re.findall(r"Used (\d+) registers", log)]
     return regs, spills

@@ -114,13 +114,28 @@ def test_backward_program_replay_matches_oracle(n, ngates, seed):
     # compare the cotangents of gates that carry a gradient slot (the random
     # lists never contain the identity, so engine ops and list entries align)
     assert len(entry.gates_c) == len(gl)
-    for gi, (kind, qubits, mat_off, grad_off) in enumerate(entry.gates_c):
+    nprot = 0
+    for gi, g in enumerate(entry.gates_c):
+        kind, qubits, mat_off, grad_off = g[:4]
         if grad_off < 0:
             continue
         cot = want_cot[gi]
+        if kind == nat.TCG_GATE_PAULI_ROT:
+            # the engine returns dL/dphi for G = cos(phi) I - i sin(phi) P
+            nprot += 1
+            z = complex(mats[mat_off])
+            pm = np.ones((1, 1), np.complex128)
+            for code in g[4]:
+                pm = np.kron(pm, sv.gate_matrix("ixyz"[code]))
+            dg = -z.imag * np.eye(pm.shape[0]) - 1j * z.real * pm
+            want = np.sum(np.conj(cot) * dg).real
+            np.testing.assert_allclose(grads[grad_off].real, want, atol=1e-3, rtol=1e-4)
+            assert grads[grad_off].imag == 0
+            continue
         want = np.diag(cot) if kind == nat.TCG_GATE_DIAG else cot.reshape(-1)
         got = grads[grad_off:grad_off + want.size]
         np.testing.assert_allclose(got, want, atol=1e-3, rtol=1e-4)
+    assert nprot > 0
 
 
 @pytest.mark.parametrize("n,seed", [(6, 0), (10, 1), (14, 2)])
@@ -170,3 +185,27 @@ def test_hea_plan_pass_counts():
     entry = cmod._build_entry(n, c._ops)
     assert entry.plan.npasses <= 8
     assert entry.plan.ngates == 312
+
+
+def test_pauli_rotation_exp1_forms_replay():
+    """exp1 on Pauli strings (identity factors, Y factors, half angles) is
+    recorded as the Pauli-rotation kind; the replayed forward program and
+    its adjoint cotangents match the oracle."""
+    X, Y, Z, I2 = (np.array(m, dtype=np.complex128) for m in
+                   ([[0, 1], [1, 0]], [[0, -1j], [1j, 0]], [[1, 0], [0, -1]], np.eye(2)))
+    gl = [("h", (0,), {}), ("h", (5,), {}),
+          ("exp1", (1, 5, 6), {"unitary": np.kron(np.kron(X, I2), Y), "theta": 0.7}),
+          ("exp1", (0, 3), {"unitary": np.kron(Y, Y), "theta": 1.3, "half": True}),
+          ("exp1", (2, 4, 7), {"unitary": np.kron(np.kron(Z, X), Z), "theta": -0.4}),
+          ("exp1", (6, 7, 2, 0), {"unitary": np.kron(np.kron(X, Y), np.kron(X, Y)), "theta": 2.1}),
+          ("rzz", (0, 7), {"theta": 0.9}), ("ry", (3,), {"theta": 0.2})]
+    n = 8
+    c, entry, mats, n_eng = build_host(n, gl)
+    kinds = [g[0] for g in entry.gates_c]
+    assert kinds.count(nat.TCG_GATE_PAULI_ROT) == 6
+    # the first exp1 drops its identity factor
+    assert tuple(entry.gates_c[2][1]) == (1, 6)
+    prog = nat.debug_program(entry.plan.handle, 0)
+    psi0 = np.zeros(1 << n, np.complex128)
+    psi0[0] = 1
+    np.testing.assert_allclose(Replay(prog, n).forward(psi0, mats), sv.run_circuit(n, gl), atol=2e-6)
