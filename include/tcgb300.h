@@ -45,7 +45,8 @@ enum {
   TCG_ERR_CUDA = 4,          /* a CUDA runtime call failed */
   TCG_ERR_SCRATCH = 5,       /* caller-provided scratch is too small */
   TCG_ERR_OOM = 6,           /* a host or device allocation failed */
-  TCG_ERR_TOO_LARGE = 7      /* request exceeds a fixed internal capacity */
+  TCG_ERR_TOO_LARGE = 7,     /* request exceeds a fixed internal capacity */
+  TCG_ERR_TIMEOUT = 8        /* a bounded device-side wait ran out of time */
 };
 
 /* ---- gate program --------------------------------------------------------- */
@@ -208,6 +209,76 @@ size_t tcg_inner_scratch_bytes(int64_t len, int64_t batch);
 /* ---- misc ------------------------------------------------------------------ */
 const char* tcg_status_string(int32_t status);
 int32_t tcg_abi_version(void);
+
+/* ---- uneven batches --------------------------------------------------------
+ * Many parameterized circuits of different qubit counts and depths, each with
+ * its own energy <H_c> = offset_c + sum_t coef_c[t] <psi_c|P_t|psi_c>, value
+ * and adjoint gradient of every circuit in ONE call: one persistent kernel
+ * launch per sweep (forward, measure, Pauli accumulate, adjoint) covers all
+ * circuits, so the call is a fixed sequence of eight kernels that a CUDA
+ * graph can capture.  Replaces the reference's loop of per-circuit
+ * `K.value_and_grad(f)` calls (tensorcircuit/backends/pytorch_backend.py:
+ * 533-544 over circuits built with tensorcircuit/templates/blocks.py:84-110
+ * and measured with tensorcircuit/templates/measurements.py:290-335), which
+ * has no batched form for circuits whose sizes differ.
+ *
+ * Parameterized gates must be Pauli rotations (TCG_GATE_PAULI_ROT) whose
+ * angle is phi = mat_scale[e] * params_c[mat_param[e]] for their matrix entry
+ * e; every other entry is a constant.  Gradients are d<H_c>/d params_c. */
+typedef struct tcg_ubatch tcg_ubatch;
+
+typedef struct tcg_ubatch_circuit {
+  int32_t nqubits;          /* >= tile_bits of the batch                    */
+  int32_t ngates;
+  const tcg_gate* gates;    /* mat_off / grad_off index the circuit's own
+                               matrix buffer; grad_off >= 0 only on
+                               parameterized Pauli rotations                */
+  int64_t nmat;             /* complex entries of the circuit's matrices    */
+  const float* mat_const;   /* host, 2*nmat floats: constant entries        */
+  const int64_t* mat_param; /* host, nmat: parameter of a rotation entry,
+                               -1 for a constant entry                      */
+  const float* mat_scale;   /* host, nmat: phi = scale * theta              */
+  int32_t nparams;
+  int32_t nterms;
+  const tcg_pauli* terms;   /* host, nterms                                  */
+  const float* coef;        /* host, nterms                                  */
+  double offset;
+} tcg_ubatch_circuit;
+
+/* tile_bits: local index bits per tile, 5 < tile_bits <= 12 and <= every
+ * circuit's qubit count (the autotuner's knob).  Host arrays are copied. */
+int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int32_t tile_bits,
+                      tcg_ubatch** out);
+int tcg_ubatch_destroy(tcg_ubatch* batch);
+
+/* nparams_total = sum of nparams (the layout of params and grads: circuit 0's
+ * parameters first); state_entries = sum of 2^n; scratch_bytes = device
+ * scratch one call needs (states, cotangents, matrices, partial sums). */
+int tcg_ubatch_info(const tcg_ubatch* batch, int64_t* nparams_total, int64_t* state_entries,
+                    size_t* scratch_bytes);
+
+/* Complex-entry offset of circuit c's state inside the scratch buffer (the
+ * states sit at the start of scratch, back to back).  After a call with
+ * grads == NULL it holds the circuit's final state; a call with gradients
+ * uncomputes it back to |0...0> during the adjoint sweep. */
+int64_t tcg_ubatch_state_offset(const tcg_ubatch* batch, int32_t c);
+
+/* energies[c] (float32) for every circuit and, when grads is not NULL,
+ * grads[nparams_total] (float32).  params: device float32 [nparams_total].
+ * Reductions run in float64 in a fixed order (deterministic). */
+int tcg_ubatch_value_and_grad(tcg_ubatch* batch, const float* params, float* energies, float* grads,
+                              void* scratch, size_t scratch_bytes, void* stream);
+
+/* Work of one call per sweep (index 0 forward, 1 adjoint, 2 measure,
+ * 3 Pauli accumulate): tiles processed and algorithmic HBM bytes (16 per
+ * amplitude for the forward sweep, 32 adjoint, 8 measure, 24 accumulate). */
+int tcg_ubatch_stats(const tcg_ubatch* batch, int64_t* tiles, double* alg_bytes);
+
+/* Synchronises the stream and reports TCG_ERR_TIMEOUT if a dependency wait
+ * of an earlier call ran out of time (its results are then invalid), else
+ * TCG_OK; clears the flag.  The flag lives in the scratch buffer: zero the
+ * scratch once before its first use so that it starts clear. */
+int tcg_ubatch_check(tcg_ubatch* batch, void* scratch, void* stream);
 
 /* Diagnostics (no reference counterpart): host pointers to a plan's pass
  * program so tests can replay its index arithmetic on the CPU.  which = 0

@@ -95,3 +95,44 @@ def run_gate_list(n: int, gl: Sequence[Tuple[str, Tuple[int, ...], Dict[str, Any
         g = torch.as_tensor(np.asarray(p["unitary"], dtype=np.complex64)).reshape([2] * (2 * k))
         psi = _apply(psi, g, q)
     return psi.reshape(-1)
+
+
+def _exp1_zz(theta: torch.Tensor) -> torch.Tensor:
+    """exp1(ZZ, theta) = cos(theta) I - i sin(theta) ZZ (tensorcircuit/gates.py:825-846, half=False)."""
+    c = torch.cos(theta).to(C64)
+    s = torch.sin(theta).to(C64)
+    zz = torch.diag(torch.tensor([1, -1, -1, 1], dtype=C64))
+    return (c * torch.eye(4, dtype=C64) - 1j * s * zz).reshape(2, 2, 2, 2)
+
+
+def qaoa_value_and_grad(n: int, edges: Sequence[Tuple[int, int]], p: int, params: np.ndarray,
+                        threads: int) -> Tuple[float, np.ndarray]:
+    """MaxCut QAOA energy sum_(ij) (1 - <Z_i Z_j>)/2 and its gradient for one
+    circuit, per-gate tensordot in circuit order with taped reverse-mode AD
+    (the reference's ``K.value_and_grad`` on the pytorch backend,
+    tensorcircuit/backends/pytorch_backend.py:533-544; circuit from
+    tensorcircuit/templates/blocks.py:84-110)."""
+    torch.set_num_threads(threads)
+    h = torch.tensor([[1, 1], [1, -1]], dtype=C64) / np.sqrt(2)
+    z = _PAULI["z"]
+
+    def f(prm: torch.Tensor) -> torch.Tensor:
+        psi = torch.zeros([2] * n, dtype=C64)
+        psi.view(-1)[0] = 1.0
+        for i in range(n):
+            psi = _apply(psi, h, (i,))
+        for layer in range(p):
+            g = _exp1_zz(prm[layer])
+            for a, b in edges:
+                psi = _apply(psi, g, (a, b))
+            r = _rx(prm[p + layer])
+            for i in range(n):
+                psi = _apply(psi, r, (i,))
+        e = torch.zeros((), dtype=torch.float32)
+        for a, b in edges:
+            phi = _apply(_apply(psi, z, (a,)), z, (b,))
+            e = e + 0.5 * (1.0 - torch.real(torch.sum(torch.conj(psi) * phi)))
+        return e
+
+    g, v = torch.func.grad_and_value(f)(torch.as_tensor(params, dtype=torch.float32))
+    return float(v), g.numpy()

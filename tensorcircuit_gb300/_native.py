@@ -20,6 +20,7 @@ TCG_ERR_CUDA = 4
 TCG_ERR_SCRATCH = 5
 TCG_ERR_OOM = 6
 TCG_ERR_TOO_LARGE = 7
+TCG_ERR_TIMEOUT = 8
 
 TCG_GATE_DENSE = 0
 TCG_GATE_DIAG = 1
@@ -58,6 +59,23 @@ class TcgPauli(ctypes.Structure):
     _fields_ = [("xmask", ctypes.c_uint64), ("zmask", ctypes.c_uint64)]
 
 
+class TcgUbatchCircuit(ctypes.Structure):
+    _fields_ = [
+        ("nqubits", ctypes.c_int32),
+        ("ngates", ctypes.c_int32),
+        ("gates", ctypes.POINTER(TcgGate)),
+        ("nmat", ctypes.c_int64),
+        ("mat_const", ctypes.POINTER(ctypes.c_float)),
+        ("mat_param", ctypes.POINTER(ctypes.c_int64)),
+        ("mat_scale", ctypes.POINTER(ctypes.c_float)),
+        ("nparams", ctypes.c_int32),
+        ("nterms", ctypes.c_int32),
+        ("terms", ctypes.POINTER(TcgPauli)),
+        ("coef", ctypes.POINTER(ctypes.c_float)),
+        ("offset", ctypes.c_double),
+    ]
+
+
 # (name, restype, argtypes) for every exported symbol
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -84,6 +102,13 @@ SIGNATURES = [
     ("tcg_probability", ctypes.c_int, [_P, _I64, _P, _P]),
     ("tcg_inner_scratch_bytes", _SZ, [_I64, _I64]),
     ("tcg_inner", ctypes.c_int, [_P, _P, _I64, _I64, _P, _P, _SZ, _P]),
+    ("tcg_ubatch_create", ctypes.c_int, [ctypes.POINTER(TcgUbatchCircuit), _I32, _I32, ctypes.POINTER(_P)]),
+    ("tcg_ubatch_destroy", ctypes.c_int, [_P]),
+    ("tcg_ubatch_info", ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_SZ)]),
+    ("tcg_ubatch_state_offset", _I64, [_P, _I32]),
+    ("tcg_ubatch_value_and_grad", ctypes.c_int, [_P, _P, _P, _P, _P, _SZ, _P]),
+    ("tcg_ubatch_stats", ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double)]),
+    ("tcg_ubatch_check", ctypes.c_int, [_P, _P, _P]),
     ("tcg_launch_count", _I64, []),
     ("tcg_debug_jit", ctypes.c_int, [_P, _I32, _I32, ctypes.POINTER(_I32), ctypes.c_char_p, _I64, _I32]),
     ("tcg_debug_program", ctypes.c_int, [_P, _I32, ctypes.POINTER(_P), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),

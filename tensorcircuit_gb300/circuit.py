@@ -53,8 +53,23 @@ def _to_np_matrix(m: Any) -> Optional[np.ndarray]:
     return a.reshape(d, d)
 
 
+_PAULI_CACHE: Dict[bytes, Optional[Tuple[int, ...]]] = {}
+
+
 def _pauli_decompose(m: np.ndarray) -> Optional[List[int]]:
-    """If m is a tensor product of single-qubit Paulis, return their codes."""
+    """If m is a tensor product of single-qubit Paulis, return their codes
+    (memoised by the matrix bytes: circuits repeat the same few matrices)."""
+    key = m.tobytes() + bytes([m.shape[0]])
+    if key in _PAULI_CACHE:
+        r = _PAULI_CACHE[key]
+        return None if r is None else list(r)
+    r = _pauli_decompose_uncached(m)
+    if len(_PAULI_CACHE) < 4096:
+        _PAULI_CACHE[key] = None if r is None else tuple(r)
+    return r
+
+
+def _pauli_decompose_uncached(m: np.ndarray) -> Optional[List[int]]:
     d = m.shape[0]
     k = int(round(np.log2(d)))
     if (1 << k) != d:

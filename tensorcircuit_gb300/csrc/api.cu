@@ -142,6 +142,7 @@ const char* tcg_status_string(int32_t s) {
     case TCG_ERR_TOO_LARGE:
       return "request exceeds a fixed internal capacity (tcg_expect_pauli_noalloc: nterms <= 64, "
              "batch <= 65535, batch * nterms <= 6898)";
+    case TCG_ERR_TIMEOUT: return "a bounded device-side wait ran out of time (results invalid)";
     default: return "unknown status";
   }
 }

@@ -43,6 +43,47 @@ struct KParams_Host {
   long long coef_stride;
 };
 
+// ---- uneven batches: many circuits, one persistent launch per sweep.
+// Work item = one tile of one pass of one circuit; items are dequeued in
+// order from a global counter, and an item of pass p waits (bounded) until
+// every tile of pass p-1 of its circuit is complete.
+struct BatchCirc {
+  ProgramView prog;     // this launch's program (FWD / MEAS / PACC / BWD)
+  int32_t n;
+  int32_t max_slots;
+  int64_t state_off;    // complex entries into the ragged state buffers
+  int64_t mat_off;      // complex entries into the ragged matrix buffer
+  int64_t part_off;     // complex entries into the partial buffer
+  int64_t part_stride;  // accumulator outputs per tile slice
+  int64_t coef_off;     // PACC coefficients
+};
+struct BatchSeg {
+  int64_t item0;        // first work item of this (circuit, pass)
+  int32_t circ;
+  int32_t pass;
+  uint32_t ntiles;
+  uint32_t need;        // completed tiles of the circuit this segment waits for
+};
+struct BatchLaunch {
+  const BatchCirc* circ;
+  const BatchSeg* segs;
+  int32_t nsegs;
+  int32_t pad;
+  int64_t nitems;
+  float2* psi;
+  float2* mu;
+  const float2* mats;
+  float2* partial;
+  const float* coef;
+  unsigned int* queue;  // work-item counter, zero at launch
+  unsigned int* done;   // per-circuit completed tiles, zero at launch
+  unsigned int* err;    // this call: a dependency wait ran out of time (zero at launch)
+  unsigned int* sticky; // set with err; cleared only by the caller's check
+};
+// L: tile bits shared by every program of the launch; max_slots: largest
+// stage slot count over the circuits.
+cudaError_t launch_batch(int mode, const BatchLaunch& bl, int L, int max_slots, cudaStream_t st);
+
 // every kernel launch of the library increments this counter
 void count_launch(int64_t n = 1);
 int64_t launch_count();

@@ -409,7 +409,7 @@ __device__ __forceinline__ void tile_load_smem(float2* sm, const float2* __restr
   for (uint32_t i = tid; i < half; i += nthreads) {
     const uint32_t j = 2 * i;
     const uint32_t off = __ldg(runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
-    const float4 q = __ldg(reinterpret_cast<const float4*>(src + (base | off)));
+    const float4 q = __ldcg(reinterpret_cast<const float4*>(src + (base | off)));
     sm[swz(j)] = make_float2(q.x, q.y);
     sm[swz(j + 1)] = make_float2(q.z, q.w);
   }
@@ -475,7 +475,7 @@ template <int R>
 __device__ __forceinline__ void regs_from_global(float2 (&v)[1 << R], const float2* __restrict__ src,
                                                  uint32_t base, const Layout& ly) {
 #pragma unroll
-  for (int r = 0; r < (1 << R); ++r) v[r] = __ldg(src + (base | ly.gt | roff<R>(ly, r, true)));
+  for (int r = 0; r < (1 << R); ++r) v[r] = __ldcg(src + (base | ly.gt | roff<R>(ly, r, true)));
 }
 template <int R>
 __device__ __forceinline__ void regs_to_global(const float2 (&v)[1 << R], float2* __restrict__ dst,
@@ -496,13 +496,15 @@ __device__ __forceinline__ bool same_layout(const DevStage& a, const DevStage& b
 }  // namespace
 
 // ============================================================================
+// One tile of one pass: state loads go through L2 (ld.global.cg) so that a
+// persistent launch may read tiles written earlier in the same launch.
 template <int MODE, int R>
-__global__ void __launch_bounds__(256, 1) pass_kernel(PassArgs A) {
+__device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int64_t b, uint32_t ntiles,
+                                          float2* smem_raw) {
   constexpr int NR = 1 << R;
   constexpr bool HAS_MU = (MODE == MODE_BWD || MODE == MODE_PACC);
   constexpr bool STORE_PSI = (MODE == MODE_FWD || MODE == MODE_BWD);
   constexpr bool STORE_MU = HAS_MU;
-  extern __shared__ __align__(16) float2 smem_raw[];
 
   const DevPass& P = A.prog.passes[A.pass];
   const int L = P.L;
@@ -512,9 +514,6 @@ __global__ void __launch_bounds__(256, 1) pass_kernel(PassArgs A) {
   const int lane = tid & 31;
   const int nwarps = (nthreads + 31) >> 5;
   const int nl = nthreads < 32 ? nthreads : 32;
-  const uint32_t tile = blockIdx.x;
-  const int64_t b = blockIdx.y;
-  const uint32_t ntiles = gridDim.x;
 
   float2* sm_psi = smem_raw;
   float2* sm_mu = smem_raw + (HAS_MU ? (1u << L) : 0u);
@@ -801,6 +800,94 @@ __global__ void __launch_bounds__(256, 1) pass_kernel(PassArgs A) {
   }
 }
 
+template <int MODE, int R>
+__global__ void __launch_bounds__(256, 1) pass_kernel(PassArgs A) {
+  extern __shared__ __align__(16) float2 smem_raw[];
+  pass_tile<MODE, R>(A, blockIdx.x, blockIdx.y, gridDim.x, smem_raw);
+}
+
+// ------------------------------------------------------ persistent batches
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// A dependency is always a set of items dequeued earlier by CTAs that are
+// running, so waits end; the limit only guards against a broken schedule.
+// After a time-out every later wait is skipped (results are then invalid and
+// the error flag says so) so the launch still finishes.
+constexpr unsigned long long kBatchWaitNs = 2000000000ull;
+
+template <int MODE, int R>
+__global__ void __launch_bounds__(256, 1) batch_kernel(BatchLaunch BL) {
+  extern __shared__ __align__(16) float2 smem_raw[];
+  __shared__ long long s_item;
+  __shared__ int s_seg;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const long long item = (long long)atomicAdd(BL.queue, 1u);
+      int seg = -1;
+      if (item < BL.nitems) {
+        int lo = 0, hi = BL.nsegs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (BL.segs[mid].item0 <= item) lo = mid;
+          else hi = mid - 1;
+        }
+        seg = lo;
+        const unsigned need = BL.segs[seg].need;
+        const unsigned* dn = BL.done + BL.segs[seg].circ;
+        if (need > 0 && ld_acquire_u32(dn) < need && ld_acquire_u32(BL.err) == 0u) {
+          const unsigned long long t0 = global_ns();
+          unsigned spins = 0;
+          while (ld_acquire_u32(dn) < need) {
+            __nanosleep(100);
+            if ((++spins & 63u) == 0u && (global_ns() - t0 > kBatchWaitNs || ld_acquire_u32(BL.err) != 0u)) {
+              atomicOr(BL.err, 1u);
+              atomicOr(BL.sticky, 1u);
+              break;
+            }
+          }
+        }
+        __threadfence();
+      }
+      s_item = item;
+      s_seg = seg;
+    }
+    __syncthreads();
+    const long long item = s_item;
+    const int seg = s_seg;
+    if (seg < 0) break;
+    const BatchSeg sg = BL.segs[seg];
+    const BatchCirc& C = BL.circ[sg.circ];
+    PassArgs A;
+    A.prog = C.prog;
+    A.pass = sg.pass;
+    A.n = C.n;
+    A.psi = BL.psi + C.state_off;
+    A.mu = BL.mu ? BL.mu + C.state_off : nullptr;
+    A.mats = BL.mats ? BL.mats + C.mat_off : nullptr;
+    A.mat_stride = 0;
+    A.partial = BL.partial ? BL.partial + C.part_off : nullptr;
+    A.part_stride = C.part_stride;
+    A.coef = BL.coef ? BL.coef + C.coef_off : nullptr;
+    A.coef_stride = 0;
+    A.max_slots = C.max_slots;
+    pass_tile<MODE, R>(A, (uint32_t)(item - sg.item0), 0, sg.ntiles, smem_raw);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(BL.done + sg.circ, 1u);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- launchers
 template <int MODE, int R>
 static cudaError_t launch_one(const PassArgs& a, int L, int64_t batch, cudaStream_t st) {
@@ -838,6 +925,46 @@ static cudaError_t launch_one(const PassArgs& a, int L, int64_t batch, cudaStrea
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+template <int MODE, int R>
+static cudaError_t launch_batch_one(const BatchLaunch& bl, int L, int max_slots, cudaStream_t st) {
+  const int nthreads = 1 << (L - R);
+  if (nthreads > kMaxThreads || nthreads < 1) return cudaErrorInvalidValue;
+  const bool has_mu = (MODE == MODE_BWD || MODE == MODE_PACC);
+  const int nwarps = (nthreads + 31) / 32;
+  const size_t smem = size_t(has_mu ? 2 : 1) * (size_t(1) << L) * sizeof(float2) +
+                      size_t(nwarps) * max_slots * sizeof(float2);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static int attr_smem[64] = {0};
+  if (dev < 64 && attr_smem[dev] < (int)smem) {
+    e = cudaFuncSetAttribute(batch_kernel<MODE, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_smem[dev] = (int)smem;
+  }
+  int nsm = 0, per_sm = 0;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<MODE, R>, nthreads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int64_t grid = int64_t(nsm) * per_sm;
+  if (grid > bl.nitems) grid = bl.nitems;
+  if (grid < 1) return cudaSuccess;
+  count_launch();
+  batch_kernel<MODE, R><<<(unsigned)grid, nthreads, smem, st>>>(bl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch(int mode, const BatchLaunch& bl, int L, int max_slots, cudaStream_t st) {
+  if (max_slots < 1) max_slots = 1;
+  if (mode == MODE_FWD) return launch_batch_one<MODE_FWD, 4>(bl, L, max_slots, st);
+  if (mode == MODE_BWD) return launch_batch_one<MODE_BWD, 4>(bl, L, max_slots, st);
+  if (mode == MODE_MEAS) return launch_batch_one<MODE_MEAS, 4>(bl, L, max_slots, st);
+  if (mode == MODE_PACC) return launch_batch_one<MODE_PACC, 4>(bl, L, max_slots, st);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_pass(int mode, int R, const PassArgs& a, int L, int64_t batch, cudaStream_t st) {

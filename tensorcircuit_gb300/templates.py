@@ -162,3 +162,23 @@ def spin_glass_measurements(c: Any, edges: Sequence[Tuple[int, int, float]],
     for v, w in (node_weights or {}).items():
         loss = loss + w * c.expectation_ps(z=[v])
     return torch.real(loss)
+
+
+def qaoa_uneven_workload(count: int = 512, seed: int = 5, nmin: int = 12, nmax: int = 24,
+                         pmax: int = 6) -> Tuple[List[Any], List[np.ndarray]]:
+    """The uneven QAOA MaxCut batch: ``count`` circuits with n ~ U{nmin,
+    nmin+2, ..., nmax} (3-regular graphs need even n), a random 3-regular
+    graph each, depth p ~ U{1..pmax}, gamma, beta ~ U[0, pi) (float32).
+    Returns (specs for tensorcircuit_gb300.batch.UnevenBatch, parameter
+    vectors [gammas, betas])."""
+    from .batch import qaoa_spec
+
+    rng = np.random.default_rng(seed)
+    specs, params = [], []
+    for _ in range(count):
+        n = int(rng.choice(np.arange(nmin, nmax + 1, 2)))
+        p = int(rng.integers(1, pmax + 1))
+        edges = random_regular_graph(3, n, np.random.default_rng(int(rng.integers(1 << 31))))
+        specs.append(qaoa_spec(n, edges, p))
+        params.append(rng.uniform(0, np.pi, 2 * p).astype(np.float32))
+    return specs, params
