@@ -594,15 +594,57 @@ def run_qaoa(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_warmstart(args, rank, world):
+    """Learned warm start: random-coupling open TFIM n=16, HEA depth 6 (186
+    angles), Adam lr 0.02; training angles generated by the engine's batched
+    adjoint Adam (``--instances`` chains x 300 steps), the 31-256-256-186
+    network trained with the project's kernels, then held-out chains
+    optimised for 300 steps from the network's angles and from random ones,
+    judged against the exact free-fermion ground energy."""
+    import torch
+
+    import tensorcircuit_gb300 as tc
+    from tensorcircuit_gb300 import _native, warmstart as ws
+
+    tc.build()
+    lib = _native.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    l0 = lib.tcg_launch_count()
+    with ClockSampler(dev.index) as clk:
+        r = ws.study(n_train=args.instances, n_test=args.held_out, steps=300, gen_steps=300,
+                     epochs=args.epochs)
+    launches = lib.tcg_launch_count() - l0
+    if rank != 0:
+        return
+    gen_evals = args.instances * 301
+    line = {
+        "metric": "warm-start Adam steps to the random start's 300-step error (ratio random / warm)",
+        "value": r["step_ratio"], "unit": "x fewer steps", "n_gpus": world, "steps": 1, "warmup": 0,
+        "ms_per_step": 1e3 * sum(r["seconds"].values()), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 simulator / bf16 network activations", "data": "synthetic",
+        "config": {"workload": "tfim_n16_hea6_warmstart", "train_chains": args.instances,
+                   "held_out": args.held_out, "epochs": args.epochs, "seed": 6},
+        "study": r,
+        "generation_throughput": {"value": gen_evals / r["seconds"]["generate"],
+                                  "unit": "n=16 energy+gradient evaluations/s"},
+        "cpu_baseline": None, "clocks": clk.summary(), "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hea", choices=["hea", "brickwall", "qaoa"],
+    ap.add_argument("--workload", default="hea", choices=["hea", "brickwall", "qaoa", "warmstart"],
                     help="hea: n=20 HEA batched vvag (default); brickwall: n=28 Haar brick wall; "
-                         "qaoa: 512 uneven QAOA circuits in one persistent launch per sweep")
+                         "qaoa: 512 uneven QAOA circuits in one persistent launch per sweep; "
+                         "warmstart: learned warm start for n=16 TFIM chains")
+    ap.add_argument("--instances", type=int, default=20000, help="warmstart: training chains")
+    ap.add_argument("--held-out", type=int, default=1000, help="warmstart: held-out chains")
+    ap.add_argument("--epochs", type=int, default=200, help="warmstart: network training epochs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -620,6 +662,8 @@ def main():
         run_brickwall(args, rank, world)
     elif args.workload == "qaoa":
         run_qaoa(args, rank, world)
+    elif args.workload == "warmstart":
+        run_warmstart(args, rank, world)
     else:
         run_gb300_arm(args, rank, world)
     if world > 1:

@@ -208,6 +208,7 @@ size_t tcg_inner_scratch_bytes(int64_t len, int64_t batch);
 
 /* ---- misc ------------------------------------------------------------------ */
 const char* tcg_status_string(int32_t status);
+/* 2: tcg_gate gained `pauli` (Pauli-rotation gates); uneven batches added. */
 int32_t tcg_abi_version(void);
 
 /* ---- uneven batches --------------------------------------------------------
@@ -279,6 +280,27 @@ int tcg_ubatch_stats(const tcg_ubatch* batch, int64_t* tiles, double* alg_bytes)
  * TCG_OK; clears the flag.  The flag lives in the scratch buffer: zero the
  * scratch once before its first use so that it starts clear. */
 int tcg_ubatch_check(tcg_ubatch* batch, void* scratch, void* stream);
+
+/* ---- learned warm start (no reference counterpart) ---------------------------
+ * Kernels of the network that maps Hamiltonian couplings to circuit angles
+ * (tensorcircuit_gb300/warmstart.py).  Row-major float32 weights w[out][in];
+ * activations bfloat16 (x_bf16 / y_bf16 = 1) or float32; float32 accumulation.
+ * act: 0 identity, 1 GELU (tanh form). */
+int tcg_mlp_linear_forward(const void* x, int32_t x_bf16, const float* w, const float* bias,
+                           int64_t batch, int32_t in, int32_t out, int32_t act, float* pre,
+                           void* y, int32_t y_bf16, void* stream);
+/* dz = dy * act'(pre); dw = dz^T x (overwritten); db = column sums of dz
+ * (overwritten); dx = dz w when dx is not NULL.  Fixed-order reductions. */
+int tcg_mlp_linear_backward(const float* dy, const float* pre, int32_t act, const void* x,
+                            int32_t x_bf16, const float* w, int64_t batch, int32_t in, int32_t out,
+                            float* dz, float* dw, float* db, float* dx, void* stream);
+/* Angle regression loss mean(1 - cos(pred - target)) over n entries:
+ * dpred = sin(pred - target) / n, partial[nblocks] = per-block loss sums. */
+int tcg_periodic_loss(const float* pred, const float* target, int64_t n, float* dpred,
+                      float* partial, int32_t nblocks, void* stream);
+/* Adam (bias-corrected, step >= 1) on n float32 parameters in place. */
+int tcg_adam_update(float* p, const float* g, float* m, float* v, int64_t n, float lr, float beta1,
+                    float beta2, float eps, int32_t step, void* stream);
 
 /* Diagnostics (no reference counterpart): host pointers to a plan's pass
  * program so tests can replay its index arithmetic on the CPU.  which = 0

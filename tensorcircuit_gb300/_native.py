@@ -109,6 +109,12 @@ SIGNATURES = [
     ("tcg_ubatch_value_and_grad", ctypes.c_int, [_P, _P, _P, _P, _P, _SZ, _P]),
     ("tcg_ubatch_stats", ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double)]),
     ("tcg_ubatch_check", ctypes.c_int, [_P, _P, _P]),
+    ("tcg_mlp_linear_forward", ctypes.c_int, [_P, _I32, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _I32, _P]),
+    ("tcg_mlp_linear_backward", ctypes.c_int,
+     [_P, _P, _I32, _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P, _P, _P]),
+    ("tcg_periodic_loss", ctypes.c_int, [_P, _P, _I64, _P, _P, _I32, _P]),
+    ("tcg_adam_update", ctypes.c_int, [_P, _P, _P, _P, _I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_float, _I32, _P]),
     ("tcg_launch_count", _I64, []),
     ("tcg_debug_jit", ctypes.c_int, [_P, _I32, _I32, ctypes.POINTER(_I32), ctypes.c_char_p, _I64, _I32]),
     ("tcg_debug_program", ctypes.c_int, [_P, _I32, ctypes.POINTER(_P), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),

@@ -13,7 +13,7 @@ using namespace tcg;
 
 namespace {
 
-constexpr int kAbiVersion = 1;
+constexpr int kAbiVersion = 2;
 
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 

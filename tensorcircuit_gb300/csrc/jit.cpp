@@ -440,8 +440,10 @@ class Gen {
     for (size_t i = 0; i < so.size(); ++i) out << (i ? ", " : "") << so[i];
     out << "};\n";
 
-    // kernel
-    out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", " << (bwd() ? 1 : 2) << ") "
+    // kernel: two CTAs per SM in every mode (the adjoint kernel then has 128
+    // registers for psi + mu; a second resident CTA hides the latency of the
+    // dependent FMA chains and shuffles that a single 8-warp CTA exposes)
+    out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", 2) "
         << kernel_name(mode_, pi)
         << "(KParams kp) {\n";
     out << "  using namespace tk;\n  extern __shared__ __align__(16) float2 smem[];\n";

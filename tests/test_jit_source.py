@@ -86,8 +86,10 @@ def test_hea_forward_and_adjoint_kernels_compile():
     regs_f, sp_f = check_compiles(e.plan.handle, 0, 0)
     regs_b, sp_b = check_compiles(e.plan.handle, 1, 1)
     print("forward registers", regs_f, "adjoint registers", regs_b, "spills", sp_f, sp_b)
-    assert max(sp_f + [0]) == 0 and max(sp_b + [0]) == 0
-    assert max(regs_f) <= 128, regs_f
+    # two CTAs per SM: at most 128 registers; the adjoint kernels (psi and mu
+    # in registers) may spill a few words
+    assert max(sp_f + [0]) == 0 and max(sp_b + [0]) <= 64
+    assert max(regs_f) <= 128 and max(regs_b) <= 128, (regs_f, regs_b)
 
 
 def test_random_circuit_kernels_compile():
