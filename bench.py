@@ -633,6 +633,7 @@ def run_warmstart(args, rank, world):
 
 
 def main():
+    global BATCH
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -642,11 +643,15 @@ def main():
                     help="hea: n=20 HEA batched vvag (default); brickwall: n=28 Haar brick wall; "
                          "qaoa: 512 uneven QAOA circuits in one persistent launch per sweep; "
                          "warmstart: learned warm start for n=16 TFIM chains")
+    ap.add_argument("--batch", type=int, default=BATCH,
+                    help="hea: parameter vectors per step (64 is the configured workload; smaller "
+                         "batches are for profiler captures)")
     ap.add_argument("--instances", type=int, default=20000, help="warmstart: training chains")
     ap.add_argument("--held-out", type=int, default=1000, help="warmstart: held-out chains")
     ap.add_argument("--epochs", type=int, default=200, help="warmstart: network training epochs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
+    BATCH = args.batch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
