@@ -305,8 +305,9 @@ int tcg_adam_update(float* p, const float* g, float* m, float* v, int64_t n, flo
 /* Diagnostics (no reference counterpart): host pointers to a plan's pass
  * program so tests can replay its index arithmetic on the CPU.  which = 0
  * forward, 1 adjoint, 2 the measurement program of an mplan (pass the
- * mplan as `plan`).  arrays[0..4] = passes, stages, ops, slot_out, runs;
- * counts[0..4] their lengths; sizes[0..4] the element sizes in bytes. */
+ * mplan as `plan`).  arrays[0..5] = passes, stages, ops, slot_out, runs,
+ * Z-rotation run entries; counts[0..5] their lengths; sizes[0..5] the
+ * element sizes in bytes (all three arrays hold 6 elements). */
 int tcg_debug_program(const void* plan, int32_t which, const void** arrays,
                       int64_t* counts, int64_t* sizes);
 

@@ -142,6 +142,11 @@ class DevOp(ctypes.Structure):
                 ("slot", ctypes.c_int32), ("mat_off", ctypes.c_int64), ("grad_off", ctypes.c_int64)]
 
 
+class ZEnt(ctypes.Structure):
+    _fields_ = [("zmask", ctypes.c_uint32), ("zreg", ctypes.c_int32), ("slot", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("mat_off", ctypes.c_int64), ("grad_off", ctypes.c_int64)]
+
+
 class SlotOut(ctypes.Structure):
     _fields_ = [("slot", ctypes.c_int32), ("pad", ctypes.c_int32), ("out_off", ctypes.c_int64)]
 
@@ -160,13 +165,13 @@ def jit_info(handle: Any, which: int, mode: int, what: int = 0, cap: int = 1 << 
 def debug_program(handle: Any, which: int) -> dict:
     """Copy of a plan's device program as lists of ctypes records."""
     lib = load()
-    arrs = (ctypes.c_void_p * 5)()
-    cnts = (ctypes.c_int64 * 5)()
-    szs = (ctypes.c_int64 * 5)()
+    arrs = (ctypes.c_void_p * 6)()
+    cnts = (ctypes.c_int64 * 6)()
+    szs = (ctypes.c_int64 * 6)()
     check(lib.tcg_debug_program(handle, which, arrs, cnts, szs), "debug_program")
     out = {}
     for i, (name, typ) in enumerate([("passes", DevPass), ("stages", DevStage), ("ops", DevOp),
-                                     ("slot_out", SlotOut), ("runs", ctypes.c_uint32)]):
+                                     ("slot_out", SlotOut), ("runs", ctypes.c_uint32), ("zents", ZEnt)]):
         if ctypes.sizeof(typ) != szs[i]:
             raise EngineError("record size mismatch for %s: %d vs %d" % (name, ctypes.sizeof(typ), szs[i]))
         if cnts[i] == 0:

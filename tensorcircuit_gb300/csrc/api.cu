@@ -476,16 +476,19 @@ int tcg_debug_program(const void* plan, int32_t which, const void** arrays, int6
   arrays[2] = p->ops.data();
   arrays[3] = p->slot_out.data();
   arrays[4] = p->runs.data();
+  arrays[5] = p->zents.data();
   counts[0] = (int64_t)p->passes.size();
   counts[1] = (int64_t)p->stages.size();
   counts[2] = (int64_t)p->ops.size();
   counts[3] = (int64_t)p->slot_out.size();
   counts[4] = (int64_t)p->runs.size();
+  counts[5] = (int64_t)p->zents.size();
   sizes[0] = sizeof(DevPass);
   sizes[1] = sizeof(DevStage);
   sizes[2] = sizeof(DevOp);
   sizes[3] = sizeof(SlotOut);
   sizes[4] = sizeof(uint32_t);
+  sizes[5] = sizeof(ZEnt);
   return TCG_OK;
 }
 

@@ -31,8 +31,22 @@ enum OpKind : int32_t {
   OP_DENSEK = 3,   // k-qubit dense on tile bits tb[0..k-1], run on the smem tile
   OP_EXPECT = 4,   // Pauli term: acc += conj(psi[a]) s(a) psi[a ^ x]
   OP_PACC = 5,     // Pauli term: mu[a] += c s(a) psi[a ^ x]
-  OP_PROT = 6      // Pauli rotation cos(phi) I - i sin(phi) P (X/Y bits in
+  OP_PROT = 6,     // Pauli rotation cos(phi) I - i sin(phi) P (X/Y bits in
                    // registers: xreg; Z/Y global mask: zmask; nY)
+  OP_ZRUN = 7      // run of k commuting Z-string rotations, entries
+                   // zents[mat_off .. mat_off + k), applied as one phase
+};
+
+// One rotation of an OP_ZRUN run: exp(-i phi Z_S) with e^{i phi} at
+// mats[mat_off]; zreg = register positions of the Z bits (the phase class),
+// zmask = all Z bits (global).
+struct ZEnt {
+  uint32_t zmask;
+  int32_t zreg;
+  int32_t slot;      // gradient slot, -1 = none
+  int32_t pad;
+  int64_t mat_off;
+  int64_t grad_off;
 };
 
 // One device op, 48 bytes.
@@ -87,6 +101,7 @@ struct ProgramView {
   const uint32_t* runs;   // run tables
   const int64_t* entries; // distinct accumulator outputs, for the final reduce
   int64_t nentries;
+  const ZEnt* zents;      // entries of OP_ZRUN runs
 };
 
 }  // namespace tcg

@@ -204,6 +204,10 @@ class Gen {
 
   std::string reduce(int E, const char* arr) const {
     std::ostringstream o;
+    if (NL_ < 32) {  // one partial warp: a butterfly per entry, lane 0 writes
+      o << " small_reduce<" << E << ", " << NL_ << ">(" << arr << ", lane, sms + op.slot);";
+      return o.str();
+    }
     o << " { int ent; const float2 t = warp_reduce<" << E << ", " << NL_ << ">(" << arr
       << ", lane, ent); if (ent >= 0) sms[warp * " << MS_ << " + op.slot + ent] = t; }";
     return o.str();
@@ -308,6 +312,56 @@ class Gen {
         b << "float g = 0.f; prot_bwd<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ", "
           << (G ? "true" : "false") << ">(v, w, cs.x, cs.y, sg, g);";
         if (G) b << " float2 a1[1] = {make_float2(g, 0.f)};" << reduce(1, "a1");
+      }
+    } else if (op.kind == OP_ZRUN) {
+      // entries are literals: each run is its own body
+      b << "float2 ph[" << NR_ << "];\n#pragma unroll\n for (int c = 0; c < " << NR_
+        << "; ++c) ph[c] = make_float2(1.f, 0.f);";
+      std::vector<const ZEnt*> grads;
+      for (int e = 0; e < op.k; ++e) {
+        const ZEnt& z = P_.zents[op.mat_off + e];
+        b << " ph[" << z.zreg << "] = cmul(ph[" << z.zreg << "], zrun_factor(Mt + " << z.mat_off << "ll, gthr, "
+          << z.zmask << "u));";
+        if (z.slot >= 0) grads.push_back(&z);
+      }
+      b << " mul_walsh<" << NR_ << ">(ph);";
+      if (fwd()) {
+        b << " zrun_apply<" << NR_ << ">(v, ph);";
+      } else {
+        if (!grads.empty()) {
+          // gradient pairs (g_{2i}, g_{2i+1}) of consecutive slots
+          const int KG = (int)grads.size();
+          int E2 = 1;
+          while (E2 < (KG + 1) / 2) E2 <<= 1;
+          b << " { float t[" << NR_ << "]; zrun_grad<" << NR_ << ">(v, w, t); float2 g[" << E2 << "];";
+          for (int i = 0; i < E2; ++i) {
+            std::string xs = "0.f", ys = "0.f";
+            for (int h = 0; h < 2; ++h) {
+              const int k = 2 * i + h;
+              if (k >= KG) continue;
+              std::ostringstream s;
+              s << "((__popc(gthr & " << grads[k]->zmask << "u) & 1u) ? -t[" << grads[k]->zreg << "] : t["
+                << grads[k]->zreg << "])";
+              (h == 0 ? xs : ys) = s.str();
+            }
+            b << " g[" << i << "] = make_float2(" << xs << ", " << ys << ");";
+          }
+          if (NL_ < 32) {
+            b << " float2 red[" << E2 << "]; small_reduce<" << E2 << ", " << NL_
+              << ">(g, lane, red); if (lane == 0) { ";
+            for (int k = 0; k < KG; ++k)
+              b << "sms[op.slot + " << k << "] = make_float2(red[" << k / 2 << "]." << (k % 2 ? "y" : "x")
+                << ", 0.f); ";
+            b << "}";
+          } else {
+            b << " int ent; const float2 s = warp_reduce<" << E2 << ", " << NL_
+              << ">(g, lane, ent); if (ent >= 0) { sms[warp * " << MS_
+              << " + op.slot + 2 * ent] = make_float2(s.x, 0.f); if (2 * ent + 1 < " << KG << ") sms[warp * "
+              << MS_ << " + op.slot + 2 * ent + 1] = make_float2(s.y, 0.f); }";
+          }
+          b << " }";
+        }
+        b << " zrun_unapply<" << NR_ << ">(v, w, ph);";
       }
     } else if (op.kind == OP_EXPECT) {
       int zr = 0;

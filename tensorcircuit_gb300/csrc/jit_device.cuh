@@ -405,6 +405,80 @@ __device__ __forceinline__ void prot_bwd(float2 (&v)[NR], float2 (&w)[NR], float
   prot<NR, X, ZR, NY>(w, c, s, sgn, true);
 }
 
+// ------------------------------------------------- runs of Z-string rotations
+// ph[c] holds the product of the run's entries of register class c (entry
+// factor e^{-i phi} when the thread's part of the parity is even, e^{+i phi}
+// when odd); the multiplicative Walsh-Hadamard transform turns it into the
+// phase of every register: ph[r] = prod_c (popc(r & c) even ? A_c : conj(A_c)).
+template <int NR>
+__device__ __forceinline__ void mul_walsh(float2 (&a)[NR]) {
+#pragma unroll
+  for (int j = 1; j < NR; j <<= 1)
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+      if (!(c & j)) {
+        const float2 x = a[c], y = a[c | j];
+        a[c] = cmul(x, y);
+        a[c | j] = cmul(x, cconj(y));
+      }
+}
+template <int NR>
+__device__ __forceinline__ void add_walsh(float (&a)[NR]) {
+#pragma unroll
+  for (int j = 1; j < NR; j <<= 1)
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+      if (!(c & j)) {
+        const float x = a[c], y = a[c | j];
+        a[c] = x + y;
+        a[c | j] = x - y;
+      }
+}
+// entry factor of a run: e^{i phi} at m, conjugated for an even thread parity
+__device__ __forceinline__ float2 zrun_factor(const float2* m, u32 gthr, u32 zm) {
+  const float2 u = ld(m);
+  return (__popc(gthr & zm) & 1u) ? u : cconj(u);
+}
+template <int NR>
+__device__ __forceinline__ void zrun_apply(float2 (&v)[NR], const float2 (&ph)[NR]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) v[r] = cmul(ph[r], v[r]);
+}
+template <int NR>
+__device__ __forceinline__ void zrun_unapply(float2 (&v)[NR], float2 (&w)[NR], const float2 (&ph)[NR]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const float2 c = cconj(ph[r]);
+    v[r] = cmul(c, v[r]);
+    w[r] = cmul(c, w[r]);
+  }
+}
+// t[c] = sum_r (-1)^{popc(r & c)} Im(conj(w_r) v_r)
+template <int NR>
+__device__ __forceinline__ void zrun_grad(const float2 (&v)[NR], const float2 (&w)[NR], float (&t)[NR]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) t[r] = fmaf(w[r].x, v[r].y, -w[r].y * v[r].x);
+  add_walsh<NR>(t);
+}
+// Butterfly sum of E values over the NL (< 32) lanes of a small block; lane 0
+// writes value e to out[e].
+template <int E, int NL>
+__device__ __forceinline__ void small_reduce(const float2 (&a)[E], int lane, float2* out) {
+  constexpr unsigned FULL = NL >= 32 ? 0xffffffffu : ((1u << NL) - 1u);
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    float2 x = a[e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      if (o < NL) {
+        x.x += __shfl_xor_sync(FULL, x.x, o);
+        x.y += __shfl_xor_sync(FULL, x.y, o);
+      }
+    }
+    if (lane == 0) out[e] = x;
+  }
+}
+
 // ----------------------------------------------------------------- reductions
 // Sum E complex values (E a power of two <= 16) over the NL lanes of a warp.
 // Returns this lane's total and sets `entry` to the entry it holds, or -1 if

@@ -402,6 +402,53 @@ __device__ void dispatch_denseK(int k, float2* tile, int L, const int* tb, const
   }
 }
 
+// ------------------------------------------------- runs of Z-string rotations
+// A run of commuting rotations exp(-i phi_e Z_{S_e}) multiplies amplitude x
+// by prod_e e^{-i phi_e s_e(x)}, s_e = (-1)^{parity(x & S_e)}.  Per thread the
+// parity splits into a thread part and a register part popc(r & c_e), c_e the
+// entry's register mask ("class").  Folding each entry into its class,
+// A_c = prod_{c_e = c} B_e, the phase of register r is
+// prod_c (popc(r & c) even ? A_c : conj(A_c)): a multiplicative Walsh-Hadamard
+// transform of A, computed with 2^R * R complex products per thread.
+template <int R>
+__device__ __forceinline__ void class_mul(float2 (&a)[1 << R], int c, float2 u) {
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i)
+    if (i == c) a[i] = cmul(a[i], u);
+}
+template <int R>
+__device__ __forceinline__ void mul_walsh(float2 (&a)[1 << R]) {
+#pragma unroll
+  for (int j = 0; j < R; ++j)
+#pragma unroll
+    for (int c = 0; c < (1 << R); ++c)
+      if (!((c >> j) & 1)) {
+        const float2 x = a[c], y = a[c | (1 << j)];
+        a[c] = cmul(x, y);
+        a[c | (1 << j)] = cmul(x, cconj(y));
+      }
+}
+template <int R>
+__device__ __forceinline__ void add_walsh(float (&a)[1 << R]) {
+#pragma unroll
+  for (int j = 0; j < R; ++j)
+#pragma unroll
+    for (int c = 0; c < (1 << R); ++c)
+      if (!((c >> j) & 1)) {
+        const float x = a[c], y = a[c | (1 << j)];
+        a[c] = x + y;
+        a[c | (1 << j)] = x - y;
+      }
+}
+template <int R>
+__device__ __forceinline__ float class_pick(const float (&a)[1 << R], int c) {
+  float r = 0.f;
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i)
+    if (i == c) r = a[i];
+  return r;
+}
+
 // ------------------------------------------------------------------ tile I/O
 __device__ __forceinline__ void tile_load_smem(float2* sm, const float2* __restrict__ src, uint32_t base,
                                                const uint32_t* runs, int L, int tid, int nthreads) {
@@ -739,6 +786,45 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
           const float2 mq = make_float2(-q.x, -q.y);
           dispatch_prot<R>(op.xreg, v, cs.x, mq, zr);
           dispatch_prot<R>(op.xreg, w, cs.x, mq, zr);
+        }
+      } else if (kind == OP_ZRUN) {
+        if (MODE == MODE_FWD || MODE == MODE_BWD) {
+          float2 ph[NR];
+#pragma unroll
+          for (int c = 0; c < NR; ++c) ph[c] = make_float2(1.f, 0.f);
+          for (int e = 0; e < op.k; ++e) {
+            const ZEnt ze = A.prog.zents[op.mat_off + e];
+            float2 u = ldm(mats + ze.mat_off);  // e^{i phi}; parity 0 takes e^{-i phi}
+            if (!(__popc(gthr & ze.zmask) & 1)) u = cconj(u);
+            class_mul<R>(ph, ze.zreg, u);
+          }
+          mul_walsh<R>(ph);
+          if (MODE == MODE_FWD) {
+#pragma unroll
+            for (int r = 0; r < NR; ++r) v[r] = cmul(ph[r], v[r]);
+          } else {
+            if (op.slot >= 0) {
+              // dL/dphi_e = sum_x s_e(x) Im(conj(mu_x) psi_x) at the run's output
+              float t[NR];
+#pragma unroll
+              for (int r = 0; r < NR; ++r) t[r] = fmaf(w[r].x, v[r].y, -w[r].y * v[r].x);
+              add_walsh<R>(t);
+              for (int e = 0; e < op.k; ++e) {
+                const ZEnt ze = A.prog.zents[op.mat_off + e];
+                if (ze.slot < 0) continue;
+                float g = class_pick<R>(t, ze.zreg);
+                if (__popc(gthr & ze.zmask) & 1) g = -g;
+                const float2 s = warp_sum(make_float2(g, 0.f), nl);
+                if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = s;
+              }
+            }
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+              const float2 c = cconj(ph[r]);
+              v[r] = cmul(c, v[r]);
+              w[r] = cmul(c, w[r]);
+            }
+          }
         }
       } else if (kind == OP_EXPECT) {
         // sign bits: fixed part parity and register bits inside zmask

@@ -20,6 +20,10 @@ namespace {
 
 inline int popc64(uint64_t v) { return __builtin_popcountll(v); }
 
+// longest OP_ZRUN (its gradients are reduced as 16 float pairs in one
+// transposed warp reduction by the specialised kernels)
+constexpr int kZRunMax = 32;
+
 uint64_t gate_mask(const PGate& g) {
   uint64_t m = 0;
   for (int i = 0; i < g.k; ++i) m |= 1ull << g.gbits[i];
@@ -127,8 +131,59 @@ int emit_stage(Program* P, DevPass& dp, const StageDraft& sd,
   for (int i = 0; i < 32; ++i) regpos_of_tile[i] = -1;
   for (int i = 0; i < R; ++i) regpos_of_tile[st.reg_tile[i]] = i;
   int slot = 0;
-  for (int oi : sd.ops) {
+  for (size_t si = 0; si < sd.ops.size(); ++si) {
+    const int oi = sd.ops[si];
     const OpDraft& o = od[oi];
+    // a run of >= 2 consecutive Z-string rotations (no X/Y factor) becomes
+    // one OP_ZRUN: they commute, so their product is one phase per amplitude
+    if (o.kind == TCG_GATE_PAULI_ROT && o.x == 0) {
+      size_t sj = si;
+      while (sj < sd.ops.size() && sj - si < (size_t)kZRunMax) {
+        const OpDraft& q = od[sd.ops[sj]];
+        if (q.kind != TCG_GATE_PAULI_ROT || q.x != 0) break;
+        ++sj;
+      }
+      if (sj - si >= 2) {
+        DevOp d;
+        std::memset(&d, 0, sizeof(d));
+        d.kind = OP_ZRUN;
+        d.k = (int)(sj - si);
+        d.mat_off = (int64_t)P->zents.size();
+        d.grad_off = -1;
+        d.slot = -1;
+        for (size_t t = si; t < sj; ++t) {
+          const OpDraft& q = od[sd.ops[t]];
+          ZEnt z;
+          std::memset(&z, 0, sizeof(z));
+          z.zmask = (uint32_t)q.z;
+          int zr = 0;
+          for (int b = 0; b < 64; ++b)
+            if (q.z >> b & 1) {
+              const int tb = tile_of_gbit[b];
+              const int rp = tb >= 0 ? regpos_of_tile[tb] : -1;
+              if (rp >= 0) zr |= 1 << rp;
+            }
+          z.zreg = zr;
+          z.mat_off = q.mat_off;
+          z.grad_off = q.grad_off;
+          z.slot = -1;
+          if (q.grad_off >= 0) {
+            if (d.slot < 0) d.slot = slot;
+            z.slot = slot;
+            SlotOut so;
+            so.slot = slot;
+            so.pad = 0;
+            so.out_off = q.grad_off;
+            P->slot_out.push_back(so);
+            slot += 1;
+          }
+          P->zents.push_back(z);
+        }
+        P->ops.push_back(d);
+        si = sj - 1;
+        continue;
+      }
+    }
     DevOp d;
     std::memset(&d, 0, sizeof(d));
     d.slot = -1;
@@ -501,7 +556,8 @@ int program_device_view(Program* p, ProgramView* view) {
   size_t o_so = al(o_op + p->ops.size() * sizeof(DevOp));
   size_t o_runs = al(o_so + p->slot_out.size() * sizeof(SlotOut));
   size_t o_ent = al(o_runs + p->runs.size() * sizeof(uint32_t));
-  size_t total = al(o_ent + p->entries.size() * sizeof(int64_t)) + 256;
+  size_t o_z = al(o_ent + p->entries.size() * sizeof(int64_t));
+  size_t total = al(o_z + p->zents.size() * sizeof(ZEnt)) + 256;
   std::vector<char> host(total, 0);
   if (!p->passes.empty()) std::memcpy(host.data() + o_pass, p->passes.data(), p->passes.size() * sizeof(DevPass));
   if (!p->stages.empty()) std::memcpy(host.data() + o_stage, p->stages.data(), p->stages.size() * sizeof(DevStage));
@@ -509,6 +565,7 @@ int program_device_view(Program* p, ProgramView* view) {
   if (!p->slot_out.empty()) std::memcpy(host.data() + o_so, p->slot_out.data(), p->slot_out.size() * sizeof(SlotOut));
   if (!p->runs.empty()) std::memcpy(host.data() + o_runs, p->runs.data(), p->runs.size() * sizeof(uint32_t));
   if (!p->entries.empty()) std::memcpy(host.data() + o_ent, p->entries.data(), p->entries.size() * sizeof(int64_t));
+  if (!p->zents.empty()) std::memcpy(host.data() + o_z, p->zents.data(), p->zents.size() * sizeof(ZEnt));
   void* d = nullptr;
   if (cudaMalloc(&d, total) != cudaSuccess) return TCG_ERR_OOM;
   if (cudaMemcpy(d, host.data(), total, cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -525,6 +582,7 @@ int program_device_view(Program* p, ProgramView* view) {
   c.view.runs = (const uint32_t*)(b + o_runs);
   c.view.entries = (const int64_t*)(b + o_ent);
   c.view.nentries = (int64_t)p->entries.size();
+  c.view.zents = (const ZEnt*)(b + o_z);
   p->dev[dev] = c;
   *view = c.view;
   return TCG_OK;

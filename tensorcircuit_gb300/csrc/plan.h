@@ -26,6 +26,7 @@ struct Program {
   std::vector<SlotOut> slot_out;
   std::vector<uint32_t> runs;
   std::vector<int64_t> entries;  // distinct accumulator outputs (sorted)
+  std::vector<ZEnt> zents;       // OP_ZRUN entries
   int max_slots = 0;         // largest stage slot count
   int64_t nout = 0;          // per-circuit accumulator outputs (complex entries)
 

@@ -266,12 +266,13 @@ def study(n_train: int, n_test: int, steps: int = 300, gen_steps: int = 300, epo
     s_w = steps_to(rel_w, level)
     s_r = steps_to(rel_r, level)
     gen_e0 = free_fermion_e0(Jtr, htr)
+    checkpoints = sorted({k for k in (0, 10, 50, 100, 200, steps) if k <= steps})
     return {
         "n_train": n_train, "n_test": n_test, "steps": steps, "gen_steps": gen_steps, "epochs": epochs,
         "train_rel_err_median": float(np.median(np.abs((hist_tr[-1] - gen_e0) / gen_e0))),
         "fit_loss_first_last": [losses[0], losses[-1]],
-        "rel_err_median_warm": {str(k): float(np.median(rel_w[k])) for k in (0, 10, 50, 100, steps)},
-        "rel_err_median_random": {str(k): float(np.median(rel_r[k])) for k in (0, 10, 50, 100, steps)},
+        "rel_err_median_warm": {str(k): float(np.median(rel_w[k])) for k in checkpoints},
+        "rel_err_median_random": {str(k): float(np.median(rel_r[k])) for k in checkpoints},
         "target_level": level,
         "steps_to_target_median_warm": float(np.median(s_w)),
         "steps_to_target_median_random": float(np.median(s_r)),

@@ -10,7 +10,7 @@ tiles, in-range global offsets -- before anything runs on a GPU.
 
 import numpy as np
 
-OP_DENSE1, OP_DENSE2, OP_DIAG, OP_DENSEK, OP_EXPECT, OP_PACC, OP_PROT = 0, 1, 2, 3, 4, 5, 6
+OP_DENSE1, OP_DENSE2, OP_DIAG, OP_DENSEK, OP_EXPECT, OP_PACC, OP_PROT, OP_ZRUN = 0, 1, 2, 3, 4, 5, 6, 7
 
 
 def dep(v, bits):
@@ -158,6 +158,22 @@ class Replay:
         sgn = 1 - 2 * (_popc(src & op.zmask) & 1)
         return (1j ** (op.nY % 4)) * sgn * V[:, r ^ X]
 
+    def _zrun_signs(self, op, G, R):
+        """(entry, s_e[thread, r]) with s_e = (-1)^parity, the parity split as
+        the kernels split it: thread part from the global index of register 0
+        plus popc(r & zreg)."""
+        zs = self.prog["zents"][op.mat_off:op.mat_off + op.k]
+        r = np.arange(1 << R)
+        out = []
+        for z in zs:
+            pt = _popc(G[:, 0] & z.zmask) & 1
+            pr = _popc(r & z.zreg) & 1
+            # the register mask must match the Z bits among the register bits
+            want = _popc((G[:, [1 << i for i in range(R)]] ^ G[:, [0]]) & z.zmask)
+            assert np.all((want > 0) == ((z.zreg >> np.arange(R)) & 1)[None, :].astype(bool))
+            out.append((z, 1 - 2 * ((pt[:, None] ^ pr[None, :]) & 1)))
+        return out
+
     @staticmethod
     def _mat(op, mats, dim):
         return np.asarray(mats[op.mat_off:op.mat_off + dim * dim], dtype=np.complex128).reshape(dim, dim)
@@ -208,6 +224,10 @@ class Replay:
             if adj:
                 s = -s
             V = c * V - 1j * s * self._pauli(V, op, G, R)
+        elif op.kind == OP_ZRUN:
+            for z, sg in self._zrun_signs(op, G, R):
+                phi = np.angle(complex(mats[z.mat_off]))
+                V = V * np.exp((1j if adj else -1j) * phi * sg)
         else:
             raise AssertionError("unexpected op kind %d" % op.kind)
         return V
@@ -250,6 +270,13 @@ class Replay:
                 for e in range(1 << k):
                     grads[op.grad_off + e] += np.sum(g[idx == e])
             W = W * d[idx]
+        elif op.kind == OP_ZRUN:
+            # the run's rotations commute: dL/dphi_e = Im <mu| Z_e |psi> at the run output
+            for z, sg in self._zrun_signs(op, G, R):
+                if z.slot >= 0:
+                    grads[z.grad_off] += np.sum(sg * np.imag(np.conj(W) * V))
+            V = self._apply(V, op, mats, G, R, adj=True)
+            W = self._apply(W, op, mats, G, R, adj=True)
         elif op.kind == OP_PROT:
             # dG/dphi = -i P G, so dL/dphi = Im <mu| P |psi_out>
             if op.slot >= 0:

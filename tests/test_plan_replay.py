@@ -209,3 +209,37 @@ def test_pauli_rotation_exp1_forms_replay():
     psi0 = np.zeros(1 << n, np.complex128)
     psi0[0] = 1
     np.testing.assert_allclose(Replay(prog, n).forward(psi0, mats), sv.run_circuit(n, gl), atol=2e-6)
+
+
+@pytest.mark.parametrize("n,nl", [(8, 2), (10, 3)])
+def test_zrun_hea_replay_forward_backward(n, nl):
+    """The HEA's rzz layers become runs of commuting Z rotations (one
+    phase per amplitude); replayed forward states and adjoint cotangents
+    match the oracle."""
+    rng = np.random.default_rng(n)
+    params = rng.uniform(0, 2 * np.pi, templates.hea_nparams(n, nl))
+    gl = templates.hea_gate_list(n, nl, params)
+    c, entry, mats, n_eng = build_host(n, gl)
+    for which in (0, 1):
+        prog = nat.debug_program(entry.plan.handle, which)
+        kinds = [op.kind for op in prog["ops"]]
+        assert 7 in kinds and len(prog["zents"]) >= n - 1
+    prog = nat.debug_program(entry.plan.handle, 0)
+    psi0 = np.zeros(1 << n, np.complex128)
+    psi0[0] = 1
+    np.testing.assert_allclose(Replay(prog, n).forward(psi0, mats), sv.run_circuit(n, gl), atol=2e-6)
+    psi_out = sv.run_circuit(n, gl)
+    mu_out = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    prog_b = nat.debug_program(entry.plan.handle, 1)
+    psi_in, mu_in, grads = Replay(prog_b, n).backward(psi_out, mu_out, mats, max(1, mats.size))
+    want_cot, want_mu = oracle_cotangents(n, gl, mu_out)
+    np.testing.assert_allclose(mu_in, want_mu, atol=1e-4)
+    for gi, g in enumerate(entry.gates_c):
+        kind, qubits, mat_off, grad_off = g[:4]
+        z = complex(mats[mat_off])
+        pm = np.ones((1, 1), np.complex128)
+        for code in g[4]:
+            pm = np.kron(pm, sv.gate_matrix("ixyz"[code]))
+        dg = -z.imag * np.eye(pm.shape[0]) - 1j * z.real * pm
+        want = np.sum(np.conj(want_cot[gi]) * dg).real
+        np.testing.assert_allclose(grads[grad_off].real, want, atol=1e-3, rtol=1e-4)
