@@ -633,8 +633,10 @@ def run_warmstart(args, rank, world):
 
 
 def main():
-    global BATCH
+    global BATCH, BW_N
     ap = argparse.ArgumentParser()
+    ap.add_argument("--bw-qubits", type=int, default=BW_N,
+                    help="brickwall: qubits (28 is the configured workload; fewer for profiler captures)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -652,6 +654,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     BATCH = args.batch
+    BW_N = args.bw_qubits
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -13,7 +13,7 @@ Usage mirrors the reference::
 
 __version__ = "0.1.0"
 
-from . import gates, quantum
+from . import gates, interfaces, quantum, torchnn
 from .backends import backend
 from .circuit import Circuit
 from .cons import (

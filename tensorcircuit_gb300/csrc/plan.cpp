@@ -436,6 +436,54 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
     std::vector<OpDraft> none;
     return emit_pass(&P, n, L, R, S, none, max_slots);
   }
+  auto need_of = [&](const PGate& g) -> uint64_t {
+    return (g.kind == TCG_GATE_DENSE) ? gate_mask(g) : (g.kind == TCG_GATE_PAULI_ROT) ? g.xmask : 0;
+  };
+  // gates of `rem` a pass with the fixed local set S can run, in order
+  // (a gate that cannot run blocks every later gate on its qubits)
+  auto take_fixed = [&](uint64_t S, std::vector<int>* taken, std::vector<int>* left) {
+    uint64_t blocked = 0;
+    for (int gi : rem) {
+      const PGate& g = gates[gi];
+      const uint64_t bits = gate_mask(g);
+      if ((bits & blocked) || (need_of(g) & ~S)) {
+        blocked |= bits;
+        if (left) left->push_back(gi);
+      } else if (taken) {
+        taken->push_back(gi);
+      }
+    }
+  };
+  auto count_fixed = [&](uint64_t S) -> int {
+    uint64_t blocked = 0;
+    int c = 0;
+    for (int gi : rem) {
+      const PGate& g = gates[gi];
+      const uint64_t bits = gate_mask(g);
+      if ((bits & blocked) || (need_of(g) & ~S)) blocked |= bits;
+      else ++c;
+    }
+    return c;
+  };
+  // window candidates: the low bits plus L - lo free bits made of one or two
+  // runs of consecutive index bits (a brick wall's light cone is a window)
+  std::vector<uint64_t> windows;
+  {
+    const int w = L - lo;
+    const uint64_t base = (lo >= 64) ? ~0ull : ((1ull << lo) - 1);
+    auto run = [](int a, int len) -> uint64_t {
+      uint64_t m = 0;
+      for (int b = a; b < a + len; ++b) m |= 1ull << b;
+      return m;
+    };
+    if (n > L && w > 0) {
+      for (int a = lo; a + w <= n; ++a) windows.push_back(base | run(a, w));
+      for (int w1 = 1; w1 < w; ++w1)
+        for (int a = lo; a + w1 <= n; ++a)
+          for (int b2 = a + w1 + 1; b2 + (w - w1) <= n; ++b2)
+            windows.push_back(base | run(a, w1) | run(b2, w - w1));
+    }
+  }
   while (!rem.empty()) {
     uint64_t S = (lo >= 64) ? ~0ull : ((1ull << lo) - 1);
     uint64_t blocked = 0;
@@ -448,8 +496,7 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
         left.push_back(gi);
         continue;
       }
-      uint64_t need = (g.kind == TCG_GATE_DENSE) ? (bits & ~S)
-                    : (g.kind == TCG_GATE_PAULI_ROT) ? (g.xmask & ~S) : 0;
+      uint64_t need = need_of(g) & ~S;
       if (popc64(S | need) <= L) {
         S |= need;
         taken.push_back(gi);
@@ -459,6 +506,29 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
       }
     }
     if (taken.empty()) return TCG_ERR_INVALID_ARG;  // cannot happen: L >= lo + 6
+    // a fixed window that runs more gates than the in-order greedy choice wins
+    {
+      int best = (int)taken.size();
+      uint64_t bestS = 0;
+      // bounded planning work: two-run windows only while they stay cheap
+      const int single = std::max(0, n - (L - lo) - lo + 1);
+      const size_t nw = (windows.size() * rem.size() > 2000000) ? std::min<size_t>(single, windows.size())
+                                                                  : windows.size();
+      for (size_t wi = 0; wi < nw; ++wi) {
+        const uint64_t Wm = windows[wi];
+        const int c = count_fixed(Wm);
+        if (c > best) {
+          best = c;
+          bestS = Wm;
+        }
+      }
+      if (bestS) {
+        S = bestS;
+        taken.clear();
+        left.clear();
+        take_fixed(S, &taken, &left);
+      }
+    }
     // pad S to L bits: prefer bits the next gates need
     for (int gi : left) {
       if (popc64(S) >= L) break;
