@@ -354,8 +354,10 @@ class Gen {
                 << ", 0.f); ";
             b << "}";
           } else {
+            // padding pairs (entries >= KG) hold zeros and must not be
+            // written: their slots belong to other ops or other warps
             b << " int ent; const float2 s = warp_reduce<" << E2 << ", " << NL_
-              << ">(g, lane, ent); if (ent >= 0) { sms[warp * " << MS_
+              << ">(g, lane, ent); if (ent >= 0 && 2 * ent < " << KG << ") { sms[warp * " << MS_
               << " + op.slot + 2 * ent] = make_float2(s.x, 0.f); if (2 * ent + 1 < " << KG << ") sms[warp * "
               << MS_ << " + op.slot + 2 * ent + 1] = make_float2(s.y, 0.f); }";
           }
