@@ -111,6 +111,7 @@ struct tcg_ubatch {
   void* dtab = nullptr;
   const BatchCirc* circ[4] = {nullptr, nullptr, nullptr, nullptr};
   const BatchSeg* segs[4] = {nullptr, nullptr, nullptr, nullptr};
+  const int32_t* coarse[4] = {nullptr, nullptr, nullptr, nullptr};
   const int64_t* d_pidx = nullptr;
   const float* d_scale = nullptr;
   const float2* d_cval = nullptr;
@@ -320,6 +321,7 @@ int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int
 
   // ---- segments: pass-major, larger circuits first within a pass
   std::vector<BatchSeg> hs[4];
+  std::vector<int32_t> hcoarse[4];
   const int modes[4] = {MODE_FWD, MODE_BWD, MODE_MEAS, MODE_PACC};
   std::vector<int> order(C);
   for (int c = 0; c < C; ++c) order[c] = c;
@@ -354,6 +356,17 @@ int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int
     B->nitems[mode] = item;
     B->nsegs[mode] = (int)hs[mode].size();
     if (hs[mode].empty()) hs[mode].push_back(BatchSeg{0, 0, 0, 0, 0});
+    // coarse index: segment holding item k * kBatchCoarse (clamped to the last item)
+    {
+      const int64_t nk = item / kBatchCoarse + 2;
+      hcoarse[mode].resize((size_t)nk);
+      size_t sgi = 0;
+      for (int64_t k = 0; k < nk; ++k) {
+        const int64_t it = std::min<int64_t>(k * kBatchCoarse, std::max<int64_t>(item - 1, 0));
+        while (sgi + 1 < hs[mode].size() && hs[mode][sgi + 1].item0 <= it) ++sgi;
+        hcoarse[mode][(size_t)k] = (int32_t)sgi;
+      }
+    }
   }
 
   // ---- program views and one device table allocation
@@ -372,12 +385,14 @@ int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int
     hc[MODE_PACC][c].prog = vt;
   }
   size_t off = 0;
-  size_t o_circ[4], o_seg[4];
+  size_t o_circ[4], o_seg[4], o_coarse[4];
   for (int m = 0; m < 4; ++m) {
     o_circ[m] = off;
     off = al256(off + hc[m].size() * sizeof(BatchCirc));
     o_seg[m] = off;
     off = al256(off + hs[m].size() * sizeof(BatchSeg));
+    o_coarse[m] = off;
+    off = al256(off + hcoarse[m].size() * sizeof(int32_t));
   }
   const size_t o_pidx = off;
   off = al256(off + pidx.size() * sizeof(int64_t));
@@ -404,6 +419,7 @@ int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int
   for (int m = 0; m < 4; ++m) {
     put(o_circ[m], hc[m].data(), hc[m].size() * sizeof(BatchCirc));
     put(o_seg[m], hs[m].data(), hs[m].size() * sizeof(BatchSeg));
+    put(o_coarse[m], hcoarse[m].data(), hcoarse[m].size() * sizeof(int32_t));
   }
   put(o_pidx, pidx.data(), pidx.size() * sizeof(int64_t));
   put(o_scale, scale.data(), scale.size() * sizeof(float));
@@ -427,6 +443,7 @@ int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int
   for (int m = 0; m < 4; ++m) {
     B->circ[m] = reinterpret_cast<const BatchCirc*>(d + o_circ[m]);
     B->segs[m] = reinterpret_cast<const BatchSeg*>(d + o_seg[m]);
+    B->coarse[m] = reinterpret_cast<const int32_t*>(d + o_coarse[m]);
   }
   B->d_pidx = reinterpret_cast<const int64_t*>(d + o_pidx);
   B->d_scale = reinterpret_cast<const float*>(d + o_scale);
@@ -519,6 +536,7 @@ int tcg_ubatch_value_and_grad(tcg_ubatch* batch, const float* params, float* ene
     std::memset(&bl, 0, sizeof(bl));
     bl.circ = B->circ[mode];
     bl.segs = B->segs[mode];
+    bl.coarse = B->coarse[mode];
     bl.nsegs = B->nsegs[mode];
     bl.nitems = B->nitems[mode];
     bl.psi = psi;

@@ -64,9 +64,13 @@ struct BatchSeg {
   uint32_t ntiles;
   uint32_t need;        // completed tiles of the circuit this segment waits for
 };
+constexpr int kBatchCoarse = 256;  // items per coarse segment-index entry
+constexpr int kBatchChunk = 4;     // items a CTA dequeues at once
+
 struct BatchLaunch {
   const BatchCirc* circ;
   const BatchSeg* segs;
+  const int32_t* coarse; // segment of item k * kBatchCoarse, k = 0 .. nitems / kBatchCoarse
   int32_t nsegs;
   int32_t pad;
   int64_t nitems;

@@ -915,18 +915,34 @@ __global__ void __launch_bounds__(256, 1) batch_kernel(BatchLaunch BL) {
   extern __shared__ __align__(16) float2 smem_raw[];
   __shared__ long long s_item;
   __shared__ int s_seg;
+  long long chunk_next = 0, chunk_end = 0;  // thread 0: rest of the dequeued chunk
+  int last_seg = 0;
   for (;;) {
     if (threadIdx.x == 0) {
-      const long long item = (long long)atomicAdd(BL.queue, 1u);
+      if (chunk_next >= chunk_end) {
+        chunk_next = (long long)atomicAdd(BL.queue, (unsigned)kBatchChunk);
+        chunk_end = chunk_next + kBatchChunk;
+        last_seg = -1;
+      }
+      const long long item = chunk_next++;
       int seg = -1;
       if (item < BL.nitems) {
-        int lo = 0, hi = BL.nsegs - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (BL.segs[mid].item0 <= item) lo = mid;
-          else hi = mid - 1;
+        if (last_seg >= 0) {
+          // items of a chunk are consecutive: step forward from the last one
+          seg = last_seg;
+          while (seg + 1 < BL.nsegs && BL.segs[seg + 1].item0 <= item) ++seg;
+        } else {
+          // the coarse index brackets the binary search to a few segments
+          const long long k = item / kBatchCoarse;
+          int lo = BL.coarse[k], hi = BL.coarse[k + 1];
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (BL.segs[mid].item0 <= item) lo = mid;
+            else hi = mid - 1;
+          }
+          seg = lo;
         }
-        seg = lo;
+        last_seg = seg;
         const unsigned need = BL.segs[seg].need;
         const unsigned* dn = BL.done + BL.segs[seg].circ;
         if (need > 0 && ld_acquire_u32(dn) < need && ld_acquire_u32(BL.err) == 0u) {
