@@ -611,19 +611,19 @@ def run_warmstart(args, rank, world):
     dev = torch.device("cuda", torch.cuda.current_device())
     l0 = lib.tcg_launch_count()
     with ClockSampler(dev.index) as clk:
-        r = ws.study(n_train=args.instances, n_test=args.held_out, steps=300, gen_steps=300,
+        r = ws.study(n_train=args.instances, n_test=args.held_out, steps=300, gen_steps=args.gen_steps,
                      epochs=args.epochs)
     launches = lib.tcg_launch_count() - l0
     if rank != 0:
         return
-    gen_evals = args.instances * 301
+    gen_evals = args.instances * (args.gen_steps + 1)
     line = {
         "metric": "warm-start Adam steps to the random start's 300-step error (ratio random / warm)",
         "value": r["step_ratio"], "unit": "x fewer steps", "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": 1e3 * sum(r["seconds"].values()), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 simulator / bf16 network activations", "data": "synthetic",
         "config": {"workload": "tfim_n16_hea6_warmstart", "train_chains": args.instances,
-                   "held_out": args.held_out, "epochs": args.epochs, "seed": 6},
+                   "held_out": args.held_out, "epochs": args.epochs, "gen_steps": args.gen_steps, "seed": 6},
         "study": r,
         "generation_throughput": {"value": gen_evals / r["seconds"]["generate"],
                                   "unit": "n=16 energy+gradient evaluations/s"},
@@ -648,9 +648,11 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="hea: parameter vectors per step (64 is the configured workload; smaller "
                          "batches are for profiler captures)")
-    ap.add_argument("--instances", type=int, default=20000, help="warmstart: training chains")
+    ap.add_argument("--instances", type=int, default=8192, help="warmstart: training chains")
     ap.add_argument("--held-out", type=int, default=1000, help="warmstart: held-out chains")
     ap.add_argument("--epochs", type=int, default=200, help="warmstart: network training epochs")
+    ap.add_argument("--gen-steps", type=int, default=1000,
+                    help="warmstart: Adam steps that produce each training chain's target angles")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     BATCH = args.batch

@@ -274,6 +274,11 @@ def study(n_train: int, n_test: int, steps: int = 300, gen_steps: int = 300, epo
         "rel_err_median_warm": {str(k): float(np.median(rel_w[k])) for k in checkpoints},
         "rel_err_median_random": {str(k): float(np.median(rel_r[k])) for k in checkpoints},
         "target_level": level,
+        # median steps to fixed relative-error levels (steps + 1 = not reached)
+        "steps_to_level_median": {
+            "%g" % lv: {"warm": float(np.median(steps_to(rel_w, lv))),
+                        "random": float(np.median(steps_to(rel_r, lv)))}
+            for lv in (0.1, 0.05, 0.03, 0.02, 1e-3)},
         "steps_to_target_median_warm": float(np.median(s_w)),
         "steps_to_target_median_random": float(np.median(s_r)),
         "step_ratio": float(np.median(s_r) / max(np.median(s_w), 1.0)),
