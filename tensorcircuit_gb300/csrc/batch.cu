@@ -106,6 +106,7 @@ struct tcg_ubatch {
   int64_t nitems[4] = {0, 0, 0, 0};
   int nsegs[4] = {0, 0, 0, 0};
   int64_t n_energy_tasks = 0, n_grad_tasks = 0;
+  bool lite = true;  // every program fits the lighter persistent body
 
   // device tables (one allocation)
   void* dtab = nullptr;
@@ -312,6 +313,17 @@ int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int
     B->param_total += U.nparams;
   }
   B->part_total = std::max(meas_part, bwd_part);
+  // the lighter kernel body covers 1-qubit dense gates, Pauli rotations,
+  // Z-rotation runs and Pauli terms in register stages
+  auto lite_ok = [](const Program& p) {
+    for (const DevStage& s : p.stages)
+      if (s.smem_stage) return false;
+    for (const DevOp& o : p.ops)
+      if (o.kind != OP_DENSE1 && o.kind != OP_PROT && o.kind != OP_ZRUN && o.kind != OP_EXPECT) return false;
+    return true;
+  };
+  for (int c = 0; c < C; ++c)
+    if (!lite_ok(B->plans[c]->fwd) || !lite_ok(B->plans[c]->bwd) || !lite_ok(*B->terms[c])) B->lite = false;
   B->n_energy_tasks = (int64_t)etasks.size();
   B->n_grad_tasks = (int64_t)gtasks.size();
   if (coef.empty()) coef.push_back(0.f);
@@ -548,7 +560,7 @@ int tcg_ubatch_value_and_grad(tcg_ubatch* batch, const float* params, float* ene
     bl.done = cnt + mode * cw + 1;
     bl.err = err;
     bl.sticky = sticky;
-    return rc_of(launch_batch(mode, bl, B->L, B->max_slots[mode], st));
+    return rc_of(launch_batch(mode, bl, B->L, B->max_slots[mode], B->lite, st));
   };
   auto reduce = [&](const RedTask* tasks, int64_t ntasks, const RedItem* items, float* out) -> int {
     if (ntasks == 0) return TCG_OK;

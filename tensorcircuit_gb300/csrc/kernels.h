@@ -86,7 +86,10 @@ struct BatchLaunch {
 };
 // L: tile bits shared by every program of the launch; max_slots: largest
 // stage slot count over the circuits.
-cudaError_t launch_batch(int mode, const BatchLaunch& bl, int L, int max_slots, cudaStream_t st);
+// lite: every program holds only 1-qubit dense gates, Pauli rotations,
+// Z-rotation runs and Pauli terms (no shared-memory stages, 2-qubit dense or
+// diagonal ops), which selects the smaller kernel body (two CTAs per SM).
+cudaError_t launch_batch(int mode, const BatchLaunch& bl, int L, int max_slots, bool lite, cudaStream_t st);
 
 // every kernel launch of the library increments this counter
 void count_launch(int64_t n = 1);

@@ -545,7 +545,10 @@ __device__ __forceinline__ bool same_layout(const DevStage& a, const DevStage& b
 // ============================================================================
 // One tile of one pass: state loads go through L2 (ld.global.cg) so that a
 // persistent launch may read tiles written earlier in the same launch.
-template <int MODE, int R>
+// LITE drops the shared-memory stages, 2-qubit dense and diagonal ops: the
+// body of programs made of 1-qubit dense gates, Pauli rotations, Z-rotation
+// runs and Pauli terms needs half the registers.
+template <int MODE, int R, bool LITE = false>
 __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int64_t b, uint32_t ntiles,
                                           float2* smem_raw) {
   constexpr int NR = 1 << R;
@@ -585,7 +588,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
 
   for (int s = P.stage_begin; s < P.stage_end; ++s) {
     const DevStage& S = A.prog.stages[s];
-    if (S.smem_stage) {
+    if (!LITE && S.smem_stage) {
       if (live) {
         regs_to_smem<R>(v, sm_psi, ly);
         if (HAS_MU) regs_to_smem<R>(w, sm_mu, ly);
@@ -667,7 +670,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
             dispatch_dense1_bwd<R, false>(op.p[0], v, w, a, acc);
           }
         }
-      } else if (kind == OP_DENSE2) {
+      } else if (!LITE && kind == OP_DENSE2) {
         const float2* m = mats + op.mat_off;
         if (MODE == MODE_FWD) {
           float2 mm[16];
@@ -694,7 +697,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
             dispatch_dense2_bwd<R, false>(op.p[0], op.p[1], v, w, a, acc);
           }
         }
-      } else if (kind == OP_DIAG) {
+      } else if (!LITE && kind == OP_DIAG) {
         const float2* m = mats + op.mat_off;
         const int k = op.k;
         // index contribution of the fixed part and of each register bit
@@ -910,8 +913,8 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 // the error flag says so) so the launch still finishes.
 constexpr unsigned long long kBatchWaitNs = 2000000000ull;
 
-template <int MODE, int R>
-__global__ void __launch_bounds__(256, 1) batch_kernel(BatchLaunch BL) {
+template <int MODE, int R, bool LITE>
+__global__ void __launch_bounds__(256, LITE ? 2 : 1) batch_kernel(BatchLaunch BL) {
   extern __shared__ __align__(16) float2 smem_raw[];
   __shared__ long long s_item;
   __shared__ int s_seg;
@@ -981,7 +984,7 @@ __global__ void __launch_bounds__(256, 1) batch_kernel(BatchLaunch BL) {
     A.coef = BL.coef ? BL.coef + C.coef_off : nullptr;
     A.coef_stride = 0;
     A.max_slots = C.max_slots;
-    pass_tile<MODE, R>(A, (uint32_t)(item - sg.item0), 0, sg.ntiles, smem_raw);
+    pass_tile<MODE, R, LITE>(A, (uint32_t)(item - sg.item0), 0, sg.ntiles, smem_raw);
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
@@ -1029,7 +1032,7 @@ static cudaError_t launch_one(const PassArgs& a, int L, int64_t batch, cudaStrea
   return cudaSuccess;
 }
 
-template <int MODE, int R>
+template <int MODE, int R, bool LITE>
 static cudaError_t launch_batch_one(const BatchLaunch& bl, int L, int max_slots, cudaStream_t st) {
   const int nthreads = 1 << (L - R);
   if (nthreads > kMaxThreads || nthreads < 1) return cudaErrorInvalidValue;
@@ -1042,30 +1045,38 @@ static cudaError_t launch_batch_one(const BatchLaunch& bl, int L, int max_slots,
   if (e != cudaSuccess) return e;
   static int attr_smem[64] = {0};
   if (dev < 64 && attr_smem[dev] < (int)smem) {
-    e = cudaFuncSetAttribute(batch_kernel<MODE, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(batch_kernel<MODE, R, LITE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
     if (e != cudaSuccess) return e;
     attr_smem[dev] = (int)smem;
   }
   int nsm = 0, per_sm = 0;
   e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<MODE, R>, nthreads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<MODE, R, LITE>, nthreads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int64_t grid = int64_t(nsm) * per_sm;
   if (grid > bl.nitems) grid = bl.nitems;
   if (grid < 1) return cudaSuccess;
   count_launch();
-  batch_kernel<MODE, R><<<(unsigned)grid, nthreads, smem, st>>>(bl);
+  batch_kernel<MODE, R, LITE><<<(unsigned)grid, nthreads, smem, st>>>(bl);
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch(int mode, const BatchLaunch& bl, int L, int max_slots, cudaStream_t st) {
+cudaError_t launch_batch(int mode, const BatchLaunch& bl, int L, int max_slots, bool lite, cudaStream_t st) {
   if (max_slots < 1) max_slots = 1;
-  if (mode == MODE_FWD) return launch_batch_one<MODE_FWD, 4>(bl, L, max_slots, st);
-  if (mode == MODE_BWD) return launch_batch_one<MODE_BWD, 4>(bl, L, max_slots, st);
-  if (mode == MODE_MEAS) return launch_batch_one<MODE_MEAS, 4>(bl, L, max_slots, st);
-  if (mode == MODE_PACC) return launch_batch_one<MODE_PACC, 4>(bl, L, max_slots, st);
+  if (lite) {
+    if (mode == MODE_FWD) return launch_batch_one<MODE_FWD, 4, true>(bl, L, max_slots, st);
+    if (mode == MODE_BWD) return launch_batch_one<MODE_BWD, 4, true>(bl, L, max_slots, st);
+    if (mode == MODE_MEAS) return launch_batch_one<MODE_MEAS, 4, true>(bl, L, max_slots, st);
+    if (mode == MODE_PACC) return launch_batch_one<MODE_PACC, 4, true>(bl, L, max_slots, st);
+    return cudaErrorInvalidValue;
+  }
+  if (mode == MODE_FWD) return launch_batch_one<MODE_FWD, 4, false>(bl, L, max_slots, st);
+  if (mode == MODE_BWD) return launch_batch_one<MODE_BWD, 4, false>(bl, L, max_slots, st);
+  if (mode == MODE_MEAS) return launch_batch_one<MODE_MEAS, 4, false>(bl, L, max_slots, st);
+  if (mode == MODE_PACC) return launch_batch_one<MODE_PACC, 4, false>(bl, L, max_slots, st);
   return cudaErrorInvalidValue;
 }
 
