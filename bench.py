@@ -633,8 +633,10 @@ def run_warmstart(args, rank, world):
 
 
 def main():
-    global BATCH, BW_N
+    global BATCH, BW_N, QB_COUNT
     ap = argparse.ArgumentParser()
+    ap.add_argument("--qaoa-circuits", type=int, default=QB_COUNT,
+                    help="qaoa: circuits in the batch (512 is the configured workload; fewer for profiler captures)")
     ap.add_argument("--bw-qubits", type=int, default=BW_N,
                     help="brickwall: qubits (28 is the configured workload; fewer for profiler captures)")
     ap.add_argument("--gpus", type=int, default=1)
@@ -657,6 +659,7 @@ def main():
     args = ap.parse_args()
     BATCH = args.batch
     BW_N = args.bw_qubits
+    QB_COUNT = args.qaoa_circuits
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
