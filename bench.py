@@ -96,6 +96,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def aggregate_replicas(ms_values, units_per_rank, world, device):
+    """Replicas (one independent batch per rank, no exchange on the data
+    path): the step time is the maximum over ranks, the throughput the units
+    of all ranks over that time.  Returns (max times in ms, units/s)."""
+    if world > 1:
+        import torch
+
+        t = torch.tensor([float(x) for x in ms_values], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_values = t.tolist()
+    return list(ms_values), [world * units_per_rank / (m / 1e3) for m in ms_values]
+
+
 def _workload_params():
     from tensorcircuit_gb300 import templates
 
@@ -283,14 +296,7 @@ def run_gb300_arm(args, rank, world):
             traffic = None
 
     # ---- aggregate over ranks (replicas)
-    circ_s = BATCH / (ms / 1e3)
-    circ_e2e = BATCH / (ms_e2e / 1e3)
-    if world > 1:
-        t = torch.tensor([ms, ms_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms_e2e = t.tolist()
-        circ_s = world * BATCH / (ms / 1e3)
-        circ_e2e = world * BATCH / (ms_e2e / 1e3)
+    (ms, ms_e2e), (circ_s, circ_e2e) = aggregate_replicas([ms, ms_e2e], BATCH, world, dev)
     if rank != 0:
         return
     cpu = None
