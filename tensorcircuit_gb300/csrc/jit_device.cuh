@@ -356,24 +356,32 @@ __device__ __forceinline__ float2 ypowc() {
        : (NY & 3) == 2 ? make_float2(-1.f, 0.f) : make_float2(0.f, 1.f);
 }
 
+// q = -i s (-i)^NY is purely imaginary for even NY and purely real for odd
+// NY, so the pair update a' = c a + q b needs four real operations per
+// amplitude: (c a.x - q b.y, c a.y + q b.x) or (c a.x + q b.x, c a.y + q b.y).
 template <int NR, int X, int ZR, int NY>
 __device__ __forceinline__ void prot(float2 (&v)[NR], float c, float s, u32 sgn, bool adj) {
-  float2 q = cmul(make_float2(0.f, -s), ypowc<NY>());
-  if (adj ^ (sgn != 0u)) q = cneg(q);
+  constexpr bool QIM = (NY & 1) == 0;
+  float qv = ((NY & 3) <= 1) ? -s : s;  // the nonzero component of q
+  if (adj ^ (sgn != 0u)) qv = -qv;
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
-    const bool neg = tk_popc(r & ZR) & 1;
-    const float2 qr = neg ? cneg(q) : q;
+    const float qr = (tk_popc(r & ZR) & 1) ? -qv : qv;
     if (X == 0) {
-      v[r] = cmul(make_float2(c + qr.x, qr.y), v[r]);
+      if (QIM) v[r] = cmul(make_float2(c, qr), v[r]);
+      else v[r] = make_float2((c + qr) * v[r].x, (c + qr) * v[r].y);
     } else {
       const int r2 = r ^ X;
       if (r2 < r) continue;
-      const bool neg2 = tk_popc(r2 & ZR) & 1;
-      const float2 q2 = neg2 ? cneg(q) : q;
+      const float q2 = (tk_popc(r2 & ZR) & 1) ? -qv : qv;
       const float2 a = v[r], bb = v[r2];
-      v[r] = cfma(qr, bb, make_float2(c * a.x, c * a.y));
-      v[r2] = cfma(q2, a, make_float2(c * bb.x, c * bb.y));
+      if (QIM) {
+        v[r] = make_float2(fmaf(-qr, bb.y, c * a.x), fmaf(qr, bb.x, c * a.y));
+        v[r2] = make_float2(fmaf(-q2, a.y, c * bb.x), fmaf(q2, a.x, c * bb.y));
+      } else {
+        v[r] = make_float2(fmaf(qr, bb.x, c * a.x), fmaf(qr, bb.y, c * a.y));
+        v[r2] = make_float2(fmaf(q2, a.x, c * bb.x), fmaf(q2, a.y, c * bb.y));
+      }
     }
   }
 }
@@ -383,23 +391,20 @@ __device__ __forceinline__ void prot(float2 (&v)[NR], float c, float s, u32 sgn,
 template <int NR, int X, int ZR, int NY, bool G>
 __device__ __forceinline__ void prot_bwd(float2 (&v)[NR], float2 (&w)[NR], float c, float s, u32 sgn, float& g) {
   if (G) {
-    float2 z = czero();
+    // g = Im(pt z), z = sum_r s(r) conj(w_r) v_{r^X}, pt = (+-)(-i)^NY: only
+    // Im z (even NY) or Re z (odd NY) is needed
+    constexpr bool IMZ = (NY & 1) == 0;
+    float zc = 0.f;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
       const float2 t = v[r ^ X];
-      const float cx = fmaf(w[r].x, t.x, w[r].y * t.y);   // conj(w) * t
-      const float cy = fmaf(w[r].x, t.y, -w[r].y * t.x);
-      if (tk_popc(r & ZR) & 1) {
-        z.x -= cx;
-        z.y -= cy;
-      } else {
-        z.x += cx;
-        z.y += cy;
-      }
+      const float term = IMZ ? fmaf(w[r].x, t.y, -w[r].y * t.x) : fmaf(w[r].x, t.x, w[r].y * t.y);
+      if (tk_popc(r & ZR) & 1) zc -= term;
+      else zc += term;
     }
-    float2 pt = ypowc<NY>();
-    if (sgn) pt = cneg(pt);
-    g = fmaf(pt.x, z.y, pt.y * z.x);  // Im(pt * z)
+    // Im(pt z): NY%4 = 0 -> z.y, 1 -> -z.x, 2 -> -z.y, 3 -> z.x
+    g = ((NY & 3) == 0 || (NY & 3) == 3) ? zc : -zc;
+    if (sgn) g = -g;
   }
   prot<NR, X, ZR, NY>(v, c, s, sgn, true);
   prot<NR, X, ZR, NY>(w, c, s, sgn, true);
