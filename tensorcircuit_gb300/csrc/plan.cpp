@@ -538,6 +538,34 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
       if (popc64(S | need) <= L) S |= need;
     }
     for (int b = 0; b < n && popc64(S) < L; ++b) S |= 1ull << b;
+    // Z-string rotations commute with every gate on other qubits and with
+    // all diagonal gates: move each one back to the nearest earlier Z-string
+    // rotation it can reach, so that runs (one phase op each) grow long
+    {
+      auto is_z = [&](const PGate& g) { return g.kind == TCG_GATE_PAULI_ROT && g.xmask == 0; };
+      std::vector<int> ord;
+      ord.reserve(taken.size());
+      for (int gi : taken) {
+        const PGate& g = gates[gi];
+        if (!is_z(g)) {
+          ord.push_back(gi);
+          continue;
+        }
+        const uint64_t m = gate_mask(g);
+        int at = -1;
+        for (int j = (int)ord.size() - 1; j >= 0; --j) {
+          const PGate& h = gates[ord[j]];
+          if (is_z(h)) {
+            at = j + 1;
+            break;
+          }
+          if (h.kind != TCG_GATE_DIAG && (gate_mask(h) & m)) break;  // does not commute
+        }
+        if (at < 0) ord.push_back(gi);
+        else ord.insert(ord.begin() + at, gi);
+      }
+      taken.swap(ord);
+    }
     std::vector<OpDraft> od;
     for (int gi : taken) {
       const PGate& g = gates[gi];
