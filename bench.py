@@ -138,6 +138,35 @@ def cpu_reference(steps, warmup, sample_circuits=1):
             "seconds_per_circuit": dt / sample_circuits}
 
 
+def gpu_plain_ad(sample_circuits=8, steps=2):
+    """The reference algorithm's taped AD (per-gate tensordot, torch.func
+    vmap/grad -- the reference's pytorch backend) placed on the same GPU,
+    on a bounded sample of the batch: the 'plain AD on the same GPU' the
+    adjoint kernel is compared with."""
+    import torch
+
+    from oracle import reference_algo as ra
+    from tensorcircuit_gb300 import templates
+
+    params = _workload_params()[:sample_circuits]
+    layout = templates.hea_layout(N_QUBITS, N_LAYERS)
+    terms = templates.tfim_terms(N_QUBITS, -1.0, -1.0)
+    try:
+        ra.vvag_hea(N_QUBITS, layout, terms, params, 1, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ra.vvag_hea(N_QUBITS, layout, terms, params, 1, device="cuda")
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+    except Exception as exc:  # e.g. out of memory for the taped states
+        return {"unavailable": "%s: %s" % (type(exc).__name__, str(exc)[:200])}
+    return {"value": sample_circuits / dt, "unit": UNIT,
+            "sample": "%d of the %d circuits, %d steps (labelled torch restatement of the reference "
+                      "algorithm: per-gate tensordot + taped AD via torch.func vmap/grad, on the GPU)" %
+                      (sample_circuits, BATCH, steps)}
+
+
 def run_reference_arm(args, rank):
     if rank != 0:
         return
@@ -300,8 +329,10 @@ def run_gb300_arm(args, rank, world):
     if rank != 0:
         return
     cpu = None
+    plain_ad = None
     if world == 1 and not args.no_cpu:
         cpu = cpu_reference(steps=1, warmup=0)
+        plain_ad = gpu_plain_ad()
     line = {
         "metric": METRIC, "value": circ_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -317,6 +348,7 @@ def run_gb300_arm(args, rank, world):
                      "forward_sweep": {"ms": ms_fwd, "passes": plan.npasses,
                                        "GB_per_s": plan.npasses * 16 * N * BATCH / (ms_fwd / 1e3) / 1e9}},
         "cpu_baseline": cpu,
+        "plain_ad_same_gpu": plain_ad,
         "e2e": {"value": circ_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),

@@ -24,16 +24,16 @@ C64 = torch.complex64
 def _rx(theta: torch.Tensor) -> torch.Tensor:
     c = torch.cos(theta / 2).to(C64)
     s = torch.sin(theta / 2).to(C64)
-    i2 = torch.eye(2, dtype=C64)
-    x = torch.tensor([[0, 1], [1, 0]], dtype=C64)
+    i2 = torch.eye(2, dtype=C64, device=theta.device)
+    x = torch.tensor([[0, 1], [1, 0]], dtype=C64, device=theta.device)
     return c * i2 - 1j * s * x
 
 
 def _rzz(theta: torch.Tensor) -> torch.Tensor:
     c = torch.cos(theta / 2).to(C64)
     s = torch.sin(theta / 2).to(C64)
-    zz = torch.diag(torch.tensor([1, -1, -1, 1], dtype=C64))
-    return (c * torch.eye(4, dtype=C64) - 1j * s * zz).reshape(2, 2, 2, 2)
+    zz = torch.diag(torch.tensor([1, -1, -1, 1], dtype=C64, device=theta.device))
+    return (c * torch.eye(4, dtype=C64, device=theta.device) - 1j * s * zz).reshape(2, 2, 2, 2)
 
 
 _PAULI = {
@@ -50,21 +50,22 @@ def _apply(psi: torch.Tensor, g: torch.Tensor, qubits: Sequence[int]) -> torch.T
 
 
 def hea_energy_fn(n: int, layout: Sequence[Tuple[str, Tuple[int, ...], int]],
-                  terms: Sequence[Tuple[float, Dict[str, List[int]]]]) -> Any:
-    psi0 = torch.zeros([2] * n, dtype=C64)
+                  terms: Sequence[Tuple[float, Dict[str, List[int]]]], device: str = "cpu") -> Any:
+    psi0 = torch.zeros([2] * n, dtype=C64, device=device)
     psi0.view(-1)[0] = 1.0
+    paulis = {k: v.to(device) for k, v in _PAULI.items()}
 
     def f(params: torch.Tensor) -> torch.Tensor:
         psi = psi0
         for name, q, k in layout:
             g = _rx(params[k]) if name == "rx" else _rzz(params[k])
             psi = _apply(psi, g, q)
-        e = torch.zeros((), dtype=torch.float32)
+        e = torch.zeros((), dtype=torch.float32, device=device)
         for coef, t in terms:
             phi = psi
             for kind, qs in t.items():
                 for qq in qs:
-                    phi = _apply(phi, _PAULI[kind], (qq,))
+                    phi = _apply(phi, paulis[kind], (qq,))
             e = e + coef * torch.real(torch.sum(torch.conj(psi) * phi))
         return e
 
@@ -73,12 +74,14 @@ def hea_energy_fn(n: int, layout: Sequence[Tuple[str, Tuple[int, ...], int]],
 
 def vvag_hea(n: int, layout: Sequence[Tuple[str, Tuple[int, ...], int]],
              terms: Sequence[Tuple[float, Dict[str, List[int]]]], params: np.ndarray,
-             threads: int) -> Tuple[np.ndarray, np.ndarray]:
+             threads: int, device: str = "cpu") -> Tuple[np.ndarray, np.ndarray]:
+    """``device="cuda"`` runs the same taped-AD restatement on the GPU (the
+    reference's pytorch backend placed on the GPU)."""
     torch.set_num_threads(threads)
-    f = hea_energy_fn(n, layout, terms)
+    f = hea_energy_fn(n, layout, terms, device)
     vg = torch.func.vmap(torch.func.grad_and_value(f))
-    g, v = vg(torch.as_tensor(params, dtype=torch.float32))
-    return v.numpy(), g.numpy()
+    g, v = vg(torch.as_tensor(params, dtype=torch.float32, device=device))
+    return v.cpu().numpy(), g.cpu().numpy()
 
 
 def run_gate_list(n: int, gl: Sequence[Tuple[str, Tuple[int, ...], Dict[str, Any]]], threads: int) -> torch.Tensor:
