@@ -315,55 +315,78 @@ class Gen {
       }
     } else if (op.kind == OP_ZRUN) {
       // entries are literals: each run is its own body
-      b << "float2 ph[" << NR_ << "];\n#pragma unroll\n for (int c = 0; c < " << NR_
-        << "; ++c) ph[c] = make_float2(1.f, 0.f);";
-      std::vector<const ZEnt*> grads;
-      for (int e = 0; e < op.k; ++e) {
-        const ZEnt& z = P_.zents[op.mat_off + e];
-        b << " ph[" << z.zreg << "] = cmul(ph[" << z.zreg << "], zrun_factor(Mt + " << z.mat_off << "ll, gthr, "
-          << z.zmask << "u));";
-        if (z.slot >= 0) grads.push_back(&z);
-      }
-      b << " mul_walsh<" << NR_ << ">(ph);";
-      if (fwd()) {
-        b << " zrun_apply<" << NR_ << ">(v, ph);";
-      } else {
-        if (!grads.empty()) {
-          // gradient pairs (g_{2i}, g_{2i+1}) of consecutive slots
-          const int KG = (int)grads.size();
-          int E2 = 1;
-          while (E2 < (KG + 1) / 2) E2 <<= 1;
-          b << " { float t[" << NR_ << "]; zrun_grad<" << NR_ << ">(v, w, t); float2 g[" << E2 << "];";
-          for (int i = 0; i < E2; ++i) {
-            std::string xs = "0.f", ys = "0.f";
-            for (int h = 0; h < 2; ++h) {
-              const int k = 2 * i + h;
-              if (k >= KG) continue;
-              std::ostringstream s;
-              s << "((__popc(gthr & " << grads[k]->zmask << "u) & 1u) ? -t[" << grads[k]->zreg << "] : t["
-                << grads[k]->zreg << "])";
-              (h == 0 ? xs : ys) = s.str();
-            }
-            b << " g[" << i << "] = make_float2(" << xs << ", " << ys << ");";
+      std::vector<const ZEnt*> slotted;
+      for (int e = 0; e < op.k; ++e)
+        if (P_.zents[op.mat_off + e].slot >= 0) slotted.push_back(&P_.zents[op.mat_off + e]);
+      // per-entry values s_e * t[class_e] reduced over the block in pairs
+      // (g_{2i}, g_{2i+1}) of consecutive slots
+      auto emit_pairs = [&]() {
+        const int KG = (int)slotted.size();
+        if (KG == 0) return;
+        int E2 = 1;
+        while (E2 < (KG + 1) / 2) E2 <<= 1;
+        b << " float2 g[" << E2 << "];";
+        for (int i = 0; i < E2; ++i) {
+          std::string xs = "0.f", ys = "0.f";
+          for (int h = 0; h < 2; ++h) {
+            const int k = 2 * i + h;
+            if (k >= KG) continue;
+            std::ostringstream s;
+            s << "((__popc(gthr & " << slotted[k]->zmask << "u) & 1u) ? -t[" << slotted[k]->zreg << "] : t["
+              << slotted[k]->zreg << "])";
+            (h == 0 ? xs : ys) = s.str();
           }
-          if (NL_ < 32) {
-            b << " float2 red[" << E2 << "]; small_reduce<" << E2 << ", " << NL_
-              << ">(g, lane, red); if (lane == 0) { ";
-            for (int k = 0; k < KG; ++k)
-              b << "sms[op.slot + " << k << "] = make_float2(red[" << k / 2 << "]." << (k % 2 ? "y" : "x")
-                << ", 0.f); ";
-            b << "}";
-          } else {
-            // padding pairs (entries >= KG) hold zeros and must not be
-            // written: their slots belong to other ops or other warps
-            b << " int ent; const float2 s = warp_reduce<" << E2 << ", " << NL_
-              << ">(g, lane, ent); if (ent >= 0 && 2 * ent < " << KG << ") { sms[warp * " << MS_
-              << " + op.slot + 2 * ent] = make_float2(s.x, 0.f); if (2 * ent + 1 < " << KG << ") sms[warp * "
-              << MS_ << " + op.slot + 2 * ent + 1] = make_float2(s.y, 0.f); }";
-          }
-          b << " }";
+          b << " g[" << i << "] = make_float2(" << xs << ", " << ys << ");";
         }
-        b << " zrun_unapply<" << NR_ << ">(v, w, ph);";
+        if (NL_ < 32) {
+          b << " float2 red[" << E2 << "]; small_reduce<" << E2 << ", " << NL_
+            << ">(g, lane, red); if (lane == 0) { ";
+          for (int k = 0; k < KG; ++k)
+            b << "sms[op.slot + " << k << "] = make_float2(red[" << k / 2 << "]." << (k % 2 ? "y" : "x")
+              << ", 0.f); ";
+          b << "}";
+        } else {
+          // padding pairs (entries >= KG) hold zeros and must not be
+          // written: their slots belong to other ops or other warps
+          b << " int ent; const float2 s = warp_reduce<" << E2 << ", " << NL_
+            << ">(g, lane, ent); if (ent >= 0 && 2 * ent < " << KG << ") { sms[warp * " << MS_
+            << " + op.slot + 2 * ent] = make_float2(s.x, 0.f); if (2 * ent + 1 < " << KG << ") sms[warp * "
+            << MS_ << " + op.slot + 2 * ent + 1] = make_float2(s.y, 0.f); }";
+        }
+      };
+      if (meas()) {
+        // Z-string terms: <Z_S> partials from one transform of |v_r|^2
+        b << "{ float t[" << NR_ << "]; zmeas_t<" << NR_ << ">(v, t);";
+        emit_pairs();
+        b << " }";
+      } else if (pacc()) {
+        // mu += (sum_t c_t s_t(x)) psi: class sums and one transform
+        b << "{ float a[" << NR_ << "];\n#pragma unroll\n for (int c = 0; c < " << NR_ << "; ++c) a[c] = 0.f;";
+        for (int e = 0; e < op.k; ++e) {
+          const ZEnt& z = P_.zents[op.mat_off + e];
+          b << " a[" << z.zreg << "] += ((__popc(gthr & " << z.zmask << "u) & 1u) ? -1.f : 1.f) * kp.coef[b * "
+            << "kp.coef_stride + " << z.mat_off << "ll];";
+        }
+        b << " add_walsh<" << NR_ << ">(a); zpacc_apply<" << NR_ << ">(v, w, a); }";
+      } else {
+        b << "float2 ph[" << NR_ << "];\n#pragma unroll\n for (int c = 0; c < " << NR_
+          << "; ++c) ph[c] = make_float2(1.f, 0.f);";
+        for (int e = 0; e < op.k; ++e) {
+          const ZEnt& z = P_.zents[op.mat_off + e];
+          b << " ph[" << z.zreg << "] = cmul(ph[" << z.zreg << "], zrun_factor(Mt + " << z.mat_off << "ll, gthr, "
+            << z.zmask << "u));";
+        }
+        b << " mul_walsh<" << NR_ << ">(ph);";
+        if (fwd()) {
+          b << " zrun_apply<" << NR_ << ">(v, ph);";
+        } else {
+          if (!slotted.empty()) {
+            b << " { float t[" << NR_ << "]; zrun_grad<" << NR_ << ">(v, w, t);";
+            emit_pairs();
+            b << " }";
+          }
+          b << " zrun_unapply<" << NR_ << ">(v, w, ph);";
+        }
       }
     } else if (op.kind == OP_EXPECT) {
       int zr = 0;

@@ -465,6 +465,20 @@ __device__ __forceinline__ void zrun_grad(const float2 (&v)[NR], const float2 (&
   for (int r = 0; r < NR; ++r) t[r] = fmaf(w[r].x, v[r].y, -w[r].y * v[r].x);
   add_walsh<NR>(t);
 }
+// t[c] = sum_r (-1)^{popc(r & c)} |v_r|^2 (Z-string term partials)
+template <int NR>
+__device__ __forceinline__ void zmeas_t(const float2 (&v)[NR], float (&t)[NR]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) t[r] = fmaf(v[r].x, v[r].x, v[r].y * v[r].y);
+  add_walsh<NR>(t);
+}
+// w_r += a_r v_r (a_r real: the summed Z-term coefficients of register r)
+template <int NR>
+__device__ __forceinline__ void zpacc_apply(const float2 (&v)[NR], float2 (&w)[NR], const float (&a)[NR]) {
+#pragma unroll
+  for (int r = 0; r < NR; ++r) w[r] = make_float2(fmaf(a[r], v[r].x, w[r].x), fmaf(a[r], v[r].y, w[r].y));
+}
+
 // Butterfly sum of E values over the NL (< 32) lanes of a small block; lane 0
 // writes value e to out[e].
 template <int E, int NL>

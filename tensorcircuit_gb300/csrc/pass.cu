@@ -791,6 +791,36 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
           dispatch_prot<R>(op.xreg, w, cs.x, mq, zr);
         }
       } else if (kind == OP_ZRUN) {
+        if (MODE == MODE_MEAS) {
+          // <Z_S> partial = sum_x s(x) |psi_x|^2: one transform of |v_r|^2
+          float t[NR];
+#pragma unroll
+          for (int r = 0; r < NR; ++r) t[r] = fmaf(v[r].x, v[r].x, v[r].y * v[r].y);
+          add_walsh<R>(t);
+          for (int e = 0; e < op.k; ++e) {
+            const ZEnt ze = A.prog.zents[op.mat_off + e];
+            float g = class_pick<R>(t, ze.zreg);
+            if (__popc(gthr & ze.zmask) & 1) g = -g;
+            const float2 s = warp_sum(make_float2(g, 0.f), nl);
+            if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = s;
+          }
+        } else if (MODE == MODE_PACC) {
+          // mu += (sum_t c_t s_t(x)) psi: class sums, one transform
+          float a[NR];
+#pragma unroll
+          for (int c = 0; c < NR; ++c) a[c] = 0.f;
+          for (int e = 0; e < op.k; ++e) {
+            const ZEnt ze = A.prog.zents[op.mat_off + e];
+            float cf = A.coef[b * A.coef_stride + ze.mat_off];
+            if (__popc(gthr & ze.zmask) & 1) cf = -cf;
+#pragma unroll
+            for (int c = 0; c < NR; ++c)
+              if (c == ze.zreg) a[c] += cf;
+          }
+          add_walsh<R>(a);
+#pragma unroll
+          for (int r = 0; r < NR; ++r) w[r] = make_float2(fmaf(a[r], v[r].x, w[r].x), fmaf(a[r], v[r].y, w[r].y));
+        }
         if (MODE == MODE_FWD || MODE == MODE_BWD) {
           float2 ph[NR];
 #pragma unroll

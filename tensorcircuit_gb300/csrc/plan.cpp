@@ -135,12 +135,17 @@ int emit_stage(Program* P, DevPass& dp, const StageDraft& sd,
     const int oi = sd.ops[si];
     const OpDraft& o = od[oi];
     // a run of >= 2 consecutive Z-string rotations (no X/Y factor) becomes
-    // one OP_ZRUN: they commute, so their product is one phase per amplitude
-    if (o.kind == TCG_GATE_PAULI_ROT && o.x == 0) {
+    // one OP_ZRUN: they commute, so their product is one phase per amplitude.
+    // In a measurement program the same op carries Z-string Pauli terms
+    // (entry mat_off = term id, every entry has a slot): all their values,
+    // or their accumulated coefficients, come from one Walsh-Hadamard
+    // transform per thread.
+    const bool zterm = (o.kind == OP_EXPECT && o.x == 0);
+    if ((o.kind == TCG_GATE_PAULI_ROT && o.x == 0) || zterm) {
       size_t sj = si;
       while (sj < sd.ops.size() && sj - si < (size_t)kZRunMax) {
         const OpDraft& q = od[sd.ops[sj]];
-        if (q.kind != TCG_GATE_PAULI_ROT || q.x != 0) break;
+        if (q.kind != o.kind || q.x != 0) break;
         ++sj;
       }
       if (sj - si >= 2) {
@@ -164,16 +169,16 @@ int emit_stage(Program* P, DevPass& dp, const StageDraft& sd,
               if (rp >= 0) zr |= 1 << rp;
             }
           z.zreg = zr;
-          z.mat_off = q.mat_off;
-          z.grad_off = q.grad_off;
+          z.mat_off = zterm ? q.term : q.mat_off;
+          z.grad_off = zterm ? q.term : q.grad_off;
           z.slot = -1;
-          if (q.grad_off >= 0) {
+          if (z.grad_off >= 0) {
             if (d.slot < 0) d.slot = slot;
             z.slot = slot;
             SlotOut so;
             so.slot = slot;
             so.pad = 0;
-            so.out_off = q.grad_off;
+            so.out_off = z.grad_off;
             P->slot_out.push_back(so);
             slot += 1;
           }

@@ -135,6 +135,12 @@ class Replay:
                     V = T[J]
                     for o in range(S.op_begin, S.op_end):
                         op = O_list[o]
+                        if op.kind == OP_ZRUN:
+                            # Z-string terms: sum_x s_t(x) |psi_x|^2, thread/register split
+                            G = self._gidx(gthr, rg, R)
+                            for z, sg in self._zrun_signs(op, G, R):
+                                out[z.mat_off] += np.sum(sg * np.abs(V) ** 2)
+                            continue
                         assert op.kind == OP_EXPECT
                         X = op.xreg
                         sbase = _popc(gthr & op.zmask) & 1
