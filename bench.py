@@ -96,6 +96,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def _traffic(key, applies):
+    """DRAM bytes per launch of the dominant kernel from the ncu captures
+    (profiles/traffic.json), when the run has the captured configuration."""
+    if not applies:
+        return None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            return json.load(fh).get(key)
+    except Exception:
+        return None
+
+
 def aggregate_replicas(ms_values, units_per_rank, world, device):
     """Replicas (one independent batch per rank, no exchange on the data
     path): the step time is the maximum over ranks, the throughput the units
@@ -316,13 +328,7 @@ def run_gb300_arm(args, rank, world):
     per_launch_s = ms_bwd / 1e3 / nb_pass
     achieved = (alg_bytes / nb_pass) / per_launch_s / 1e9
     peak, peak_kind = _peaks()
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get("pass_kernel_bwd_bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic = _traffic("pass_kernel_bwd_bytes_per_launch", BATCH == 64)
 
     # ---- aggregate over ranks (replicas)
     (ms, ms_e2e), (circ_s, circ_e2e) = aggregate_replicas([ms, ms_e2e], BATCH, world, dev)
@@ -489,7 +495,8 @@ def run_brickwall(args, rank, world):
                    "fwd_passes": plan.npasses, "zz_0_27": float(zz.real), "x_13": float(x13.real)},
         "roofline": {"bound": "hbm", "kernel": "forward pass (tcg_forward, one launch per pass)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": None, "alg_bytes_per_launch": 16.0 * N,
+                     "peak_source": peak_kind, "traffic": _traffic("brickwall_fwd_bytes_per_launch", n == 28),
+                     "alg_bytes_per_launch": 16.0 * N,
                      "ms_forward": ms_fwd, "passes": plan.npasses,
                      "amp_updates_per_s": len(gl) * N / (ms_fwd / 1e3),
                      "gate_updates_per_s_forward": len(gl) / (ms_fwd / 1e3)},
