@@ -519,10 +519,16 @@ class Gen {
     for (size_t i = 0; i < so.size(); ++i) out << (i ? ", " : "") << so[i];
     out << "};\n";
 
-    // kernel: two CTAs per SM in every mode (the adjoint kernel then has 128
-    // registers for psi + mu; a second resident CTA hides the latency of the
-    // dependent FMA chains and shuffles that a single 8-warp CTA exposes)
-    out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", 2) "
+    // kernel: three CTAs per SM for the modes that hold psi only (80
+    // registers), two for the ones that also hold mu or the 16 phases of a
+    // Z-rotation run (128 registers): more resident warps hide the dependent
+    // FMA chains and shuffles of these issue-bound kernels
+    bool zrun = false;
+    for (int s = dp_->stage_begin; s < dp_->stage_end; ++s)
+      for (int o = P_.stages[s].op_begin; o < P_.stages[s].op_end; ++o)
+        if (P_.ops[o].kind == OP_ZRUN) zrun = true;
+    const int min_ctas = (has_mu_ || (zrun && fwd())) ? 2 : 3;
+    out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", " << min_ctas << ") "
         << kernel_name(mode_, pi)
         << "(KParams kp) {\n";
     out << "  using namespace tk;\n  extern __shared__ __align__(16) float2 smem[];\n";

@@ -86,10 +86,21 @@ def test_hea_forward_and_adjoint_kernels_compile():
     regs_f, sp_f = check_compiles(e.plan.handle, 0, 0)
     regs_b, sp_b = check_compiles(e.plan.handle, 1, 1)
     print("forward registers", regs_f, "adjoint registers", regs_b, "spills", sp_f, sp_b)
-    # two CTAs per SM: at most 128 registers; the adjoint kernels (psi and mu
-    # in registers) may spill a few words
-    assert max(sp_f + [0]) == 0 and max(sp_b + [0]) <= 64
+    # forward passes with Z-rotation runs and the adjoint keep two CTAs per SM
+    # (<= 128 registers); either may spill a few words
+    assert max(sp_f + [0]) <= 64 and max(sp_b + [0]) <= 64
     assert max(regs_f) <= 128 and max(regs_b) <= 128, (regs_f, regs_b)
+
+
+def test_brickwall_forward_kernels_fit_three_ctas():
+    """Dense 2-qubit passes (no Z runs) run three CTAs per SM: <= 80
+    registers with at most a few spilled words."""
+    n = 24
+    gl = templates.brickwall_gate_list(n, 8, 3)
+    c = templates.apply_gate_list(cmod.Circuit(n), gl)
+    e = cmod._build_entry(n, c._ops)
+    regs, spills = check_compiles(e.plan.handle, 0, 0)
+    assert max(regs) <= 80 and max(spills + [0]) <= 64, (regs, spills)
 
 
 def test_random_circuit_kernels_compile():
