@@ -410,11 +410,26 @@ __device__ void dispatch_denseK(int k, float2* tile, int L, const int* tb, const
 // A_c = prod_{c_e = c} B_e, the phase of register r is
 // prod_c (popc(r & c) even ? A_c : conj(A_c)): a multiplicative Walsh-Hadamard
 // transform of A, computed with 2^R * R complex products per thread.
+// Run-time class index into a register array: a switch (one indexed branch
+// and one update) instead of 2^R predicated updates.
+#define TCG_CASES16(M) M(0) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11) M(12) M(13) M(14) M(15)
 template <int R>
 __device__ __forceinline__ void class_mul(float2 (&a)[1 << R], int c, float2 u) {
-#pragma unroll
-  for (int i = 0; i < (1 << R); ++i)
-    if (i == c) a[i] = cmul(a[i], u);
+  switch (c) {
+#define TCG_CM(I) case I: if ((I) < (1 << R)) a[(I) < (1 << R) ? (I) : 0] = cmul(a[(I) < (1 << R) ? (I) : 0], u); break;
+    TCG_CASES16(TCG_CM)
+#undef TCG_CM
+    default: break;
+  }
+}
+template <int R>
+__device__ __forceinline__ void class_add(float (&a)[1 << R], int c, float x) {
+  switch (c) {
+#define TCG_CA(I) case I: if ((I) < (1 << R)) a[(I) < (1 << R) ? (I) : 0] += x; break;
+    TCG_CASES16(TCG_CA)
+#undef TCG_CA
+    default: break;
+  }
 }
 template <int R>
 __device__ __forceinline__ void mul_walsh(float2 (&a)[1 << R]) {
@@ -442,11 +457,12 @@ __device__ __forceinline__ void add_walsh(float (&a)[1 << R]) {
 }
 template <int R>
 __device__ __forceinline__ float class_pick(const float (&a)[1 << R], int c) {
-  float r = 0.f;
-#pragma unroll
-  for (int i = 0; i < (1 << R); ++i)
-    if (i == c) r = a[i];
-  return r;
+  switch (c) {
+#define TCG_CP(I) case I: return a[(I) < (1 << R) ? (I) : 0];
+    TCG_CASES16(TCG_CP)
+#undef TCG_CP
+    default: return 0.f;
+  }
 }
 
 // ------------------------------------------------------------------ tile I/O
@@ -813,9 +829,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
             const ZEnt ze = A.prog.zents[op.mat_off + e];
             float cf = A.coef[b * A.coef_stride + ze.mat_off];
             if (__popc(gthr & ze.zmask) & 1) cf = -cf;
-#pragma unroll
-            for (int c = 0; c < NR; ++c)
-              if (c == ze.zreg) a[c] += cf;
+            class_add<R>(a, ze.zreg, cf);
           }
           add_walsh<R>(a);
 #pragma unroll
