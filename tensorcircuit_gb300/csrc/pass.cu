@@ -272,36 +272,41 @@ __device__ __forceinline__ void dispatch_pacc(int x, const float2 (&v)[1 << R], 
 
 // Pauli rotation on registers: v[r] <- c v[r] + (-1)^{popc(r & zr)} q v[r ^ X]
 // (q = -i s (-i)^nY with the thread's sign folded in; the adjoint passes -q).
-template <int R, int X>
-__device__ __forceinline__ void prot_rt(float2 (&v)[1 << R], float c, float2 q, int zr) {
+// q is purely imaginary (QIM, even nY) or purely real, so it is carried as
+// one real number qv and the update costs four operations per amplitude.
+template <int R, int X, bool QIM>
+__device__ __forceinline__ void prot_rt(float2 (&v)[1 << R], float c, float qv, int zr) {
 #pragma unroll
   for (int r = 0; r < (1 << R); ++r) {
-    const float2 qr = (__popc(r & zr) & 1) ? make_float2(-q.x, -q.y) : q;
+    const float qr = (__popc(r & zr) & 1) ? -qv : qv;
     if (X == 0) {
-      v[r] = cmul(make_float2(c + qr.x, qr.y), v[r]);
+      if (QIM) v[r] = cmul(make_float2(c, qr), v[r]);
+      else v[r] = make_float2((c + qr) * v[r].x, (c + qr) * v[r].y);
     } else {
       const int r2 = r ^ X;
       if (r2 < r) continue;
-      const float2 q2 = (__popc(r2 & zr) & 1) ? make_float2(-q.x, -q.y) : q;
+      const float q2 = (__popc(r2 & zr) & 1) ? -qv : qv;
       const float2 a = v[r], bb = v[r2];
-      v[r] = cfma(qr, bb, make_float2(c * a.x, c * a.y));
-      v[r2] = cfma(q2, a, make_float2(c * bb.x, c * bb.y));
+      if (QIM) {
+        v[r] = make_float2(fmaf(-qr, bb.y, c * a.x), fmaf(qr, bb.x, c * a.y));
+        v[r2] = make_float2(fmaf(-q2, a.y, c * bb.x), fmaf(q2, a.x, c * bb.y));
+      } else {
+        v[r] = make_float2(fmaf(qr, bb.x, c * a.x), fmaf(qr, bb.y, c * a.y));
+        v[r2] = make_float2(fmaf(q2, a.x, c * bb.x), fmaf(q2, a.y, c * bb.y));
+      }
     }
   }
 }
 
-// sum_r (-1)^{popc(r & zr)} conj(w[r]) v[r ^ X]
-template <int R, int X>
-__device__ __forceinline__ float2 prot_dot(const float2 (&v)[1 << R], const float2 (&w)[1 << R], int zr) {
-  float2 z = czero();
+// Im (IMZ) or Re of sum_r (-1)^{popc(r & zr)} conj(w[r]) v[r ^ X]
+template <int R, int X, bool IMZ>
+__device__ __forceinline__ float prot_dot(const float2 (&v)[1 << R], const float2 (&w)[1 << R], int zr) {
+  float z = 0.f;
 #pragma unroll
   for (int r = 0; r < (1 << R); ++r) {
     const float2 t = v[r ^ X];
-    const float cx = fmaf(w[r].x, t.x, w[r].y * t.y);
-    const float cy = fmaf(w[r].x, t.y, -w[r].y * t.x);
-    const bool neg = __popc(r & zr) & 1;
-    z.x += neg ? -cx : cx;
-    z.y += neg ? -cy : cy;
+    const float term = IMZ ? fmaf(w[r].x, t.y, -w[r].y * t.x) : fmaf(w[r].x, t.x, w[r].y * t.y);
+    z += (__popc(r & zr) & 1) ? -term : term;
   }
   return z;
 }
@@ -309,25 +314,43 @@ __device__ __forceinline__ float2 prot_dot(const float2 (&v)[1 << R], const floa
 #define TCG_X16(M) M(0) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11) M(12) M(13) M(14) M(15)
 
 template <int R>
-__device__ __forceinline__ void dispatch_prot(int x, float2 (&v)[1 << R], float c, float2 q, int zr) {
-#define TCG_PR(XX) case XX: if ((XX) < (1 << R)) prot_rt<R, ((XX) < (1 << R) ? (XX) : 0)>(v, c, q, zr); break;
-  switch (x) {
-    TCG_X16(TCG_PR)
-    default: break;
-  }
+__device__ __forceinline__ void dispatch_prot(int x, float2 (&v)[1 << R], float c, float qv, int zr, bool qim) {
+  if (qim) {
+#define TCG_PR(XX) case XX: if ((XX) < (1 << R)) prot_rt<R, ((XX) < (1 << R) ? (XX) : 0), true>(v, c, qv, zr); break;
+    switch (x) {
+      TCG_X16(TCG_PR)
+      default: break;
+    }
 #undef TCG_PR
+  } else {
+#define TCG_PR(XX) case XX: if ((XX) < (1 << R)) prot_rt<R, ((XX) < (1 << R) ? (XX) : 0), false>(v, c, qv, zr); break;
+    switch (x) {
+      TCG_X16(TCG_PR)
+      default: break;
+    }
+#undef TCG_PR
+  }
 }
 
 template <int R>
-__device__ __forceinline__ float2 dispatch_prot_dot(int x, const float2 (&v)[1 << R], const float2 (&w)[1 << R],
-                                                    int zr) {
-  float2 z = czero();
-#define TCG_PD(XX) case XX: if ((XX) < (1 << R)) z = prot_dot<R, ((XX) < (1 << R) ? (XX) : 0)>(v, w, zr); break;
-  switch (x) {
-    TCG_X16(TCG_PD)
-    default: break;
-  }
+__device__ __forceinline__ float dispatch_prot_dot(int x, const float2 (&v)[1 << R], const float2 (&w)[1 << R],
+                                                   int zr, bool imz) {
+  float z = 0.f;
+  if (imz) {
+#define TCG_PD(XX) case XX: if ((XX) < (1 << R)) z = prot_dot<R, ((XX) < (1 << R) ? (XX) : 0), true>(v, w, zr); break;
+    switch (x) {
+      TCG_X16(TCG_PD)
+      default: break;
+    }
 #undef TCG_PD
+  } else {
+#define TCG_PD(XX) case XX: if ((XX) < (1 << R)) z = prot_dot<R, ((XX) < (1 << R) ? (XX) : 0), false>(v, w, zr); break;
+    switch (x) {
+      TCG_X16(TCG_PD)
+      default: break;
+    }
+#undef TCG_PD
+  }
   return z;
 }
 
@@ -790,21 +813,24 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
 #pragma unroll
         for (int ri = 0; ri < R; ++ri)
           if (ly.rg[ri] & op.zmask) zr |= 1 << ri;
-        const float2 ph = ypow(op.nY);
-        float2 q = cmul(make_float2(0.f, -cs.y), ph);
-        if (sg) q = make_float2(-q.x, -q.y);
+        // q = (0, -s) (-i)^nY: (0, -s), (-s, 0), (0, s), (s, 0) for nY % 4 = 0..3
+        const int ny = op.nY & 3;
+        const bool qim = (ny & 1) == 0;
+        float qv = (ny <= 1) ? -cs.y : cs.y;
+        if (sg) qv = -qv;
         if (MODE == MODE_FWD) {
-          dispatch_prot<R>(op.xreg, v, cs.x, q, zr);
+          dispatch_prot<R>(op.xreg, v, cs.x, qv, zr, qim);
         } else if (MODE == MODE_BWD) {
           if (op.slot >= 0) {
-            const float2 z = dispatch_prot_dot<R>(op.xreg, v, w, zr);
-            const float2 pt = sg ? make_float2(-ph.x, -ph.y) : ph;
-            const float2 t = warp_sum(make_float2(fmaf(pt.x, z.y, pt.y * z.x), 0.f), nl);
+            // g = Im(pt z), pt = (+-)(-i)^nY: z.y, -z.x, -z.y, z.x for nY % 4 = 0..3
+            float g = dispatch_prot_dot<R>(op.xreg, v, w, zr, qim);
+            if (ny == 1 || ny == 2) g = -g;
+            if (sg) g = -g;
+            const float2 t = warp_sum(make_float2(g, 0.f), nl);
             if (lane == 0) sm_slot[warp * A.max_slots + op.slot] = t;
           }
-          const float2 mq = make_float2(-q.x, -q.y);
-          dispatch_prot<R>(op.xreg, v, cs.x, mq, zr);
-          dispatch_prot<R>(op.xreg, w, cs.x, mq, zr);
+          dispatch_prot<R>(op.xreg, v, cs.x, -qv, zr, qim);
+          dispatch_prot<R>(op.xreg, w, cs.x, -qv, zr, qim);
         }
       } else if (kind == OP_ZRUN) {
         if (MODE == MODE_MEAS) {
