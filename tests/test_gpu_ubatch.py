@@ -133,3 +133,33 @@ def test_uneven_batch_c4_graph_replay_vs_per_circuit_engine(tc):
         v, g = K.value_and_grad(f)(torch.tensor(params[i], dtype=torch.float32, device="cuda"))
         assert abs(v.item() - e1[i].item()) <= 1e-5 * max(1.0, abs(v.item()))
         np.testing.assert_allclose(gs[i].cpu().numpy(), g.cpu().numpy(), atol=1e-4)
+
+
+def test_uneven_batch_small_circuits_and_errors(tc):
+    """Circuits down to 6 qubits with the smallest tile width, a circuit
+    with no parameters, and the error mapping of invalid batches."""
+    from tensorcircuit_gb300 import batch, templates
+
+    def fixed(c, params):
+        c.h(0)
+        c.cnot(0, 3)
+        c.rzz(1, 5, theta=0.4)
+
+    rng = np.random.default_rng(3)
+    specs = [batch.qaoa_spec(6, templates.random_regular_graph(3, 6, rng), 2),
+             (6, fixed, 0, [(1.0, {"z": [0, 3]}), (0.5, {"x": [1]})], 0.0),
+             batch.qaoa_spec(8, templates.random_regular_graph(3, 8, rng), 1)]
+    ub = batch.UnevenBatch(specs, tile_bits=6, graph=False)
+    params = [rng.uniform(0, np.pi, s[2]).astype(np.float32) for s in specs]
+    e, g = ub.value_and_grad(params)
+    ub.check()
+    want0, g0 = _qaoa_oracle(6, [tuple(t["z"]) for _, t in specs[0][3]], 2, params[0].astype(np.float64))
+    assert abs(e[0].item() - want0) < 1e-5
+    np.testing.assert_allclose(ub.split(g)[0].cpu().numpy(), g0, atol=2e-5)
+    psi = sv.run_circuit(6, [("h", (0,), {}), ("cnot", (0, 3), {}), ("rzz", (1, 5), {"theta": 0.4})])
+    want1 = (sv.expectation_ps(psi, 6, z=[0, 3]) + 0.5 * sv.expectation_ps(psi, 6, x=[1])).real
+    assert abs(e[1].item() - want1) < 1e-5
+    with pytest.raises(ValueError):
+        batch.UnevenBatch(specs, tile_bits=7, graph=False)  # wider than the 6-qubit circuits
+    with pytest.raises(ValueError):
+        ub.value_and_grad(np.zeros(3, np.float32))  # wrong parameter count
