@@ -971,6 +971,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+// Bulk L2 prefetch of one 256-byte run (TMA unit; a hint, never faults on
+// a valid address).  Runs are 256-byte aligned.
+__device__ __forceinline__ void prefetch_l2_run(const float2* p) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], 256;" ::"l"(__cvta_generic_to_global(p)) : "memory");
+}
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -988,10 +993,16 @@ __global__ void __launch_bounds__(256, LITE ? 2 : 1) batch_kernel(BatchLaunch BL
   extern __shared__ __align__(16) float2 smem_raw[];
   __shared__ long long s_item;
   __shared__ int s_seg;
+  // L2 prefetch of the chunk's next tile: its runs, psi (and mu)
+  __shared__ const float2* s_pf_psi;
+  __shared__ const float2* s_pf_mu;
+  __shared__ const uint32_t* s_pf_runs;
+  __shared__ int s_pf_n;
   long long chunk_next = 0, chunk_end = 0;  // thread 0: rest of the dequeued chunk
   int last_seg = 0;
   for (;;) {
     if (threadIdx.x == 0) {
+      s_pf_n = 0;
       if (chunk_next >= chunk_end) {
         chunk_next = (long long)atomicAdd(BL.queue, (unsigned)kBatchChunk);
         chunk_end = chunk_next + kBatchChunk;
@@ -1016,6 +1027,24 @@ __global__ void __launch_bounds__(256, LITE ? 2 : 1) batch_kernel(BatchLaunch BL
           seg = lo;
         }
         last_seg = seg;
+        // the next tile of the chunk: its data may still be rewritten before
+        // it is read (L2 stays coherent), so the prefetch is only a hint
+        const long long nxt = chunk_next;
+        if (nxt < chunk_end && nxt < BL.nitems) {
+          int ns = seg;
+          while (ns + 1 < BL.nsegs && BL.segs[ns + 1].item0 <= nxt) ++ns;
+          const BatchSeg& q = BL.segs[ns];
+          const BatchCirc& qc = BL.circ[q.circ];
+          const DevPass& qp = qc.prog.passes[q.pass];
+          const uint32_t t = (uint32_t)(nxt - q.item0);
+          uint32_t base = 0;
+          for (int i = 0; i < qp.nnonlocal; ++i)
+            if ((t >> i) & 1u) base |= 1u << qp.nlbits[i];
+          s_pf_psi = BL.psi + qc.state_off + base;
+          s_pf_mu = BL.mu ? BL.mu + qc.state_off + base : nullptr;
+          s_pf_runs = qc.prog.runs + qp.runs_off;
+          s_pf_n = 1 << (qp.L - kLo);
+        }
         const unsigned need = BL.segs[seg].need;
         const unsigned* dn = BL.done + BL.segs[seg].circ;
         if (need > 0 && ld_acquire_u32(dn) < need && ld_acquire_u32(BL.err) == 0u) {
@@ -1039,6 +1068,17 @@ __global__ void __launch_bounds__(256, LITE ? 2 : 1) batch_kernel(BatchLaunch BL
     const long long item = s_item;
     const int seg = s_seg;
     if (seg < 0) break;
+    {
+      const int pn = s_pf_n;
+      const float2* pp = s_pf_psi;
+      const float2* pm = s_pf_mu;
+      const uint32_t* pr = s_pf_runs;
+      for (int k = threadIdx.x; k < pn; k += blockDim.x) {
+        const uint32_t off = __ldg(pr + k);  // one 2^kLo-amplitude (256-byte) run
+        prefetch_l2_run(pp + off);
+        if (pm) prefetch_l2_run(pm + off);
+      }
+    }
     const BatchSeg sg = BL.segs[seg];
     const BatchCirc& C = BL.circ[sg.circ];
     PassArgs A;
