@@ -97,8 +97,9 @@ def _pauli_decompose_uncached(m: np.ndarray) -> Optional[List[int]]:
 class _Op:
     """One recorded gate.
 
-    kind: "const" (numpy matrix), "fam" (parameterized family), "any"
-    (user torch matrix), "exp1"/"exp" (exponential of a given hermitian)."""
+    kind: "const" (numpy matrix), "fam" (parameterized family), "prot"
+    (Pauli rotation: data = (theta, scale, Pauli codes)), "any" (user torch
+    matrix), "exp1"/"exp" (exponential of a given hermitian)."""
 
     __slots__ = ("kind", "name", "qubits", "data", "diag", "nq")
 
@@ -117,7 +118,8 @@ class _PlanEntry:
     def __init__(self, plan: eng.GatePlan, const_block: Optional[np.ndarray], groups: List[Any], nmat: int,
                  gates_c: Optional[List[Any]] = None) -> None:
         self.plan = plan
-        self.gates_c = gates_c or []  # (kind, qubits, mat_off, grad_off) per gate
+        # (kind, qubits, mat_off, grad_off[, Pauli codes]) per gate
+        self.gates_c = gates_c or []
         # Pauli terms the last circuit of this structure asked for, in order
         self.last_terms: Optional[List[Tuple[int, int]]] = None
         self.const_np = const_block
@@ -188,7 +190,6 @@ def _build_entry(n_eng: int, ops: Sequence[_Op]) -> _PlanEntry:
     mat_off: Dict[int, int] = dict(const_off)
     grad_off: Dict[int, int] = {}
     glist = []
-    prot_offs: List[int] = []
     for k in order:
         idx = groups[k]
         op0 = ops[idx[0]]
@@ -200,8 +201,6 @@ def _build_entry(n_eng: int, ops: Sequence[_Op]) -> _PlanEntry:
             mat_off[i] = off + j * E
             if ops[i].nq <= 2 or ops[i].kind == "prot":
                 grad_off[i] = off + j * E
-            if ops[i].kind == "prot":
-                prot_offs.append(off + j * E)
         off += E * len(idx)
         glist.append((k, idx, E))
     gates_c = []
@@ -213,9 +212,7 @@ def _build_entry(n_eng: int, ops: Sequence[_Op]) -> _PlanEntry:
             gates_c.append((kind, op.qubits, mat_off[i], grad_off.get(i, -1)))
     plan = eng.GatePlan(n_eng, gates_c, off)
     const_block = np.concatenate(const_mats) if const_mats else None
-    entry = _PlanEntry(plan, const_block, glist, off, gates_c)
-    entry.prot_offs = np.asarray(prot_offs, dtype=np.int64)
-    return entry
+    return _PlanEntry(plan, const_block, glist, off, gates_c)
 
 
 def _stack_scalars(vals: Sequence[Any], dev: torch.device) -> torch.Tensor:
