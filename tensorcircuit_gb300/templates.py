@@ -16,6 +16,7 @@ engine's Circuit and the CPU oracle build the same circuits.
 from typing import Any, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
+import torch
 
 from . import gates as G
 
@@ -43,8 +44,12 @@ def hea_nparams(n: int, nlayers: int) -> int:
 
 
 def apply_hea(c: Any, n: int, nlayers: int, params: Any) -> Any:
+    # one unbind instead of a select per gate: under autograd its backward
+    # is a single stack, where per-gate selects each scatter into a zero
+    # tensor of all parameters
+    ps = params.unbind(-1) if isinstance(params, torch.Tensor) and params.dim() == 1 else params
     for name, q, k in hea_layout(n, nlayers):
-        getattr(c, name)(*q, theta=params[k])
+        getattr(c, name)(*q, theta=ps[k])
     return c
 
 
