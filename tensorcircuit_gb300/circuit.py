@@ -314,7 +314,7 @@ class Circuit:
         # circuit with the same structure uses the list as its prediction
         self._req_terms: List[Tuple[int, int]] = []
         self._pred_terms: Optional[List[Tuple[int, int]]] = None
-        self._term_batch: Optional[torch.Tensor] = None
+        self._term_batch: Optional[Tuple[torch.Tensor, ...]] = None
 
     # ------------------------------------------------------------------ gates
     def _norm_index(self, index: Sequence[int]) -> Tuple[int, ...]:
@@ -587,8 +587,9 @@ class Circuit:
         pred = self._pred_terms
         if pred is not None and len(pred) > 1 and i < len(pred) and pred[i] == term:
             if self._term_batch is None:
-                self._term_batch = eng.ExpectFn.apply(psi_eng, anchor, tuple(pred), run)
-            return self._term_batch[..., i]
+                # unbound once: the backward of all the slices is one stack
+                self._term_batch = eng.ExpectFn.apply(psi_eng, anchor, tuple(pred), run).unbind(-1)
+            return self._term_batch[i]
         return eng.ExpectFn.apply(psi_eng, anchor, (term,), run)[..., 0]
 
     def expectation_ps_batch(self, terms: Sequence[Dict[str, Sequence[int]]]) -> Tensor:
