@@ -679,6 +679,165 @@ def run_qaoa(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+MC_N, MC_LAYERS, MC_GAMMA, MC_SEED = 10, 4, 0.15, 7
+MC_TRAJ = 1024
+MC_NSTATUS = MC_LAYERS * (MC_N - 1) * 2
+MC_METRIC = "MC-noise trajectories/s, value+grad (n=10, 4 layers, 72 phase-damping channels, <Z5>)"
+MC_UNIT = "trajectories/s"
+MC_WORKLOAD = "mcnoise_n10_l4_phasedamping"
+
+
+def _mc_inputs():
+    rng = np.random.default_rng(MC_SEED)
+    params = rng.uniform(0, 2 * np.pi, (MC_LAYERS, MC_N)).astype(np.float32)
+    status = rng.random((MC_TRAJ, MC_NSTATUS), dtype=np.float32)
+    return params, status
+
+
+def mcnoise_energy(tc, params, status):
+    """examples/mcnoise_boost_v2.py:20-37 at n=10, 4 layers: H on all; per
+    layer cnot(i, i+1) then phase damping (gamma 0.15, a general Kraus
+    channel) on i and i+1; rx(params[j, i]) on all; <Z_5>."""
+    import torch
+
+    c = tc.Circuit(MC_N)
+    for i in range(MC_N):
+        c.H(i)
+    s = 0
+    for j in range(MC_LAYERS):
+        for i in range(MC_N - 1):
+            c.cnot(i, i + 1)
+            c.phasedamping(i, gamma=MC_GAMMA, status=status[s])
+            c.phasedamping(i + 1, gamma=MC_GAMMA, status=status[s + 1])
+            s += 2
+        for i in range(MC_N):
+            c.rx(i, theta=params[j, i])
+    return torch.real(c.expectation_ps(z=[MC_N // 2]))
+
+
+def _mc_cpu_worker(chunk):
+    from oracle import reference_algo as ra
+
+    params, status = _mc_inputs()
+    t0 = time.perf_counter()
+    for b in chunk:
+        ra.mcnoise_value_and_grad(MC_N, MC_LAYERS, MC_GAMMA, params, status[b], 1)
+    return time.perf_counter() - t0
+
+
+def cpu_mcnoise(per_core=48):
+    """Labelled torch restatement of the reference algorithm (per-gate
+    tensordot, general_kraus probabilities by contraction, taped AD), one
+    trajectory per call, spread over the host cores by a spawn pool."""
+    import multiprocessing as mp
+
+    cores = len(os.sched_getaffinity(0))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_mc_cpu_worker, [[b] for b in range(cores)])  # import + first-call warm-up
+        chunks = [list(range(w * per_core, (w + 1) * per_core)) for w in range(cores)]
+        t0 = time.perf_counter()
+        pool.map(_mc_cpu_worker, chunks)
+        dt = time.perf_counter() - t0
+    ntraj = cores * per_core
+    return {"value": ntraj / dt, "unit": MC_UNIT, "cores": cores, "kind": "port",
+            "sample": "%d trajectories (%d per core, %.1f s wall; labelled torch restatement of the reference "
+                      "algorithm: per-gate tensordot, general_kraus by contraction, taped AD)" %
+                      (ntraj, per_core, dt)}
+
+
+def run_mcnoise(args, rank, world):
+    """Monte-Carlo noise trajectories: ``MC_TRAJ`` status vectors (seed 7)
+    through ``K.vvag(f, argnums=params, vectorized_argnums=status)`` -- every
+    trajectory's <Z_5> and the parameter gradient summed over trajectories,
+    each general-Kraus channel one segment boundary of the batched sweep."""
+    import torch
+
+    import tensorcircuit_gb300 as tc
+    from tensorcircuit_gb300 import _native
+
+    tc.build()
+    lib = _native.load()
+    K_ = tc.set_backend("pytorch")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    params_np, status_np = _mc_inputs()
+    ntraj = args.trajectories
+    status_np = np.resize(status_np, (ntraj, MC_NSTATUS))
+    p_host = torch.from_numpy(params_np).pin_memory()
+    s_host = torch.from_numpy(status_np).pin_memory()
+    p_dev, s_dev = p_host.to(dev), s_host.to(dev)
+
+    def f(p, st):
+        return mcnoise_energy(tc, p, st)
+
+    eager = K_.vvag(f, argnums=0, vectorized_argnums=1)
+    # the reference's own trajectory examples jit the value_and_grad; here
+    # the jit replays the whole step (every segment) from one CUDA graph
+    step = eager if args.mc_eager else K_.jit(eager)
+    warmup = max(args.warmup, 3)
+    for _ in range(warmup + 1):
+        v, g = step(p_dev, s_dev)
+    torch.cuda.synchronize()
+    # engine kernels per step, counted on one eager call (a graph replay
+    # launches the same kernels without passing the host-side counter)
+    l0 = lib.tcg_launch_count()
+    eager(p_dev, s_dev)
+    torch.cuda.synchronize()
+    launches_per_step = lib.tcg_launch_count() - l0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(args.steps):
+            v, g = step(p_dev, s_dev)
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    vh = torch.empty((ntraj,), dtype=torch.float32).pin_memory()
+    gh = torch.empty(tuple(params_np.shape), dtype=torch.float32).pin_memory()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        v, g = step(p_host.to(dev, non_blocking=True), s_host.to(dev, non_blocking=True))
+        vh.copy_(v, non_blocking=True)
+        gh.copy_(g, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    # segments: one per channel plus the last; per segment and trajectory a
+    # forward pass (16 B/amp), the Pauli measurement (8), the cotangent
+    # accumulation (24) and the adjoint pass (32)
+    segs = MC_NSTATUS + 1
+    alg = segs * 80 * (1 << MC_N) * ntraj
+    peak, peak_kind = _peaks()
+    achieved = alg / (ms / 1e3) / 1e9
+    if rank != 0:
+        return
+    cpu = None if args.no_cpu else cpu_mcnoise()
+    line = {
+        "metric": MC_METRIC, "value": ntraj / (ms / 1e3), "unit": MC_UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64", "data": "synthetic",
+        "config": {"workload": MC_WORKLOAD, "trajectories": ntraj, "n_qubits": MC_N, "layers": MC_LAYERS,
+                   "channels_per_trajectory": MC_NSTATUS, "gamma": MC_GAMMA, "seed": MC_SEED,
+                   "jit": not args.mc_eager,
+                   "jit_capture_errors": None if args.mc_eager else step.capture_errors(),
+                   "l2": "no flush: %d trajectories x 8 KiB states stay in L2 (launch-latency bound)" % ntraj},
+        "roofline": {"bound": "hbm", "kernel": "all engine sweeps of one step (segment passes)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "alg_bytes_per_step": alg},
+        "cpu_baseline": cpu,
+        "e2e": {"value": ntraj / (ms_e2e / 1e3), "unit": MC_UNIT,
+                "h2d_bytes_per_step": int(params_np.nbytes + status_np.nbytes),
+                "d2h_bytes_per_step": int(ntraj * 4 + params_np.nbytes)},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches_per_step * args.steps),
+        "gpu_launches_per_step": int(launches_per_step),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_warmstart(args, rank, world):
     """Learned warm start: random-coupling open TFIM n=16, HEA depth 6 (186
     angles), Adam lr 0.02; training angles generated by the engine's batched
@@ -728,17 +887,20 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hea", choices=["hea", "brickwall", "qaoa", "warmstart"],
+    ap.add_argument("--workload", default="hea", choices=["hea", "brickwall", "qaoa", "warmstart", "mcnoise"],
                     help="hea: n=20 HEA batched vvag (default); brickwall: n=28 Haar brick wall; "
                          "qaoa: 512 uneven QAOA circuits in one persistent launch per sweep; "
-                         "warmstart: learned warm start for n=16 TFIM chains")
+                         "warmstart: learned warm start for n=16 TFIM chains; "
+                         "mcnoise: Monte-Carlo phase-damping trajectories, value+grad")
+    ap.add_argument("--trajectories", type=int, default=MC_TRAJ, help="mcnoise: trajectories per step")
+    ap.add_argument("--mc-eager", action="store_true", help="mcnoise: run the step eagerly instead of replaying it from a CUDA graph")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="hea: parameter vectors per step (64 is the configured workload; smaller "
                          "batches are for profiler captures)")
     ap.add_argument("--instances", type=int, default=8192, help="warmstart: training chains")
     ap.add_argument("--held-out", type=int, default=1000, help="warmstart: held-out chains")
     ap.add_argument("--epochs", type=int, default=200, help="warmstart: network training epochs")
-    ap.add_argument("--gen-steps", type=int, default=1000,
+    ap.add_argument("--gen-steps", type=int, default=2500,
                     help="warmstart: Adam steps that produce each training chain's target angles")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
@@ -762,6 +924,8 @@ def main():
         run_qaoa(args, rank, world)
     elif args.workload == "warmstart":
         run_warmstart(args, rank, world)
+    elif args.workload == "mcnoise":
+        run_mcnoise(args, rank, world)
     else:
         run_gb300_arm(args, rank, world)
     if world > 1:

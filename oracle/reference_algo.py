@@ -139,3 +139,51 @@ def qaoa_value_and_grad(n: int, edges: Sequence[Tuple[int, int]], p: int, params
 
     g, v = torch.func.grad_and_value(f)(torch.as_tensor(params, dtype=torch.float32))
     return float(v), g.numpy()
+
+
+def _pick_sign_rule(x: float, cum: Sequence[float]) -> int:
+    """int(sum_{i<l-1} sign(x - c_i) / 2 + (l - 1) / 2)
+    (tensorcircuit/circuit.py:541-556)."""
+    l = len(cum)
+    s = sum(float(np.sign(np.float32(x) - np.float32(c))) for c in cum[: l - 1])
+    return int(s / 2.0 + (l - 1) / 2.0)
+
+
+def mcnoise_value_and_grad(n: int, nlayer: int, gamma: float, params: np.ndarray, status: np.ndarray,
+                           threads: int) -> Tuple[float, np.ndarray]:
+    """One Monte-Carlo trajectory of the phase-damping circuit of
+    examples/mcnoise_boost_v2.py:20-37 (H on all; per layer cnot(i, i+1)
+    then phase damping on i and i+1 through general_kraus, then rx on every
+    qubit; <Z_{n/2}>), value and gradient by taped AD.  general_kraus as
+    tensorcircuit/circuit.py:635-694: p_k = ||K_k psi||^2 by contraction, the
+    sign-rule pick, K_r psi / (sqrt(p_r) + 1e-10)."""
+    torch.set_num_threads(threads)
+    h = torch.tensor([[1, 1], [1, -1]], dtype=C64) / np.sqrt(2)
+    cnot = torch.tensor([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=C64).reshape(2, 2, 2, 2)
+    k0 = torch.tensor([[1, 0], [0, np.sqrt(1 - gamma)]], dtype=C64)
+    k1 = torch.tensor([[0, 0], [0, np.sqrt(gamma)]], dtype=C64)
+    z = _PAULI["z"]
+
+    def f(prm: torch.Tensor) -> torch.Tensor:
+        psi = torch.zeros([2] * n, dtype=C64)
+        psi.view(-1)[0] = 1.0
+        for i in range(n):
+            psi = _apply(psi, h, (i,))
+        s = 0
+        for j in range(nlayer):
+            for i in range(n - 1):
+                psi = _apply(psi, cnot, (i, i + 1))
+                for q in (i, i + 1):
+                    v = [_apply(psi, k0, (q,)), _apply(psi, k1, (q,))]
+                    p = [torch.real(torch.sum(torch.conj(t) * t)) for t in v]
+                    cum = np.cumsum([float(t.detach()) for t in p], dtype=np.float32)
+                    r = _pick_sign_rule(float(status[s]), cum)
+                    psi = v[r] / (torch.sqrt(p[r]) + 1e-10).to(C64)
+                    s += 1
+            for i in range(n):
+                psi = _apply(psi, _rx(prm[j, i]), (i,))
+        phi = _apply(psi, z, (n // 2,))
+        return torch.real(torch.sum(torch.conj(psi) * phi))
+
+    g, v = torch.func.grad_and_value(f)(torch.as_tensor(params, dtype=torch.float32))
+    return float(v), g.numpy()

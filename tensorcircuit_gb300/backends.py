@@ -11,7 +11,7 @@ and their gradients come from one batched adjoint sweep.
 """
 
 from functools import partial
-from typing import Any, Callable, Optional, Sequence, Tuple, Union
+from typing import Any, Callable, List, Optional, Sequence, Tuple, Union
 
 import numpy as np
 import torch
@@ -80,9 +80,10 @@ class GraphJit:
                 g = torch.cuda.CUDAGraph()
                 with torch.cuda.graph(g):
                     out = self.f(*static_args)
-            except Exception:  # not capturable: stay eager
+            except Exception as exc:  # not capturable: stay eager
                 torch.cuda.synchronize()
                 ent["failed"] = True
+                ent["error"] = "%s: %s" % (type(exc).__name__, str(exc)[:300])
                 return self.f(*args)
             ent["graph"], ent["inputs"], ent["outputs"] = g, static_args, out
         src_leaves = pytree.tree_flatten(args)[0]
@@ -92,6 +93,10 @@ class GraphJit:
                 d.copy_(s, non_blocking=True)
         ent["graph"].replay()
         return pytree.tree_map(lambda t: t.clone() if isinstance(t, torch.Tensor) else t, ent["outputs"])
+
+    def capture_errors(self) -> List[str]:
+        """Why capture failed for the argument signatures that stayed eager."""
+        return [e["error"] for e in self.cache.values() if e.get("error")]
 
 
 class PyTorchBackend:

@@ -18,6 +18,7 @@ import torch
 
 from . import _native as nat
 from . import engine as eng
+from . import channels as _channels
 from . import gates
 from .quantum import sample2all, sample_int2bin
 
@@ -99,7 +100,9 @@ class _Op:
 
     kind: "const" (numpy matrix), "fam" (parameterized family), "prot"
     (Pauli rotation: data = (theta, scale, Pauli codes)), "any" (user torch
-    matrix), "exp1"/"exp" (exponential of a given hermitian)."""
+    matrix), "exp1"/"exp" (exponential of a given hermitian), "kraus" (one
+    operator of a Kraus set picked per trajectory: data = (set key, operator
+    stack [l, entries] on the device, pick index))."""
 
     __slots__ = ("kind", "name", "qubits", "data", "diag", "nq")
 
@@ -151,6 +154,8 @@ def _group_key(op: _Op) -> Any:
         return ("exp1", op.nq, op.data[2], op.diag)
     if op.kind == "exp":
         return ("exp", op.nq)
+    if op.kind == "kraus":
+        return ("kraus", op.nq, op.diag, op.data[0])
     raise ValueError(op.kind)
 
 
@@ -197,9 +202,11 @@ def _build_entry(n_eng: int, ops: Sequence[_Op]) -> _PlanEntry:
             E = 1
         else:
             E = (1 << op0.nq) if op0.diag else (1 << (2 * op0.nq))
+        # constant Kraus sets take no gradient
+        const_kraus = op0.kind == "kraus" and k[3][0] == "n"
         for j, i in enumerate(idx):
             mat_off[i] = off + j * E
-            if ops[i].nq <= 2 or ops[i].kind == "prot":
+            if (ops[i].nq <= 2 or ops[i].kind == "prot") and not const_kraus:
                 grad_off[i] = off + j * E
         off += E * len(idx)
         glist.append((k, idx, E))
@@ -282,7 +289,218 @@ def _group_block(key: Any, ops: Sequence[_Op], idx: Sequence[int], dev: torch.de
         theta = _stack_scalars([ops[i].data[0] for i in idx], dev)
         u = _stack_mats([ops[i].data[1] for i in idx], d, dev)
         return gates.build_exp_dense(theta, u)
+    if kind == "kraus":
+        rs = torch.stack([ops[i].data[2] for i in idx], -1).long()
+        if key[3][0] == "n":
+            # one shared constant set: a single gather for the whole group
+            return ops[idx[0]].data[1][rs]
+        return torch.stack([ops[i].data[1][r] for i, r in zip(idx, rs.unbind(-1))], -2)
     raise ValueError(kind)
+
+
+# ----------------------------------------------------------------------------
+# Monte-Carlo trajectory noise (tensorcircuit/circuit.py:354-764)
+# ----------------------------------------------------------------------------
+_PAULI_NP = [np.eye(2), np.array([[0, 1], [1, 0]]), np.array([[0, -1j], [1j, 0]]), np.diag([1.0, -1.0])]
+_KRAUS_DEV: Dict[Any, torch.Tensor] = {}
+
+
+def _kraus_mats(kraus: Sequence[Any], d: int) -> Tuple[List[Any], bool]:
+    """Kraus operators as d x d numpy (complex128) or torch (complex64)
+    matrices; the flag says whether any is a torch tensor."""
+    out: List[Any] = []
+    is_t = False
+    for k in kraus:
+        t = k.tensor if isinstance(k, gates.Gate) else k
+        if isinstance(t, torch.Tensor):
+            is_t = True
+            out.append(t.to(C64).reshape(d, d))
+        else:
+            a = np.asarray(t, dtype=np.complex128)
+            if a.size != d * d:
+                raise ValueError("Kraus operator of size %d does not act on %d qubits" % (a.size, d.bit_length() - 1))
+            out.append(a.reshape(d, d))
+    if not out:
+        raise ValueError("empty Kraus list")
+    return out, is_t
+
+
+def _kraus_device_set(mats: Sequence[np.ndarray], extra: np.ndarray, diag: bool,
+                      dev: torch.device) -> Tuple[Any, torch.Tensor]:
+    """Content key and cached device stack [l, entries] of a constant set."""
+    stack = np.stack([np.diag(m) if diag else m.reshape(-1) for m in mats]).astype(np.complex64)
+    h = hashlib.sha1(stack.tobytes())
+    h.update(np.ascontiguousarray(extra).tobytes())
+    key = ("n", stack.shape, h.hexdigest())
+    t = _KRAUS_DEV.get((key, dev.index))
+    if t is None:
+        t = torch.as_tensor(stack, device=dev)
+        _KRAUS_DEV[(key, dev.index)] = t
+    return key, t
+
+
+_UK_PREP: Dict[Any, Any] = {}
+
+
+def _unitary_kraus_prep(mats: Sequence[np.ndarray], prob: Optional[Sequence[float]], d: int,
+                        dev: torch.device) -> Tuple[Any, torch.Tensor, torch.Tensor, bool]:
+    """For a constant set: (set key, device operator stack, device
+    cumulative probabilities, diagonal flag), memoised by content.  Without
+    ``prob`` the probabilities are tr(K^dag K)/d in float32 and each operator
+    is divided by sqrt(p) (a zero-probability operator stays zero)."""
+    pb = b"" if prob is None else np.asarray(prob, dtype=np.float32).tobytes()
+    fp = (d, dev.index, pb, prob is None, b"".join(np.ascontiguousarray(m).tobytes() for m in mats))
+    r = _UK_PREP.get(fp)
+    if r is None:
+        if len(_UK_PREP) > 4096:
+            _UK_PREP.clear()
+        if prob is None:
+            m64 = [m.astype(np.complex64) for m in mats]
+            p = np.array([np.real(np.trace(m.conj().T @ m)) / d for m in m64], dtype=np.float32)
+            mats = [m / np.sqrt(float(q)) if q > 0 else np.zeros_like(m) for m, q in zip(mats, p)]
+        else:
+            p = np.asarray(prob, dtype=np.float32).reshape(-1)
+        if len(p) != len(mats):
+            raise ValueError("prob has %d entries for %d Kraus operators" % (len(p), len(mats)))
+        cum_np = np.cumsum(p, dtype=np.float32)
+        diag = all(gates.is_diagonal(m) for m in mats)
+        key, kdev = _kraus_device_set(mats, cum_np, diag, dev)
+        r = (key, kdev, torch.as_tensor(cum_np, device=dev), diag)
+        _UK_PREP[fp] = r
+    return r
+
+
+def _pick(status: Any, cum: torch.Tensor, dev: torch.device) -> torch.Tensor:
+    """The Kraus pick of tensorcircuit/circuit.py:541-556: for a uniform x
+    and cumulative probabilities c, int(sum_{i<l-1} sign(x - c_i) / 2 +
+    (l - 1) / 2) -- the number of c_i below x plus half the number equal to
+    x, truncated.  ``cum`` may carry batch dimensions."""
+    if status is None:
+        x = torch.rand((), device=dev)
+    elif isinstance(status, torch.Tensor):
+        x = torch.real(status) if status.is_complex() else status
+        x = x.to(device=dev, dtype=torch.float32)
+        if x.dim() > 0 and x.numel() == 1:
+            x = x.reshape(())
+    else:
+        x = torch.full((), float(np.real(np.asarray(status).reshape(-1)[0])), dtype=torch.float32, device=dev)
+    l = cum.shape[-1]
+    if l == 1:
+        return torch.zeros_like(x, dtype=torch.int32)
+    s = torch.sign(x.unsqueeze(-1) - cum[..., : l - 1]).sum(-1)
+    return (s * 0.5 + (l - 1) * 0.5).to(torch.int32)
+
+
+_STRINGS: Dict[int, List[Tuple[Tuple[int, ...], np.ndarray]]] = {}
+
+
+def _pauli_strings(k: int) -> List[Tuple[Tuple[int, ...], np.ndarray]]:
+    """All 4^k Pauli strings on k gate legs (codes per leg, matrix), the
+    first leg outermost."""
+    out = _STRINGS.get(k)
+    if out is None:
+        out = [((), np.ones((1, 1)))]
+        for _ in range(k):
+            out = [(c + (j,), np.kron(m, _PAULI_NP[j])) for c, m in out for j in range(4)]
+        _STRINGS[k] = out
+    return out
+
+
+# Device-side constants are made once and reused: a host-to-device copy from
+# pageable memory would wait for the stream (and cannot be captured into a
+# CUDA graph).
+_DEV_CONST: Dict[Any, torch.Tensor] = {}
+
+
+def _dev_const(m: np.ndarray, dev: torch.device) -> torch.Tensor:
+    key = (m.tobytes(), m.shape, dev.index)
+    t = _DEV_CONST.get(key)
+    if t is None:
+        if len(_DEV_CONST) > 4096:
+            _DEV_CONST.clear()
+        t = torch.as_tensor(np.asarray(m, dtype=np.complex64), device=dev)
+        _DEV_CONST[key] = t
+    return t
+
+
+def _pauli_stack(k: int, dev: torch.device) -> torch.Tensor:
+    return _dev_const(np.stack([s for _, s in _pauli_strings(k)]), dev)
+
+
+_ARANGE: Dict[Any, torch.Tensor] = {}
+
+
+def _arange(l: int, dev: torch.device) -> torch.Tensor:
+    t = _ARANGE.get((l, dev.index))
+    if t is None:
+        t = torch.arange(l, device=dev)
+        _ARANGE[(l, dev.index)] = t
+    return t
+
+
+_KRAUS_PREP: Dict[Any, Any] = {}
+
+
+def _kraus_prep(mats: Sequence[np.ndarray], k: int, dev: torch.device) -> Tuple[Any, torch.Tensor, torch.Tensor, bool]:
+    """For a constant Kraus set: (set key, device operator stack, device
+    matrix coef[i, s] = tr(K_i^dag K_i P_s) / 2^k of the Pauli expansion,
+    diagonal flag), memoised by content."""
+    fp = (k, dev.index, b"".join(np.ascontiguousarray(m).tobytes() for m in mats))
+    r = _KRAUS_PREP.get(fp)
+    if r is None:
+        if len(_KRAUS_PREP) > 4096:
+            _KRAUS_PREP.clear()
+        d = 1 << k
+        coef = np.array([[np.real(np.trace(m.conj().T @ m @ s)) / d for _, s in _pauli_strings(k)] for m in mats])
+        diag = all(gates.is_diagonal(m) for m in mats)
+        key, kdev = _kraus_device_set(mats, np.zeros(0), diag, dev)
+        r = (key, kdev, torch.as_tensor(coef.astype(np.float32), device=dev), diag)
+        _KRAUS_PREP[fp] = r
+    return r
+
+
+_SPECS: Dict[Any, Tuple[Tuple[int, int], ...]] = {}
+
+
+def _kraus_spec(idx: Tuple[int, ...], n_eng: int) -> Tuple[Tuple[int, int], ...]:
+    """The 4^k Pauli strings on qubits idx as (xmask, zmask) terms."""
+    spec = _SPECS.get((idx, n_eng))
+    if spec is None:
+        out = []
+        for codes, _ in _pauli_strings(len(idx)):
+            xs = [q for q, c in zip(idx, codes) if c == 1]
+            ys = [q for q, c in zip(idx, codes) if c == 2]
+            zs = [q for q, c in zip(idx, codes) if c == 3]
+            out.append(eng.pauli_masks(n_eng, xs, ys, zs))
+        spec = tuple(out)
+        _SPECS[(idx, n_eng)] = spec
+    return spec
+
+
+def _apply_local(psi: torch.Tensor, m: torch.Tensor, idx: Sequence[int], n: int) -> torch.Tensor:
+    """psi -> (m on qubits idx) psi for a per-trajectory, differentiable
+    operator ``m`` [..., d, d]; used only for Kraus operators given as
+    tensors that need gradients (the engine's adjoint sweep assumes the
+    operators it un-applies are unitary)."""
+    k = len(idx)
+    lead = psi.shape[:-1]
+    nl = len(lead)
+    if m.dim() > 2:
+        m = m.expand(lead + m.shape[-2:])
+    t = psi.reshape(lead + (2,) * n)
+    g = m.reshape(m.shape[:-2] + (2,) * (2 * k))
+    # contract the gate's input legs with the state's legs idx
+    letters = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
+    sl = letters[:nl]
+    st = list(letters[nl:nl + n])
+    outl = list(st)
+    gin = [st[q] for q in idx]
+    gout = list(letters[nl + n:nl + n + k])
+    for j, q in enumerate(idx):
+        outl[q] = gout[j]
+    gl = (sl if m.dim() > 2 else "") + "".join(gout) + "".join(gin)
+    r = torch.einsum("%s,%s->%s" % (gl, sl + "".join(st), sl + "".join(outl)), g, t)
+    return r.reshape(lead + (1 << n,))
 
 
 class Circuit:
@@ -315,6 +533,11 @@ class Circuit:
         self._req_terms: List[Tuple[int, int]] = []
         self._pred_terms: Optional[List[Tuple[int, int]]] = None
         self._term_batch: Optional[Tuple[torch.Tensor, ...]] = None
+        # general Kraus channels need the state in the middle of the circuit:
+        # the gates before one become a finished segment whose (rescaled)
+        # output state is the input of the gates after it
+        self._seg_input: Optional[torch.Tensor] = None
+        self._seg_ops = 0
 
     # ------------------------------------------------------------------ gates
     def _norm_index(self, index: Sequence[int]) -> Tuple[int, ...]:
@@ -454,6 +677,134 @@ class Circuit:
     def mpo(self, *index: int, **kws: Any) -> None:
         raise NotImplementedError("MPO gates are not supported by the statevector engine")
 
+    # ------------------------------------------------------------------ noise
+    def unitary_kraus(self, kraus: Sequence[Any], *index: int, prob: Optional[Sequence[float]] = None,
+                      status: Optional[Any] = None, name: Optional[str] = None) -> Tensor:
+        """Apply one operator of ``kraus``, picked by ``status`` (a uniform
+        in [0, 1); drawn when None) against the cumulative ``prob``
+        (tensorcircuit/circuit.py:473-560).  Without ``prob`` the
+        probabilities are tr(K^dag K)/d and each operator is divided by
+        sqrt(p).  Returns the pick as an int32 tensor.
+
+        The operator becomes one gate of the engine's plan whose matrix is
+        gathered per trajectory from the set, so a ``vmap`` over statuses
+        runs every trajectory in the same batched sweep.  A zero-probability
+        operator is stored as zero instead of 0/0."""
+        idx = self._norm_index(index)
+        d = 1 << len(idx)
+        mats, is_t = _kraus_mats(kraus, d)
+        dev = eng.device()
+        if not is_t and (prob is None or not any(isinstance(p, torch.Tensor) for p in
+                                                 (prob if _is_seq(prob) else [prob]))):
+            key, kdev, cum, diag = _unitary_kraus_prep(mats, prob, d, dev)
+        else:
+            kt = torch.stack([m.to(dev) if isinstance(m, torch.Tensor) else _dev_const(m, dev) for m in mats])
+            if prob is None:
+                p = torch.real(torch.einsum("kij,kij->k", kt.conj(), kt)) / d
+                pos = p > 0
+                inv = torch.where(pos, torch.rsqrt(torch.where(pos, p, torch.ones_like(p))), torch.zeros_like(p))
+                kt = kt * inv.to(C64).reshape(-1, 1, 1)
+            else:
+                p = torch.stack([q.to(device=dev, dtype=torch.float32) if isinstance(q, torch.Tensor)
+                                 else torch.full((), float(q), dtype=torch.float32, device=dev) for q in prob])
+            cum = torch.cumsum(p.to(torch.float32), -1)
+            diag = False
+            key, kdev = ("t", len(mats), d), kt.reshape(len(mats), d * d)
+        r = _pick(status, cum, dev)
+        ir = {"gatef": "unitary_kraus", "index": tuple(index), "name": name or "unitary_kraus", "split": None,
+              "mpo": False, "parameters": {"prob": prob, "status": status}}
+        self._record(_Op("kraus", "kraus", idx, (key, kdev, r), diag, len(idx)), ir)
+        return r
+
+    unitary_kraus2 = unitary_kraus
+
+    def general_kraus(self, kraus: Sequence[Any], *index: int, status: Optional[Any] = None,
+                      with_prob: bool = False, name: Optional[str] = None) -> Any:
+        """Monte-Carlo trajectory step of a general channel
+        (tensorcircuit/circuit.py:635-724): p_i = <psi|K_i^dag K_i|psi>,
+        the pick of ``unitary_kraus`` with those probabilities, and the
+        state continues as K_r psi / (sqrt(p_r) + 1e-10).
+
+        The p_i come from ONE measurement pass over the current state: K_i^dag
+        K_i expanded in the 4^k Pauli strings of its qubits, all measured by
+        the engine's Pauli kernel (differentiable through the adjoint sweep).
+        The gates so far become a finished segment; its rescaled output is
+        the next segment's input and K_r that segment's first gate (for
+        constant operators; operators given as tensors are applied to the
+        state directly, so that their gradients are exact).  Returns the
+        pick (and, with ``with_prob``, the list of p_i)."""
+        idx = self._norm_index(index)
+        k = len(idx)
+        d = 1 << k
+        mats, is_t = _kraus_mats(kraus, d)
+        dev = eng.device()
+        strings = _pauli_strings(k)
+        if is_t:
+            kt = torch.stack([m if isinstance(m, torch.Tensor) else _dev_const(m, dev) for m in mats]).to(dev)
+            mm = torch.einsum("kji,kjl->kil", kt.conj(), kt)
+            coef = torch.real(torch.einsum("kil,sli->ks", mm, _pauli_stack(k, dev))) / d
+        else:
+            key, kdev, coef, diag = _kraus_prep(mats, k, dev)
+        psi, psi_eng, anchor, run, n_eng = self._engine_state()
+        spec = _kraus_spec(idx, n_eng)
+        ev = torch.real(eng.ExpectFn.apply(psi_eng, anchor, spec, run))
+        p = ev @ coef.t()
+        r = _pick(status, torch.cumsum(p, -1), dev)
+        pr = torch.sum(torch.where(r.unsqueeze(-1) == _arange(len(mats), dev), p, 0.0), -1)
+        scale = (1.0 / (torch.sqrt(pr) + 1e-10)).to(C64)
+        ir = {"gatef": "general_kraus", "index": tuple(index), "name": name or "general_kraus", "split": None,
+              "mpo": False, "parameters": {"status": status}}
+        self._seg_ops += len(self._ops)
+        self._ops = []
+        if is_t:
+            kr = kt[r.long()]
+            self._seg_input = _apply_local(psi, kr, idx, self._nqubits) * scale.unsqueeze(-1)
+            self._qir.append(ir)
+            self._cache = None
+            self._req_terms = []
+            self._pred_terms = None
+            self._term_batch = None
+        else:
+            self._seg_input = psi * scale.unsqueeze(-1)
+            self._record(_Op("kraus", "kraus", idx, (key, kdev, r), diag, k), ir)
+        if with_prob:
+            return r, list(p.unbind(-1))
+        return r
+
+    apply_general_kraus = general_kraus
+
+    def depolarizing2(self, index: int, *, px: float, py: float, pz: float,
+                      status: Optional[Any] = None) -> float:
+        """X, Y, Z or I on ``index`` with probabilities px, py, pz, rest
+        (tensorcircuit/circuit.py:354-386)."""
+        self.unitary_kraus([gates.CONSTANT_GATES["x"], gates.CONSTANT_GATES["y"], gates.CONSTANT_GATES["z"],
+                            gates.CONSTANT_GATES["i"]], index, prob=[px, py, pz, 1 - px - py - pz],
+                           status=status)
+        return 0.0
+
+    def depolarizing_reference(self, index: int, *, px: float, py: float, pz: float,
+                               status: Optional[Any] = None) -> Tensor:
+        """As :meth:`depolarizing2`, returning the pick [0: X, 1: Y, 2: Z,
+        3: I] (tensorcircuit/circuit.py:389-445)."""
+        return self.unitary_kraus([gates.CONSTANT_GATES["x"], gates.CONSTANT_GATES["y"],
+                                   gates.CONSTANT_GATES["z"], gates.CONSTANT_GATES["i"]], index,
+                                  prob=[px, py, pz, 1 - px - py - pz], status=status)
+
+    @staticmethod
+    def apply_general_kraus_delayed(krausf: Any, is_unitary: bool = False) -> Any:
+        """Circuit method for a channel constructor
+        (tensorcircuit/circuit.py:727-745)."""
+
+        def apply(self: "Circuit", *index: int, status: Optional[Any] = None, name: Optional[str] = None,
+                  **vars: Any) -> None:
+            kraus = krausf(**vars)
+            if is_unitary:
+                self.unitary_kraus(kraus, *index, status=status, name=name)
+            else:
+                self.general_kraus(kraus, *index, status=status, name=name)
+
+        return apply
+
     # ------------------------------------------------------------------ state
     def _engine_state(self) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor, eng.Run, int]:
         if self._cache is not None:
@@ -475,20 +826,27 @@ class Circuit:
             b = _group_block(gkey, self._ops, idx, dev).to(C64)
             blocks.append(b.reshape(b.shape[:-2] + (b.shape[-2] * b.shape[-1],)))
         if blocks:
+            if len(blocks) > 1 and len({tuple(b.shape[:-1]) for b in blocks}) > 1:
+                # some groups carry batch dimensions (per-trajectory Kraus
+                # picks, batched parameters): broadcast the others to them
+                lead = torch.broadcast_shapes(*[b.shape[:-1] for b in blocks])
+                blocks = [b.expand(lead + b.shape[-1:]) for b in blocks]
             mats = blocks[0] if len(blocks) == 1 else torch.cat(blocks, -1)
         else:
             mats = torch.zeros(1, dtype=C64, device=dev)
         # input state
         N = 1 << n
-        if self.inputs is None:
+        inp = self._seg_input if self._seg_input is not None else self.inputs
+        if inp is None:
             psi0 = _basis0(n_eng, dev)
         else:
-            inp = self.inputs
             if isinstance(inp, gates.Gate):
                 inp = inp.tensor
             if not isinstance(inp, torch.Tensor):
                 inp = torch.as_tensor(np.asarray(inp, dtype=np.complex64))
-            inp = inp.to(device=dev, dtype=C64).reshape(-1)
+            inp = inp.to(device=dev, dtype=C64)
+            if inp.shape[-1] != N:
+                inp = inp.reshape(-1)  # the [2] * n leg form
             if inp.shape[-1] != N:
                 raise ValueError("inputs has %d amplitudes, %d qubits need %d" % (inp.shape[-1], n, N))
             if pad:
@@ -525,6 +883,8 @@ class Circuit:
     def matrix(self) -> Tensor:
         """The circuit unitary, from running the plan on all 2^n basis states
         as one batch."""
+        if self._seg_input is not None:
+            raise ValueError("a circuit with general Kraus channels has no unitary")
         n = self._nqubits
         dev = eng.device()
         c = Circuit(n, inputs=torch.eye(1 << n, dtype=C64, device=dev))
@@ -753,7 +1113,7 @@ class Circuit:
         return self._qir
 
     def __len__(self) -> int:
-        return len(self._ops)
+        return self._seg_ops + len(self._ops)
 
     def gate_count(self) -> int:
         return len(self._qir)
@@ -826,3 +1186,9 @@ for _a in gates.gate_aliases:
     for _alias in _a[1:]:
         setattr(Circuit, _alias, getattr(Circuit, _a[0]))
         setattr(Circuit, _alias.upper(), getattr(Circuit, _a[0].upper()))
+
+# channel methods (tensorcircuit/circuit.py:747-764): depolarizing and
+# generaldepolarizing through unitary_kraus, the others through general_kraus
+for _c in _channels.channels:
+    setattr(Circuit, _c, Circuit.apply_general_kraus_delayed(getattr(_channels, _c + "channel"),
+                                                             is_unitary=_c in _channels.UNITARY_CHANNELS))

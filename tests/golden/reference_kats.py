@@ -110,3 +110,31 @@ VVAG = dict(src="tests/test_backends.py:426-476", n=4, nlayers=3, batch=8, atol=
 # tests/test_quantum.py:495-502 -- ps2xyz / xyz2ps
 PS_XYZ = dict(src="tests/test_quantum.py:495-502",
               xyz={"x": [1], "z": [2]}, ps=[0, 1, 3], ps6=[0, 1, 3, 0, 0, 0])
+
+# tests/test_circuit.py:1595-1640 -- general_kraus on |++>: operators
+# sqrt(.5)|0><0|, sqrt(.5)|1><1|, sqrt(.5) I have probabilities .25/.25/.5;
+# status .3 picks 1 (qubit 0 -> |1>), status .8 picks 2 (identity)
+GENERAL_KRAUS = dict(
+    src="tests/test_circuit.py:1595-1640", n=2, pre=[("h", (0,), {}), ("h", (1,), {})],
+    kraus=[np.sqrt(0.5) * np.array([[1.0, 0], [0, 0]]), np.sqrt(0.5) * np.array([[0, 0], [0, 1.0]]),
+           np.sqrt(0.5) * np.eye(2)],
+    status=[0.3, 0.8], picks=[1, 2], z=[-1.0, 0.0], probs=[0.25, 0.25, 0.5], atol=1e-5,
+)
+
+# tests/test_circuit.py:1439-1446 -- the registered reset channel on |+>
+# with status .8 leaves amplitude 1 on |00>
+RESET = dict(src="tests/test_circuit.py:1439-1446", n=2, pre=[("h", (0,), {})], status=0.8, amp0=1.0,
+             atol=1e-9)
+
+# tests/test_channels.py:24-45 -- Kraus completeness of the channel
+# constructors, and isotropic(0.3, 2) == general(0.02, 2)
+CHANNEL_IDENTITY = dict(src="tests/test_channels.py:24-45",
+                        cases=[("depolarizing", (0.1, 0.15, 0.2)), ("amplitudedamping", (0.25, 0.3)),
+                               ("phasedamping", (0.6,)), ("reset", ()), ("generaldepolarizing", (0.1, 1)),
+                               ("generaldepolarizing", ([0.1, 0.1, 0.1], 1)), ("generaldepolarizing", (0.02, 2))],
+                        iso=((0.02 * 15, 2), (0.02, 2)), atol=1e-5)
+
+# tests/test_circuit.py:119-238 -- depolarizing trajectories keep the state
+# normalised (n=5: H on all, cnot ring, one noise op per qubit, then cz ring
+# or X on all); the reference asserts norm 1 within 1e-4
+DEPOLARIZING_NORM = dict(src="tests/test_circuit.py:119-238", n=5, probs=[0.2, 0.2, 0.2, 0.4], p=0.2, atol=1e-4)
