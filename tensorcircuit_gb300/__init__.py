@@ -13,9 +13,10 @@ Usage mirrors the reference::
 
 __version__ = "0.1.0"
 
-from . import gates, interfaces, quantum, torchnn
+from . import channels, gates, interfaces, quantum, torchnn
 from .backends import backend
 from .circuit import Circuit
+from .densitymatrix import DMCircuit, DMCircuit2, DMCircuit_reference
 from .cons import (
     dtypestr,
     get_backend,
@@ -32,7 +33,8 @@ from .cons import (
 from .gates import Gate
 
 __all__ = [
-    "Circuit", "Gate", "backend", "gates", "quantum", "set_backend", "set_dtype", "set_contractor",
+    "Circuit", "DMCircuit", "DMCircuit2", "DMCircuit_reference", "Gate", "backend", "channels", "gates",
+    "quantum", "set_backend", "set_dtype", "set_contractor",
     "get_backend", "get_dtype", "runtime_backend", "runtime_dtype", "runtime_contractor", "dtypestr",
     "rdtypestr", "set_tensornetwork_backend",
 ]

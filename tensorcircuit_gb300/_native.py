@@ -228,6 +228,10 @@ def check(status: int, what: str = "") -> None:
 
 
 def ptr(t: Any) -> int:
+    # a lazily conjugated / negated view shares the raw buffer of its base:
+    # the kernels would read the unconjugated values
+    if t.is_conj() or t.is_neg():
+        raise ValueError("a conjugate or negative view reached the engine; resolve it first")
     return int(t.data_ptr())
 
 

@@ -104,15 +104,19 @@ class _Op:
     operator of a Kraus set picked per trajectory: data = (set key, operator
     stack [l, entries] on the device, pick index))."""
 
-    __slots__ = ("kind", "name", "qubits", "data", "diag", "nq")
+    __slots__ = ("kind", "name", "qubits", "data", "diag", "nq", "conj")
 
-    def __init__(self, kind: str, name: str, qubits: Tuple[int, ...], data: Any, diag: bool, nq: int) -> None:
+    def __init__(self, kind: str, name: str, qubits: Tuple[int, ...], data: Any, diag: bool, nq: int,
+                 conj: bool = False) -> None:
         self.kind = kind
         self.name = name
         self.qubits = qubits
         self.data = data
         self.diag = diag
         self.nq = nq
+        # the gate's matrix is the complex conjugate of the one its data
+        # builds (the column-side twin of a density-matrix gate)
+        self.conj = conj
 
 
 class _PlanEntry:
@@ -144,6 +148,11 @@ _entries: Dict[Any, _PlanEntry] = {}
 
 
 def _group_key(op: _Op) -> Any:
+    k = _group_key_plain(op)
+    return k + ("*",) if op.conj else k
+
+
+def _group_key_plain(op: _Op) -> Any:
     if op.kind == "prot":
         return ("prot", op.data[1])
     if op.kind == "fam":
@@ -260,6 +269,12 @@ def _stack_mats(vals: Sequence[Any], d: int, dev: torch.device) -> torch.Tensor:
 
 
 def _group_block(key: Any, ops: Sequence[_Op], idx: Sequence[int], dev: torch.device) -> torch.Tensor:
+    if key[-1] == "*":
+        # a physical conjugate (the engine reads the raw buffer, which a
+        # lazily conjugated view would leave unconjugated), built from
+        # real/imag so that vmap batches it
+        b = _group_block(key[:-1], ops, idx, dev).to(C64)
+        return torch.complex(b.real, -b.imag)
     kind = key[0]
     if kind == "prot":
         return gates.build_prot(_stack_scalars([ops[i].data[0] for i in idx], dev), key[1])
@@ -520,6 +535,8 @@ class Circuit:
         if nqubits < 1:
             raise ValueError("a circuit needs at least one qubit")
         self._nqubits = nqubits
+        # qubits of the vector the engine evolves (2n for a density matrix)
+        self._nvec = nqubits
         self.inputs = inputs
         self.mps_inputs = None
         self.split = split
@@ -790,6 +807,128 @@ class Circuit:
                                    gates.CONSTANT_GATES["z"], gates.CONSTANT_GATES["i"]], index,
                                   prob=[px, py, pz, 1 - px - py - pz], status=status)
 
+    def _apply_nonunitary(self, m: Any, idx: Tuple[int, ...], ir: Dict[str, Any]) -> None:
+        """Apply a non-unitary operator (projector, superoperator): it starts
+        a new segment, so the adjoint sweep -- which un-applies a segment's
+        gates with G^dag -- stays exact for every other gate and passes
+        m^dag mu to the segment's input.  Constant operators become the
+        segment's first engine gate; tensors that need gradients are applied
+        by a torch contraction."""
+        psi = self._engine_state()[0]
+        self._seg_ops += len(self._ops)
+        self._ops = []
+        if isinstance(m, torch.Tensor):
+            self._seg_input = _apply_local(psi, m.to(device=psi.device, dtype=C64), idx, self._nvec)
+            self._qir.append(ir)
+            self._cache = None
+            self._req_terms = []
+            self._pred_terms = None
+            self._term_batch = None
+            return
+        m = np.asarray(m, dtype=np.complex128)
+        self._seg_input = psi
+        key = "m:" + hashlib.sha1(m.tobytes()).hexdigest()
+        Circuit._record(self, _Op("const", key, idx, m, gates.is_diagonal(m), len(idx)), ir)
+
+    def mid_measurement(self, index: int, keep: int = 0) -> Tensor:
+        """Post-select qubit ``index`` on |keep> (unnormalised), returning
+        ``keep`` as an int32 tensor (tensorcircuit/circuit.py:302-348)."""
+        idx = self._norm_index([index])
+        proj = np.diag([1.0, 0.0]) if keep < 0.5 else np.diag([0.0, 1.0])
+        ir = {"gatef": "mid_measurement", "index": (index,), "name": "mid_measurement", "split": None,
+              "mpo": False, "parameters": {"keep": keep}}
+        self._apply_nonunitary(proj, idx, ir)
+        return torch.full((), int(keep >= 0.5), dtype=torch.int32, device=eng.device())
+
+    mid_measure = mid_measurement
+    post_select = mid_measurement
+    post_selection = mid_measurement
+
+    def cond_measurement(self, index: int, status: Optional[Any] = None) -> Tensor:
+        """Z measurement of qubit ``index`` that collapses the trajectory:
+        ``general_kraus`` with the two projectors (basecircuit.py:824-853).
+        Returns the outcome."""
+        return self.general_kraus([np.diag([1.0, 0.0]), np.diag([0.0, 1.0])], index, status=status,
+                                  name="measure")
+
+    cond_measure = cond_measurement
+
+    def select_gate(self, which: Any, kraus: Sequence[Any], *index: int) -> None:
+        """Apply ``kraus[which]`` for an int tensor ``which``
+        (abstractcircuit.py:1076-1095): one engine gate whose matrix row is
+        gathered per batch element."""
+        idx = self._norm_index(index)
+        d = 1 << len(idx)
+        mats, is_t = _kraus_mats(kraus, d)
+        dev = eng.device()
+        if is_t:
+            kt = torch.stack([m.to(dev) if isinstance(m, torch.Tensor) else _dev_const(m, dev) for m in mats])
+            key, kdev, diag = ("t", len(mats), d), kt.reshape(len(mats), d * d), False
+        else:
+            diag = all(gates.is_diagonal(m) for m in mats)
+            key, kdev = _kraus_device_set(mats, np.zeros(0), diag, dev)
+        if isinstance(which, torch.Tensor):
+            r = which.to(device=dev, dtype=torch.int32)
+        else:
+            r = torch.full((), int(which), dtype=torch.int32, device=dev)
+        ir = {"gatef": "select_gate", "index": tuple(index), "name": "select_gate", "split": None, "mpo": False,
+              "parameters": {"which": which}}
+        self._record(_Op("kraus", "kraus", idx, (key, kdev, r), diag, len(idx)), ir)
+
+    conditional_gate = select_gate
+
+    def _probability_vector(self) -> Tensor:
+        psi = self.wavefunction()
+        return torch.real(psi * torch.conj(psi))
+
+    def measure_jit(self, *index: int, with_prob: bool = False, status: Optional[Any] = None) -> Tuple[Tensor, Any]:
+        """Sequential Z measurement of ``index`` (basecircuit.py:371-441):
+        for the k-th qubit, pu = P(0 | earlier outcomes), outcome
+        int(sign(status[k] - pu + eps)/2 + 1/2) with eps = 0.31415926e-12,
+        and p multiplied by pu or 1 - pu.  The marginals come from one
+        probability vector summed over the unmeasured qubits."""
+        n = self._nqubits
+        idx = [int(i) if int(i) >= 0 else n + int(i) for i in index]
+        p = self._probability_vector()
+        dev = p.device
+        lead = p.shape[:-1]
+        t = p.reshape(lead + (2,) * n)
+        nl = len(lead)
+        rest = [nl + q for q in range(n) if q not in idx]
+        if rest:
+            t = t.sum(dim=rest)
+        # order the measured qubits as requested
+        order = sorted(range(len(idx)), key=lambda j: idx[j])
+        perm = list(range(nl)) + [nl + order.index(j) for j in range(len(idx))]
+        t = t.permute(perm)
+        if status is None:
+            u = torch.rand(lead + (len(idx),), device=dev)
+        else:
+            u = status if isinstance(status, torch.Tensor) else torch.as_tensor(np.asarray(status, dtype=np.float32))
+            u = torch.real(u).to(device=dev, dtype=torch.float32)
+        prob = torch.ones(lead, dtype=torch.float32, device=dev)
+        bits = []
+        cur = t
+        for k in range(len(idx)):
+            marg = cur.sum(dim=tuple(range(nl + 1, cur.dim()))) if cur.dim() > nl + 1 else cur
+            pu = marg[..., 0] / prob
+            s = torch.sign(u[..., k] - pu + 0.31415926e-12) / 2 + 0.5
+            bits.append(s)
+            prob = prob * (pu * (1 - 2 * s) + s)
+            # condition on the outcome: keep the slice of the drawn bit
+            one = (s > 0.5).reshape(lead + (1,) * (cur.dim() - nl - 1))
+            cur = torch.where(one, cur.select(nl, 1), cur.select(nl, 0))
+        sample = torch.stack(bits, -1)
+        if with_prob:
+            return sample, prob
+        return sample, -1.0
+
+    measure = measure_jit
+
+    def perfect_sampling(self, status: Optional[Any] = None) -> Tuple[Tensor, Tensor]:
+        """All qubits by ``measure_jit`` (basecircuit.py:359-369)."""
+        return self.measure_jit(*range(self._nqubits), with_prob=True, status=status)
+
     @staticmethod
     def apply_general_kraus_delayed(krausf: Any, is_unitary: bool = False) -> Any:
         """Circuit method for a channel constructor
@@ -810,7 +949,7 @@ class Circuit:
         if self._cache is not None:
             return self._cache  # type: ignore
         dev = eng.device()
-        n = self._nqubits
+        n = self._nvec
         n_eng = max(n, nat.MIN_QUBITS)
         pad = n_eng - n
         key = _struct_key(n_eng, self._ops)
@@ -1092,8 +1231,7 @@ class Circuit:
         x, y, z = list(x or []), list(y or []), list(z or [])
         if shots is None:
             return torch.real(self.expectation_ps(x=x, y=y, z=z))
-        psi = self.wavefunction()
-        c = Circuit(self._nqubits, inputs=psi)
+        c = self._measurement_copy()
         for i in x:
             c.H(i)
         for i in y:
@@ -1108,15 +1246,136 @@ class Circuit:
 
     sexpps = sample_expectation_ps
 
+    def _measurement_copy(self) -> "Circuit":
+        """A fresh circuit starting from this one's output state."""
+        return Circuit(self._nqubits, inputs=self.wavefunction())
+
     # ---------------------------------------------------------------- misc
     def to_qir(self) -> List[Dict[str, Any]]:
         return self._qir
 
+    # Entries that are trajectory draws or projections rather than gates;
+    # rebuilding a circuit from its qir (from_qir, inverse, to_circuit)
+    # leaves them out, as the reference's qir holds gates only.
+    _NON_GATE_QIR = ("unitary_kraus", "general_kraus", "mid_measurement", "select_gate")
+
+    @staticmethod
+    def _qir_name(d: Dict[str, Any]) -> str:
+        g = d.get("gatef")
+        if isinstance(g, str):
+            return g
+        if g is not None and hasattr(g, "n"):
+            return g.n
+        return d.get("name") or "any"
+
+    @classmethod
+    def from_qir(cls, qir: List[Dict[str, Any]], circuit_params: Optional[Dict[str, Any]] = None) -> "Circuit":
+        """Rebuild a circuit from its gate records (abstractcircuit.py:
+        366-425); ``nqubits`` defaults to one more than the largest index."""
+        params = dict(circuit_params or {})
+        if "nqubits" not in params:
+            params["nqubits"] = 1 + max((max(d["index"]) for d in qir if d.get("index")), default=0)
+        c = cls(**params)
+        return cls._apply_qir(c, qir)
+
+    @staticmethod
+    def _apply_qir(c: "Circuit", qir: List[Dict[str, Any]]) -> "Circuit":
+        for d in qir:
+            name = Circuit._qir_name(d)
+            if name in Circuit._NON_GATE_QIR:
+                continue
+            idx = tuple(d["index"])
+            if "gatef" not in d or d.get("gatef") is None:
+                c.apply_general_gate(d["gate"], *idx, name=d.get("name"))
+            elif "parameters" in d:
+                getattr(c, name)(*idx, **dict(d["parameters"]))
+            else:
+                getattr(c, name)(*idx)
+        return c
+
+    def append_from_qir(self, qir: List[Dict[str, Any]]) -> None:
+        self._apply_qir(self, qir)
+
+    def prepend(self, c: "Circuit") -> "Circuit":
+        """``c``'s gates, then this circuit's (abstractcircuit.py:1133-1146)."""
+        newc = type(self).from_qir(c.to_qir() + self.to_qir(), dict(self.circuit_param))
+        self.__dict__.update(newc.__dict__)
+        return self
+
+    def append(self, c: "Circuit", indices: Optional[List[int]] = None) -> "Circuit":
+        """This circuit's gates, then ``c``'s, with ``c``'s qubit i placed on
+        ``indices[i]`` (abstractcircuit.py:1148-1183)."""
+        qir = c.to_qir()
+        if indices is not None:
+            qir = [dict(d, index=tuple(indices[i] for i in d["index"])) for d in qir]
+        self._apply_qir(self, qir)
+        return self
+
+    def inverse(self, circuit_params: Optional[Dict[str, Any]] = None) -> "Circuit":
+        """The adjoint circuit: gates in reverse order, each inverted
+        (abstractcircuit.py:428-507): self-inverse constant gates repeat,
+        sd/td become s/t and s/t/wroot their adjoints, rotations negate
+        theta (iswap's default angle is 1), u/cu map (phi, lbd) to
+        (pi - lbd, pi - phi), ``any`` takes the conjugate transpose."""
+        params = dict(circuit_params or {})
+        params.setdefault("nqubits", self._nqubits)
+        c = type(self)(**params)
+        self_inverse = [g for g in gates.sgates if g not in ("wroot", "sd", "td", "s", "t")]
+        for d in reversed(self._qir):
+            name = self._qir_name(d)
+            if name in self._NON_GATE_QIR:
+                continue
+            idx = tuple(d["index"])
+            if d.get("gatef") is None:
+                # a general gate recorded by its matrix
+                m = d["gate"].tensor if isinstance(d.get("gate"), gates.Gate) else d.get("gate")
+                if isinstance(m, torch.Tensor):
+                    dd = int(round(m.numel() ** 0.5))
+                    m = torch.conj(m.reshape(dd, dd)).transpose(0, 1)
+                else:
+                    m = _to_np_matrix(m).conj().T
+                c.apply_general_gate(m, *idx, name=d.get("name"))
+                continue
+            if "parameters" not in d:
+                if name in self_inverse:
+                    getattr(c, name)(*idx)
+                elif name in ("sd", "td"):
+                    getattr(c, name[:-1])(*idx)
+                else:
+                    c.apply_general_gate(_to_np_matrix(gates.CONSTANT_GATES[name]).conj().T, *idx, name=name)
+                continue
+            p = dict(d["parameters"])
+            if name in ("u", "cu"):
+                phi, lbd = p.get("phi", 0.0), p.get("lbd", 0.0)
+                p["lbd"], p["phi"] = -phi + np.pi, -lbd + np.pi
+            elif name == "any":
+                u = p["unitary"]
+                u = u.tensor if isinstance(u, gates.Gate) else u
+                if isinstance(u, torch.Tensor):
+                    dd = int(round(u.numel() ** 0.5))
+                    p["unitary"] = torch.conj(u.reshape(dd, dd)).transpose(0, 1)
+                else:
+                    p["unitary"] = _to_np_matrix(u).conj().T
+            elif name == "multicontrol":
+                u = _to_np_matrix(p["unitary"])
+                p["unitary"] = u.conj().T
+            else:
+                p["theta"] = -p.get("theta", 1.0 if name == "iswap" else 0.0)
+            getattr(c, name)(*idx, **p)
+        return c
+
     def __len__(self) -> int:
         return self._seg_ops + len(self._ops)
 
-    def gate_count(self) -> int:
-        return len(self._qir)
+    def gate_count(self, gate_list: Optional[Union[str, Sequence[str]]] = None) -> int:
+        """Number of recorded gates, or of those named in ``gate_list``
+        (abstractcircuit.py gate_count)."""
+        if gate_list is None:
+            return len(self._qir)
+        if isinstance(gate_list, str):
+            gate_list = [gate_list]
+        names = set(gate_list)
+        return sum(1 for d in self._qir if self._qir_name(d) in names or d.get("name") in names)
 
     def engine_stats(self) -> Dict[str, int]:
         """Pass/stage counts of the plan the engine uses for this circuit."""

@@ -193,7 +193,9 @@ def _lead(*shapes: Tuple[int, ...]) -> Tuple[int, ...]:
 
 
 def _flat(t: torch.Tensor, lead: Tuple[int, ...], tail: int) -> torch.Tensor:
-    return t.expand(lead + (tail,)).reshape(-1, tail)
+    # conjugate / negative views (autograd produces them, e.g. the backward
+    # of conj) become physical here, before a raw pointer is taken
+    return t.resolve_conj().resolve_neg().expand(lead + (tail,)).reshape(-1, tail)
 
 
 def _bd(x: Optional[torch.Tensor], d: Optional[int]) -> Optional[torch.Tensor]:
@@ -408,6 +410,6 @@ def probability_native(psi: torch.Tensor) -> torch.Tensor:
     """|psi|^2 through the engine kernel (no autograd)."""
     lib = nat.load()
     p = torch.empty(psi.shape, dtype=torch.float32, device=psi.device)
-    src = psi.detach().contiguous()
+    src = psi.detach().resolve_conj().resolve_neg().contiguous()
     nat.check(lib.tcg_probability(nat.ptr(src), src.numel(), nat.ptr(p), _stream()), "probability")
     return p

@@ -138,3 +138,37 @@ CHANNEL_IDENTITY = dict(src="tests/test_channels.py:24-45",
 # normalised (n=5: H on all, cnot ring, one noise op per qubit, then cz ring
 # or X on all); the reference asserts norm 1 within 1e-4
 DEPOLARIZING_NORM = dict(src="tests/test_circuit.py:119-238", n=5, probs=[0.2, 0.2, 0.2, 0.4], p=0.2, atol=1e-4)
+
+# tests/test_dmcircuit.py -- density-matrix known answers
+_RHO0 = np.array([[0, 0, 0, 0], [0, 0.5, 0, -0.5j], [0, 0, 0, 0], [0, 0.5j, 0, 0.5]])
+_B1 = np.array([[0, 1.0j], [0, 0]])
+_B2 = np.array([[0, 0], [1.0j, 0]])
+_IB1, _IB2 = np.kron(np.eye(2), _B1), np.kron(np.eye(2), _B2)
+_RHO1 = _IB1 @ _RHO0 @ _IB1.conj().T + _IB2 @ _RHO0 @ _IB2.conj().T
+_IY = np.kron(np.eye(2), np.array([[0, -1.0j], [1.0j, 0]]))
+DM = dict(
+    gate=dict(src="tests/test_dmcircuit.py:19-24", n=3, z0=0.0, z1=-1.0, atol=1e-4),
+    state_inputs=dict(src="tests/test_dmcircuit.py:27-50", w1_z=(-1.0, -1.0, 1.0),
+                      w2=np.array([1, 0, 0, 1.0j]) / np.sqrt(2),
+                      answer=np.array([[0, 0, 0, 0], [0, 0.5, -0.5j, 0], [0, 0.5j, 0.5, 0], [0, 0, 0, 0]])),
+    dm_inputs=dict(src="tests/test_dmcircuit.py:53-71", rho0=_RHO0, b1=_B1, b2=_B2, rho1=_RHO1,
+                   rho2=_IY @ _RHO1 @ _IY.conj().T, atol=1e-4),
+    depolarizing=dict(src="tests/test_dmcircuit.py:108-128",
+                      ans=np.array([[0.4, 0, 0.4, 0], [0, 0.1, 0, 0.1], [0.4, 0, 0.4, 0], [0, 0.1, 0, 0.1]]),
+                      atol=1e-5),
+    mult_qubit_kraus=dict(src="tests/test_dmcircuit.py:131-175",
+                          xx=np.array([[0, 0, 0, 1], [0, 0, 1, 0], [0, 1, 0, 0], [1, 0, 0, 0]]) / np.sqrt(2),
+                          yz=np.array([[0, 0, -1.0j, 0], [0, 0, 0, 1.0j], [1.0j, 0, 0, 0], [0, -1.0j, 0, 0]])
+                          / np.sqrt(2), theta=0.2, grad=0.199, atol=1e-2),
+    noise_param_ad=dict(src="tests/test_dmcircuit.py:178-198", p=0.1, value=-0.6, grad=4.0, atol=1e-2),
+    ad_channel=dict(src="tests/test_dmcircuit.py:201-214", p=0.1, theta=0.1, value=0.7562, grad=-2.388,
+                    atol=1e-4),
+    inputs_pipeline=dict(src="tests/test_dmcircuit.py:217-226", value=0.0, atol=1e-5),
+    multicontrol=dict(src="tests/test_dmcircuit.py:247-254", value=0.93, atol=1e-6),
+    to_circuit=dict(src="tests/test_dmcircuit.py:257-268", dm=-0.6, pure=-1.0, atol=1e-5),
+    perfect_sampling=dict(src="tests/test_dmcircuit.py:289-303", status=[0.9, 0.5, 0.7], bits=[1, 0, 1],
+                          p=0.111375, atol=1e-5),
+    amplitude=dict(src="tests/test_dmcircuit.py:392-399", before=0.5, after=0.4, atol=1e-5),
+    cond_measure=dict(src="tests/test_dmcircuit.py:450-456", before=1.0, after=0.0, atol=1e-5),
+    sexpps=dict(src="tests/test_dmcircuit.py:474-502", y=1.0, atol=1e-5, shot_tol=0.015),
+)

@@ -214,7 +214,7 @@ def test_noisy_gradient_vs_finite_differences(tc):
     g = _np(pt.grad)
     p64 = params.astype(np.float64)
     e0, picks0 = _oracle_energy(p64, status, prog)
-    assert abs(float(e) - e0) <= 1e-5 * max(1.0, abs(e0))
+    assert abs(float(e.detach()) - e0) <= 1e-5 * max(1.0, abs(e0))
     eps = 1e-3
     for k in range(0, P, 3):
         pp, pm = p64.copy(), p64.copy()
