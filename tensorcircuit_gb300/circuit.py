@@ -1367,15 +1367,70 @@ class Circuit:
     def __len__(self) -> int:
         return self._seg_ops + len(self._ops)
 
+    @staticmethod
+    def standardize_gate(name: str) -> str:
+        """The canonical name of a gate alias (cx -> cnot, ccx -> toffoli)."""
+        name = name.lower()
+        for group in gates.gate_aliases:
+            if name in group:
+                return group[0]
+        return name
+
     def gate_count(self, gate_list: Optional[Union[str, Sequence[str]]] = None) -> int:
-        """Number of recorded gates, or of those named in ``gate_list``
-        (abstractcircuit.py gate_count)."""
+        """Number of recorded gates, or of those whose canonical name is in
+        ``gate_list`` (abstractcircuit.py:623-653)."""
         if gate_list is None:
             return len(self._qir)
         if isinstance(gate_list, str):
             gate_list = [gate_list]
-        names = set(gate_list)
-        return sum(1 for d in self._qir if self._qir_name(d) in names or d.get("name") in names)
+        names = {self.standardize_gate(g) for g in gate_list}
+        return sum(1 for d in self._qir if self._qir_name(d) in names)
+
+    def gate_count_by_condition(self, cond_func: Any) -> int:
+        return sum(1 for d in self._qir if cond_func(d))
+
+    def gate_summary(self) -> Dict[str, int]:
+        summary: Dict[str, int] = {}
+        for d in self._qir:
+            summary[d["name"]] = summary.get(d["name"], 0) + 1
+        return summary
+
+    # --------------------------------------------------------------- text I/O
+    def to_json(self, file: Optional[str] = None, simplified: bool = False) -> str:
+        """The gate records as JSON (tensorcircuit/translation.py:616-673)."""
+        from . import translation
+
+        s = translation.dumps(self.to_qir(), simplified=simplified)
+        if file is not None:
+            with open(file, "w") as fh:
+                fh.write(s)
+        return s
+
+    @classmethod
+    def from_json(cls, jsonstr: Any, circuit_params: Optional[Dict[str, Any]] = None) -> "Circuit":
+        import json
+
+        from . import translation
+
+        data = json.loads(jsonstr) if isinstance(jsonstr, str) else jsonstr
+        return cls.from_qir(translation.json2qir(data), circuit_params)
+
+    @classmethod
+    def from_json_file(cls, file: str, circuit_params: Optional[Dict[str, Any]] = None) -> "Circuit":
+        with open(file) as fh:
+            return cls.from_json(fh.read(), circuit_params)
+
+    @classmethod
+    def from_qsim_file(cls, file: str, circuit_params: Optional[Dict[str, Any]] = None) -> "Circuit":
+        """A qsim circuit file: the qubit count on the first line, then one
+        gate per line."""
+        from . import translation
+
+        with open(file) as fh:
+            lines = fh.readlines()
+        params = dict(circuit_params or {})
+        params.setdefault("nqubits", int(lines[0]))
+        return translation.apply_qsim(cls(**params), lines[1:])
 
     def engine_stats(self) -> Dict[str, int]:
         """Pass/stage counts of the plan the engine uses for this circuit."""

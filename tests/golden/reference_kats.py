@@ -172,3 +172,6 @@ DM = dict(
     cond_measure=dict(src="tests/test_dmcircuit.py:450-456", before=1.0, after=0.0, atol=1e-5),
     sexpps=dict(src="tests/test_dmcircuit.py:474-502", y=1.0, atol=1e-5, shot_tol=0.015),
 )
+
+# tests/test_circuit.py:1465-1479 -- gate counting with aliases
+GATE_COUNT = dict(src="tests/test_circuit.py:1465-1479", total=8, h=2, ccnot=3, rx_multicontrol=2, on_q0=2)
