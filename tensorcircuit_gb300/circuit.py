@@ -1420,6 +1420,27 @@ class Circuit:
         with open(file) as fh:
             return cls.from_json(fh.read(), circuit_params)
 
+    def to_openqasm(self, **kws: Any) -> str:
+        """OpenQASM 2 text with the qelib1 gates (the reference goes through
+        qiskit, abstractcircuit.py:793-802); other 1-qubit gates become u3
+        (global phase dropped), other multi-qubit gates raise."""
+        from . import translation
+
+        return translation.qir2qasm(self.to_qir(), self._nqubits)
+
+    @classmethod
+    def from_openqasm(cls, qasmstr: str, circuit_params: Optional[Dict[str, Any]] = None,
+                      keep_measure_order: bool = False) -> "Circuit":
+        from . import translation
+
+        return translation.qasm2circuit(qasmstr, cls, circuit_params)
+
+    @classmethod
+    def from_openqasm_file(cls, file: str, circuit_params: Optional[Dict[str, Any]] = None,
+                           keep_measure_order: bool = False) -> "Circuit":
+        with open(file) as fh:
+            return cls.from_openqasm(fh.read(), circuit_params)
+
     @classmethod
     def from_qsim_file(cls, file: str, circuit_params: Optional[Dict[str, Any]] = None) -> "Circuit":
         """A qsim circuit file: the qubit count on the first line, then one

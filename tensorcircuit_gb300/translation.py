@@ -1,6 +1,6 @@
 """Circuit records to and from text: the reference's JSON form
-(tensorcircuit/translation.py:587-702) and qsim files
-(abstractcircuit.py ``from_qsim_file`` / ``_apply_qsim``).
+(tensorcircuit/translation.py:587-702), qsim files
+(abstractcircuit.py ``from_qsim_file`` / ``_apply_qsim``) and OpenQASM 2.
 
 JSON entries are ``{"name", "qubits"}`` plus, unless ``simplified``, the
 gate matrix as ``[real, imag]`` nested lists, the U-gate angles of 1-qubit
@@ -193,3 +193,126 @@ def apply_qsim(c: Any, lines: Sequence[str]) -> Any:
 
 def dumps(qir: List[Dict[str, Any]], simplified: bool = False) -> str:
     return json.dumps(qir2json(qir, simplified=simplified))
+
+
+# ----------------------------------------------------------------- OpenQASM 2
+# The reference writes and reads OpenQASM through qiskit (abstractcircuit.py:
+# 793-840), which this image does not have; the same gate vocabulary of
+# qelib1.inc is written and parsed here directly.
+_QASM_FIXED = {"i": "id", "x": "x", "y": "y", "z": "z", "h": "h", "s": "s", "t": "t", "sd": "sdg", "td": "tdg",
+               "cnot": "cx", "cz": "cz", "cy": "cy", "swap": "swap", "toffoli": "ccx", "fredkin": "cswap"}
+_QASM_ROT = {"rx": "rx", "ry": "ry", "rz": "rz", "crx": "crx", "cry": "cry", "crz": "crz", "rxx": "rxx",
+             "ryy": "ryy", "rzz": "rzz", "phase": "u1", "cphase": "cu1"}
+
+
+def _num(v: Any) -> float:
+    if isinstance(v, torch.Tensor):
+        v = v.detach().cpu()
+    return float(np.real(np.asarray(v)))
+
+
+def qir2qasm(qir: List[Dict[str, Any]], n: int) -> str:
+    from .circuit import Circuit
+
+    lines = ["OPENQASM 2.0;", 'include "qelib1.inc";', "qreg q[%d];" % n]
+    for d in qir:
+        name = Circuit._qir_name(d)
+        if name in Circuit._NON_GATE_QIR:
+            continue
+        qs = ",".join("q[%d]" % int(q) for q in d["index"])
+        p = d.get("parameters", {}) if d.get("gatef") is not None else {}
+        if d.get("gatef") is not None and name in _QASM_FIXED and not p:
+            lines.append("%s %s;" % (_QASM_FIXED[name], qs))
+        elif name in _QASM_ROT:
+            lines.append("%s(%.17g) %s;" % (_QASM_ROT[name], _num(p.get("theta", 0.0)), qs))
+        elif name == "u":
+            lines.append("u3(%.17g,%.17g,%.17g) %s;" % (_num(p.get("theta", 0.0)), _num(p.get("phi", 0.0)),
+                                                        _num(p.get("lbd", 0.0)), qs))
+        elif len(d["index"]) == 1:
+            # any other 1-qubit gate: its U angles (the global phase is dropped)
+            th, ph, lb = get_u_parameter(qir_matrix(d))
+            lines.append("u3(%.17g,%.17g,%.17g) %s;" % (th, ph, lb, qs))
+        else:
+            raise NotImplementedError("gate %s has no OpenQASM 2 form here" % name)
+    return "\n".join(lines) + "\n"
+
+
+def _qasm_expr(s: str) -> float:
+    """Arithmetic of numbers and pi (+ - * / ^, parentheses, unary minus)."""
+    import ast
+
+    tree = ast.parse(s.strip().replace("^", "**"), mode="eval")
+
+    def ev(node: Any) -> float:
+        if isinstance(node, ast.Expression):
+            return ev(node.body)
+        if isinstance(node, ast.Constant) and isinstance(node.value, (int, float)):
+            return float(node.value)
+        if isinstance(node, ast.Name) and node.id == "pi":
+            return float(np.pi)
+        if isinstance(node, ast.UnaryOp) and isinstance(node.op, (ast.USub, ast.UAdd)):
+            v = ev(node.operand)
+            return -v if isinstance(node.op, ast.USub) else v
+        if isinstance(node, ast.BinOp) and isinstance(node.op, (ast.Add, ast.Sub, ast.Mult, ast.Div, ast.Pow)):
+            a, b = ev(node.left), ev(node.right)
+            return {ast.Add: a + b, ast.Sub: a - b, ast.Mult: a * b,
+                    ast.Div: a / b if isinstance(node.op, ast.Div) else 0.0,
+                    ast.Pow: a ** b if isinstance(node.op, ast.Pow) else 0.0}[type(node.op)]
+        raise ValueError("unsupported OpenQASM expression: %s" % s)
+
+    return ev(tree)
+
+
+def qasm2circuit(text: str, cls: Any, circuit_params: Any = None) -> Any:
+    """Parse OpenQASM 2 (qelib1 gates, one or more qregs; measure, barrier
+    and creg lines are skipped) onto a new circuit of class ``cls``."""
+    import re
+
+    body = re.sub(r"//[^\n]*", "", text)
+    stmts = [s.strip() for s in body.split(";") if s.strip()]
+    regs: Dict[str, int] = {}
+    total = 0
+    gates_: List[Tuple[str, List[float], List[int]]] = []
+    inv_fixed = {v: k for k, v in _QASM_FIXED.items()}
+    inv_rot = {v: k for k, v in _QASM_ROT.items()}
+    for s in stmts:
+        if s.startswith("OPENQASM") or s.startswith("include") or s.startswith("creg") or \
+                s.startswith("barrier") or s.startswith("measure"):
+            continue
+        m = re.match(r"qreg\s+(\w+)\s*\[\s*(\d+)\s*\]$", s)
+        if m:
+            regs[m.group(1)] = total
+            total += int(m.group(2))
+            continue
+        m = re.match(r"(\w+)\s*(\(([^)]*)\))?\s+(.+)$", s, re.S)
+        if not m:
+            raise ValueError("cannot parse OpenQASM statement: %s" % s)
+        params = [_qasm_expr(x) for x in m.group(3).split(",")] if m.group(3) else []
+        qs = []
+        for a in m.group(4).split(","):
+            mm = re.match(r"\s*(\w+)\s*\[\s*(\d+)\s*\]\s*$", a)
+            if not mm:
+                raise ValueError("cannot parse OpenQASM operand: %s" % a)
+            qs.append(regs[mm.group(1)] + int(mm.group(2)))
+        gates_.append((m.group(1).lower(), params, qs))
+    cp = dict(circuit_params or {})
+    cp.setdefault("nqubits", total)
+    c = cls(**cp)
+    for name, params, qs in gates_:
+        if name in inv_fixed:
+            getattr(c, inv_fixed[name])(*qs)
+        elif name in ("cu1", "cp"):
+            c.cphase(*qs, theta=params[0])
+        elif name in ("u1", "p"):
+            c.phase(*qs, theta=params[0])
+        elif name in inv_rot:
+            getattr(c, inv_rot[name])(*qs, theta=params[0])
+        elif name in ("u3", "u"):
+            c.u(*qs, theta=params[0], phi=params[1], lbd=params[2])
+        elif name == "u2":
+            c.u(*qs, theta=np.pi / 2, phi=params[0], lbd=params[1])
+        elif name == "sx":
+            c.rx(*qs, theta=np.pi / 2)
+        else:
+            raise NotImplementedError("OpenQASM gate %s" % name)
+    return c

@@ -89,3 +89,54 @@ def test_qsim_text(tmp_path):
     names = [tc.Circuit._qir_name(d) for d in c.to_qir()]
     assert names == ["h", "rx", "cz", "rz", "iswap", "cphase", "phase"]
     assert c.to_qir()[4]["parameters"]["theta"] == -0.3
+
+
+def test_openqasm_round_trip():
+    import tensorcircuit_gb300 as tc
+    from tensorcircuit_gb300 import translation as tr
+
+    c = tc.Circuit(4)
+    c.h(0)
+    c.sd(1)
+    c.cnot(0, 2)
+    c.rx(1, theta=0.25)
+    c.rzz(2, 3, theta=-0.5)
+    c.cphase(0, 3, theta=0.75)
+    c.u(2, theta=0.1, phi=0.2, lbd=0.3)
+    c.toffoli(0, 1, 3)
+    c.wroot(1)
+    text = c.to_openqasm()
+    assert text.startswith("OPENQASM 2.0;") and "qreg q[4];" in text
+    assert "sdg q[1];" in text and "cx q[0],q[2];" in text and "ccx q[0],q[1],q[3];" in text
+    c2 = tc.Circuit.from_openqasm(text)
+    names = [tc.Circuit._qir_name(d) for d in c2.to_qir()]
+    assert names == ["h", "sd", "cnot", "rx", "rzz", "cphase", "u", "toffoli", "u"]
+    # every gate matches up to the global phase u3 drops
+    for a, b in zip(c.to_qir(), c2.to_qir()):
+        ma, mb = tr.qir_matrix(a), tr.qir_matrix(b)
+        ph = np.vdot(mb.reshape(-1), ma.reshape(-1)) / ma.shape[0]
+        np.testing.assert_allclose(abs(ph), 1.0, atol=1e-9)
+        np.testing.assert_allclose(ma, ph * mb, atol=1e-9)
+
+
+def test_openqasm_parsing_forms():
+    import tensorcircuit_gb300 as tc
+
+    text = """OPENQASM 2.0;
+include "qelib1.inc";
+qreg a[2];
+qreg b[1];
+creg c[3];
+// comment
+u2(0, pi) a[0];
+cu1(pi/4) a[1],b[0];
+rx(-pi/2 + 0.5*2) b[0];
+barrier a[0],a[1];
+measure a[0] -> c[0];
+"""
+    c = tc.Circuit.from_openqasm(text)
+    assert c._nqubits == 3
+    q = c.to_qir()
+    assert [d["index"] for d in q] == [(0,), (1, 2), (2,)]
+    np.testing.assert_allclose(q[1]["parameters"]["theta"], np.pi / 4)
+    np.testing.assert_allclose(q[2]["parameters"]["theta"], -np.pi / 2 + 1.0)
