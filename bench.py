@@ -838,6 +838,125 @@ def run_mcnoise(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+DM_N, DM_LAYERS, DM_P, DM_BATCH, DM_SEED = 10, 4, 0.01, 64, 8
+DM_METRIC = "density-matrix value+grad circuits/s (n=10 noisy HEA, 4 layers, depolarizing 0.01, TFIM energy)"
+DM_UNIT = "circuits/s"
+DM_WORKLOAD = "dm_n10_l4_depol_b64_vvag"
+
+
+def dm_energy(tc, params):
+    """Noisy HEA on a density matrix: per layer rx on every qubit, rzz on
+    the open chain, depolarizing(p, p, p) on every qubit; energy
+    sum <Z_i Z_i+1> + sum <X_i>."""
+    import torch
+
+    c = tc.DMCircuit(DM_N)
+    ps = params.unbind(-1)
+    k = 0
+    for _ in range(DM_LAYERS):
+        for i in range(DM_N):
+            c.rx(i, theta=ps[k])
+            k += 1
+        for i in range(DM_N - 1):
+            c.rzz(i, i + 1, theta=ps[k])
+            k += 1
+        for i in range(DM_N):
+            c.depolarizing(i, px=DM_P, py=DM_P, pz=DM_P)
+    e = 0.0
+    for i in range(DM_N - 1):
+        e = e + torch.real(c.expectation_ps(z=[i, i + 1]))
+    for i in range(DM_N):
+        e = e + torch.real(c.expectation_ps(x=[i]))
+    return e
+
+
+def cpu_dm(sample=2):
+    from oracle import reference_algo as ra
+
+    threads = len(os.sched_getaffinity(0))
+    rng = np.random.default_rng(DM_SEED)
+    params = rng.uniform(0, 2 * np.pi, (DM_BATCH, DM_LAYERS * (2 * DM_N - 1))).astype(np.float32)
+    ra.dm_value_and_grad(DM_N, 1, DM_P, params[0][: 2 * DM_N - 1], threads)  # warm-up
+    t0 = time.perf_counter()
+    for b in range(sample):
+        ra.dm_value_and_grad(DM_N, DM_LAYERS, DM_P, params[b], threads)
+    dt = time.perf_counter() - t0
+    return {"value": sample / dt, "unit": DM_UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of the %d circuits (%.1f s; labelled torch restatement of the reference's DMCircuit2 "
+                      "algorithm: per-gate tensordot on both legs of rho, superoperator channels, taped AD)" %
+                      (sample, DM_BATCH, dt)}
+
+
+def run_dm(args, rank, world):
+    """Density matrices: ``DM_BATCH`` parameter vectors (seed 8) of the noisy
+    HEA through ``K.jit(K.vvag(f))``; rho is a 20-qubit engine vector per
+    circuit, each run of channels one segment boundary."""
+    import torch
+
+    import tensorcircuit_gb300 as tc
+    from tensorcircuit_gb300 import _native
+
+    tc.build()
+    lib = _native.load()
+    K_ = tc.set_backend("pytorch")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rng = np.random.default_rng(DM_SEED)
+    params_np = rng.uniform(0, 2 * np.pi, (DM_BATCH, DM_LAYERS * (2 * DM_N - 1))).astype(np.float32)
+    p_host = torch.from_numpy(params_np).pin_memory()
+    p_dev = p_host.to(dev)
+    eager = K_.vvag(lambda p: dm_energy(tc, p), argnums=0, vectorized_argnums=0)
+    step = K_.jit(eager)
+    warmup = max(args.warmup, 3)
+    for _ in range(warmup + 1):
+        v, g = step(p_dev)
+    torch.cuda.synchronize()
+    l0 = lib.tcg_launch_count()
+    eager(p_dev)
+    torch.cuda.synchronize()
+    launches_per_step = lib.tcg_launch_count() - l0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(args.steps):
+            v, g = step(p_dev)
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    vh = torch.empty((DM_BATCH,), dtype=torch.float32).pin_memory()
+    gh = torch.empty(tuple(params_np.shape), dtype=torch.float32).pin_memory()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        v, g = step(p_host.to(dev, non_blocking=True))
+        vh.copy_(v, non_blocking=True)
+        gh.copy_(g, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    if rank != 0:
+        return
+    cpu = None if args.no_cpu else cpu_dm()
+    line = {
+        "metric": DM_METRIC, "value": DM_BATCH / (ms / 1e3), "unit": DM_UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": DM_WORKLOAD, "n_qubits": DM_N, "engine_qubits": 2 * DM_N, "layers": DM_LAYERS,
+                   "depolarizing": DM_P, "batch": DM_BATCH, "params": int(params_np.shape[1]), "seed": DM_SEED,
+                   "jit_capture_errors": step.capture_errors(),
+                   "l2": "no flush: 64 density matrices of 8 MiB (512 MiB) exceed the 129 MB L2"},
+        "roofline": None,
+        "cpu_baseline": cpu,
+        "e2e": {"value": DM_BATCH / (ms_e2e / 1e3), "unit": DM_UNIT, "h2d_bytes_per_step": int(params_np.nbytes),
+                "d2h_bytes_per_step": int(DM_BATCH * 4 + params_np.nbytes)},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches_per_step * args.steps),
+        "gpu_launches_per_step": int(launches_per_step),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_warmstart(args, rank, world):
     """Learned warm start: random-coupling open TFIM n=16, HEA depth 6 (186
     angles), Adam lr 0.02; training angles generated by the engine's batched
@@ -887,11 +1006,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hea", choices=["hea", "brickwall", "qaoa", "warmstart", "mcnoise"],
+    ap.add_argument("--workload", default="hea", choices=["hea", "brickwall", "qaoa", "warmstart", "mcnoise", "dm"],
                     help="hea: n=20 HEA batched vvag (default); brickwall: n=28 Haar brick wall; "
                          "qaoa: 512 uneven QAOA circuits in one persistent launch per sweep; "
                          "warmstart: learned warm start for n=16 TFIM chains; "
-                         "mcnoise: Monte-Carlo phase-damping trajectories, value+grad")
+                         "mcnoise: Monte-Carlo phase-damping trajectories, value+grad; "
+                         "dm: noisy HEA on n=10 density matrices, value+grad")
     ap.add_argument("--trajectories", type=int, default=MC_TRAJ, help="mcnoise: trajectories per step")
     ap.add_argument("--mc-eager", action="store_true", help="mcnoise: run the step eagerly instead of replaying it from a CUDA graph")
     ap.add_argument("--batch", type=int, default=BATCH,
@@ -926,6 +1046,8 @@ def main():
         run_warmstart(args, rank, world)
     elif args.workload == "mcnoise":
         run_mcnoise(args, rank, world)
+    elif args.workload == "dm":
+        run_dm(args, rank, world)
     else:
         run_gb300_arm(args, rank, world)
     if world > 1:

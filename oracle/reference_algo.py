@@ -187,3 +187,49 @@ def mcnoise_value_and_grad(n: int, nlayer: int, gamma: float, params: np.ndarray
 
     g, v = torch.func.grad_and_value(f)(torch.as_tensor(params, dtype=torch.float32))
     return float(v), g.numpy()
+
+
+def dm_value_and_grad(n: int, nlayers: int, p: float, params: np.ndarray, threads: int) -> Tuple[float, np.ndarray]:
+    """Noisy HEA on a density matrix, the reference's DMCircuit2 algorithm
+    (tensorcircuit/densitymatrix.py:331-366): rho as a [2]*2n tensor, each
+    gate contracted on the row legs and its conjugate on the column legs, the
+    depolarizing channel (channels.py:56-102) as the superoperator
+    sum_i K_i (x) conj(K_i) contracted on (row, column) legs; per layer rx on
+    every qubit, rzz on the open chain, depolarizing(p, p, p) on every qubit;
+    energy sum <Z_i Z_i+1> + sum <X_i> = tr(rho H); taped AD."""
+    torch.set_num_threads(threads)
+    x = _PAULI["x"]
+    z = _PAULI["z"]
+    ks = [np.sqrt(1 - 3 * p) * np.eye(2), np.sqrt(p) * np.array([[0, 1], [1, 0]]),
+          np.sqrt(p) * np.array([[0, -1j], [1j, 0]]), np.sqrt(p) * np.array([[1, 0], [0, -1]])]
+    sup = torch.tensor(sum(np.kron(k, np.conj(k)) for k in ks), dtype=C64).reshape(2, 2, 2, 2)
+
+    def both(rho: torch.Tensor, g: torch.Tensor, q: Sequence[int]) -> torch.Tensor:
+        rho = _apply(rho, g, q)
+        return _apply(rho, torch.conj(g), [i + n for i in q])
+
+    def f(prm: torch.Tensor) -> torch.Tensor:
+        rho = torch.zeros([2] * (2 * n), dtype=C64)
+        rho.view(-1)[0] = 1.0
+        k = 0
+        for _ in range(nlayers):
+            for i in range(n):
+                rho = both(rho, _rx(prm[k]), (i,))
+                k += 1
+            for i in range(n - 1):
+                rho = both(rho, _rzz(prm[k]), (i, i + 1))
+                k += 1
+            for i in range(n):
+                rho = _apply(rho, sup, (i, i + n))
+        m = rho.reshape(1 << n, 1 << n)
+        e = torch.zeros((), dtype=torch.float32)
+        for i in range(n - 1):
+            op = _apply(_apply(rho, z, (i,)), z, (i + 1,)).reshape(1 << n, 1 << n)
+            e = e + torch.real(torch.trace(op))
+        for i in range(n):
+            e = e + torch.real(torch.trace(_apply(rho, x, (i,)).reshape(1 << n, 1 << n)))
+        del m
+        return e
+
+    g, v = torch.func.grad_and_value(f)(torch.as_tensor(params, dtype=torch.float32))
+    return float(v), g.numpy()

@@ -808,12 +808,22 @@ class Circuit:
                                   prob=[px, py, pz, 1 - px - py - pz], status=status)
 
     def _apply_nonunitary(self, m: Any, idx: Tuple[int, ...], ir: Dict[str, Any]) -> None:
-        """Apply a non-unitary operator (projector, superoperator): it starts
-        a new segment, so the adjoint sweep -- which un-applies a segment's
-        gates with G^dag -- stays exact for every other gate and passes
-        m^dag mu to the segment's input.  Constant operators become the
-        segment's first engine gate; tensors that need gradients are applied
-        by a torch contraction."""
+        """Apply a non-unitary operator (projector, superoperator).
+
+        The adjoint sweep un-applies a segment's gates with G^dag to rebuild
+        the state each gradient needs; that is exact for unitary gates and
+        wrong for this one, while the cotangent it passes on (m^dag mu) is
+        exact either way.  So a constant non-unitary operator may sit in a
+        segment only ahead of every gate that takes a gradient: it joins the
+        current segment while that holds only constant gates, and otherwise
+        starts a new one, whose input is the current output state.  Tensors
+        that need gradients are applied to the materialised state by a
+        torch contraction."""
+        if not isinstance(m, torch.Tensor) and all(op.kind == "const" for op in self._ops):
+            m = np.asarray(m, dtype=np.complex128)
+            key = "m:" + hashlib.sha1(m.tobytes()).hexdigest()
+            Circuit._record(self, _Op("const", key, idx, m, gates.is_diagonal(m), len(idx)), ir)
+            return
         psi = self._engine_state()[0]
         self._seg_ops += len(self._ops)
         self._ops = []
