@@ -202,6 +202,20 @@ class Gen {
     o << "  }\n";
   }
 
+  // One real value (a rotation's gradient): a real butterfly; the first
+  // lane writes (sum, 0) where the complex reduction would.
+  std::string reduce_real(const char* var) const {
+    std::ostringstream o;
+    if (NL_ < 32) {
+      o << " { const float t = warp_sum1<" << NL_ << ">(" << var
+        << "); if (lane == 0) sms[op.slot] = make_float2(t, 0.f); }";
+      return o.str();
+    }
+    o << " { const float t = warp_sum1<" << NL_ << ">(" << var << "); if (lane == 0) sms[warp * " << MS_
+      << " + op.slot] = make_float2(t, 0.f); }";
+    return o.str();
+  }
+
   std::string reduce(int E, const char* arr) const {
     std::ostringstream o;
     if (NL_ < 32) {  // one partial warp: a butterfly per entry, lane 0 writes
@@ -311,7 +325,7 @@ class Gen {
         const bool G = op.slot >= 0;
         b << "float g = 0.f; prot_bwd<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ", "
           << (G ? "true" : "false") << ">(v, w, cs.x, cs.y, sg, g);";
-        if (G) b << " float2 a1[1] = {make_float2(g, 0.f)};" << reduce(1, "a1");
+        if (G) b << reduce_real("g");
       }
     } else if (op.kind == OP_ZRUN) {
       // entries are literals: each run is its own body

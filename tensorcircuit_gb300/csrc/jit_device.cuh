@@ -364,23 +364,41 @@ __device__ __forceinline__ void prot(float2 (&v)[NR], float c, float s, u32 sgn,
   constexpr bool QIM = (NY & 1) == 0;
   float qv = ((NY & 3) <= 1) ? -s : s;  // the nonzero component of q
   if (adj ^ (sgn != 0u)) qv = -qv;
+  // Cross terms first (products into temporaries), then one FMA per
+  // component that reads the component's own old value last: every result
+  // can take the register of the value it replaces, so the op loop's
+  // register arrays need no copies at the end of the body.
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
     const float qr = (tk_popc(r & ZR) & 1) ? -qv : qv;
     if (X == 0) {
-      if (QIM) v[r] = cmul(make_float2(c, qr), v[r]);
-      else v[r] = make_float2((c + qr) * v[r].x, (c + qr) * v[r].y);
+      if (QIM) {
+        const float px = qr * v[r].y, py = qr * v[r].x;
+        v[r].x = fmaf(c, v[r].x, -px);
+        v[r].y = fmaf(c, v[r].y, py);
+      } else {
+        const float f = c + qr;
+        v[r].x = f * v[r].x;
+        v[r].y = f * v[r].y;
+      }
     } else {
       const int r2 = r ^ X;
       if (r2 < r) continue;
       const float q2 = (tk_popc(r2 & ZR) & 1) ? -qv : qv;
-      const float2 a = v[r], bb = v[r2];
       if (QIM) {
-        v[r] = make_float2(fmaf(-qr, bb.y, c * a.x), fmaf(qr, bb.x, c * a.y));
-        v[r2] = make_float2(fmaf(-q2, a.y, c * bb.x), fmaf(q2, a.x, c * bb.y));
+        const float pax = qr * v[r2].y, pay = qr * v[r2].x;
+        const float pbx = q2 * v[r].y, pby = q2 * v[r].x;
+        v[r].x = fmaf(c, v[r].x, -pax);
+        v[r].y = fmaf(c, v[r].y, pay);
+        v[r2].x = fmaf(c, v[r2].x, -pbx);
+        v[r2].y = fmaf(c, v[r2].y, pby);
       } else {
-        v[r] = make_float2(fmaf(qr, bb.x, c * a.x), fmaf(qr, bb.y, c * a.y));
-        v[r2] = make_float2(fmaf(q2, a.x, c * bb.x), fmaf(q2, a.y, c * bb.y));
+        const float pax = qr * v[r2].x, pay = qr * v[r2].y;
+        const float pbx = q2 * v[r].x, pby = q2 * v[r].y;
+        v[r].x = fmaf(c, v[r].x, pax);
+        v[r].y = fmaf(c, v[r].y, pay);
+        v[r2].x = fmaf(c, v[r2].x, pbx);
+        v[r2].y = fmaf(c, v[r2].y, pby);
       }
     }
   }
@@ -394,13 +412,22 @@ __device__ __forceinline__ void prot_bwd(float2 (&v)[NR], float2 (&w)[NR], float
     // g = Im(pt z), z = sum_r s(r) conj(w_r) v_{r^X}, pt = (+-)(-i)^NY: only
     // Im z (even NY) or Re z (odd NY) is needed
     constexpr bool IMZ = (NY & 1) == 0;
+    // two FMAs per amplitude: the parity sign of register r is a
+    // compile-time constant, so it folds into the operands' signs
     float zc = 0.f;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
       const float2 t = v[r ^ X];
-      const float term = IMZ ? fmaf(w[r].x, t.y, -w[r].y * t.x) : fmaf(w[r].x, t.x, w[r].y * t.y);
-      if (tk_popc(r & ZR) & 1) zc -= term;
-      else zc += term;
+      const bool neg = (tk_popc(r & ZR) & 1) != 0;
+      const float wx = neg ? -w[r].x : w[r].x;
+      const float wy = neg ? -w[r].y : w[r].y;
+      if (IMZ) {
+        zc = fmaf(wx, t.y, zc);
+        zc = fmaf(-wy, t.x, zc);
+      } else {
+        zc = fmaf(wx, t.x, zc);
+        zc = fmaf(wy, t.y, zc);
+      }
     }
     // Im(pt z): NY%4 = 0 -> z.y, 1 -> -z.x, 2 -> -z.y, 3 -> z.x
     g = ((NY & 3) == 0 || (NY & 3) == 3) ? zc : -zc;
@@ -499,6 +526,18 @@ __device__ __forceinline__ void small_reduce(const float2 (&a)[E], int lane, flo
 }
 
 // ----------------------------------------------------------------- reductions
+// Sum of one real value over the NL lanes (butterfly: every lane ends with
+// the total) -- half the shuffles of the complex form, for rotation
+// gradients, which are real.
+template <int NL>
+__device__ __forceinline__ float warp_sum1(float x) {
+  constexpr unsigned FULL = NL >= 32 ? 0xffffffffu : ((1u << NL) - 1u);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    if (o < NL) x += __shfl_xor_sync(FULL, x, o);
+  return x;
+}
+
 // Sum E complex values (E a power of two <= 16) over the NL lanes of a warp.
 // Returns this lane's total and sets `entry` to the entry it holds, or -1 if
 // another lane writes that entry.  Full warps use a transpose-reduce (each

@@ -276,23 +276,40 @@ __device__ __forceinline__ void dispatch_pacc(int x, const float2 (&v)[1 << R], 
 // one real number qv and the update costs four operations per amplitude.
 template <int R, int X, bool QIM>
 __device__ __forceinline__ void prot_rt(float2 (&v)[1 << R], float c, float qv, int zr) {
+  // cross terms into temporaries first, then one FMA per component reading
+  // its own old value last, so results can stay in the registers they
+  // replace (no copies at the end of the op)
 #pragma unroll
   for (int r = 0; r < (1 << R); ++r) {
     const float qr = (__popc(r & zr) & 1) ? -qv : qv;
     if (X == 0) {
-      if (QIM) v[r] = cmul(make_float2(c, qr), v[r]);
-      else v[r] = make_float2((c + qr) * v[r].x, (c + qr) * v[r].y);
+      if (QIM) {
+        const float px = qr * v[r].y, py = qr * v[r].x;
+        v[r].x = fmaf(c, v[r].x, -px);
+        v[r].y = fmaf(c, v[r].y, py);
+      } else {
+        const float f = c + qr;
+        v[r].x = f * v[r].x;
+        v[r].y = f * v[r].y;
+      }
     } else {
       const int r2 = r ^ X;
       if (r2 < r) continue;
       const float q2 = (__popc(r2 & zr) & 1) ? -qv : qv;
-      const float2 a = v[r], bb = v[r2];
       if (QIM) {
-        v[r] = make_float2(fmaf(-qr, bb.y, c * a.x), fmaf(qr, bb.x, c * a.y));
-        v[r2] = make_float2(fmaf(-q2, a.y, c * bb.x), fmaf(q2, a.x, c * bb.y));
+        const float pax = qr * v[r2].y, pay = qr * v[r2].x;
+        const float pbx = q2 * v[r].y, pby = q2 * v[r].x;
+        v[r].x = fmaf(c, v[r].x, -pax);
+        v[r].y = fmaf(c, v[r].y, pay);
+        v[r2].x = fmaf(c, v[r2].x, -pbx);
+        v[r2].y = fmaf(c, v[r2].y, pby);
       } else {
-        v[r] = make_float2(fmaf(qr, bb.x, c * a.x), fmaf(qr, bb.y, c * a.y));
-        v[r2] = make_float2(fmaf(q2, a.x, c * bb.x), fmaf(q2, a.y, c * bb.y));
+        const float pax = qr * v[r2].x, pay = qr * v[r2].y;
+        const float pbx = q2 * v[r].x, pby = q2 * v[r].y;
+        v[r].x = fmaf(c, v[r].x, pax);
+        v[r].y = fmaf(c, v[r].y, pay);
+        v[r2].x = fmaf(c, v[r2].x, pbx);
+        v[r2].y = fmaf(c, v[r2].y, pby);
       }
     }
   }
