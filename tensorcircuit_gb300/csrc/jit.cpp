@@ -271,8 +271,8 @@ class Gen {
         const bool scalar = (k == 1) ? rb[0] < 0 : (rb[0] < 0 && rb[1] < 0);
         if (fwd()) {
           if (scalar) {
-            if (k == 1) b << "C = cmul(C, ld(Mt + op.off + " << t0 << "));";
-            else b << "C = cmul(C, ld(Mt + op.off + ((" << t0 << " << 1) | " << t1 << ")));";
+            if (k == 1) b << "cmul_ip(C, ld(Mt + op.off + " << t0 << "));";
+            else b << "cmul_ip(C, ld(Mt + op.off + ((" << t0 << " << 1) | " << t1 << ")));";
             *usesC = true;
           } else if (k == 1) {
             b << "diag1<" << NR_ << ", " << rb[0] << ">(v, Mt + op.off, " << t0 << ", false);";
@@ -304,10 +304,10 @@ class Gen {
           for (int i = 0; i < k; ++i)
             if (rb[i] >= 0 && ((r >> rb[i]) & 1)) c |= 1u << (k - 1 - i);
           if (fwd()) {
-            b << " v[" << r << "] = cmul(ld(d + (rt | " << c << "u)), v[" << r << "]);";
+            b << " cmul_ip(v[" << r << "], ld(d + (rt | " << c << "u)));";
           } else {
-            b << " { const float2 e = cconj(ld(d + (rt | " << c << "u))); v[" << r << "] = cmul(e, v[" << r
-              << "]); w[" << r << "] = cmul(e, w[" << r << "]); }";
+            b << " { const float2 e = cconj(ld(d + (rt | " << c << "u))); cmul_ip(v[" << r << "], e); cmul_ip(w["
+              << r << "], e); }";
           }
         }
       }
@@ -569,7 +569,7 @@ class Gen {
     for (size_t i = 0; i < sig_body_.size(); ++i)
       out << "        case " << i << ": { " << sig_body_[i] << " } break;\n";
     out << "        default: break;\n      }\n    }\n";
-    out << "    if (useC) {\n#pragma unroll\n      for (int r = 0; r < " << NR_ << "; ++r) v[r] = cmul(C, v[r]);\n    }\n";
+    out << "    if (useC) {\n#pragma unroll\n      for (int r = 0; r < " << NR_ << "; ++r) cmul_ip(v[r], C);\n    }\n";
     if (bwd() || meas()) {
       out << "    if (soe > sob) {\n      __syncthreads();\n";
       out << "      for (int e = sob + (int)tid; e < soe; e += " << NT_ << ") {\n";

@@ -34,6 +34,14 @@ __device__ __forceinline__ float2 cfmac(float2 a, float2 b, float2 c) {
   return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.y, b.x, fmaf(-a.x, b.y, c.y)));
 }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+// v <- p v with the cross products first and one FMA per component reading
+// its own old value last, so the result can stay in v's registers (the op
+// loops carry their register arrays; a result in new registers costs copies)
+__device__ __forceinline__ void cmul_ip(float2& v, float2 p) {
+  const float tx = p.y * v.y, ty = p.y * v.x;
+  v.x = fmaf(p.x, v.x, -tx);
+  v.y = fmaf(p.x, v.y, ty);
+}
 __device__ __forceinline__ float2 czero() { return make_float2(0.f, 0.f); }
 __device__ __forceinline__ float2 cone() { return make_float2(1.f, 0.f); }
 __device__ __forceinline__ float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
@@ -197,7 +205,7 @@ __device__ __forceinline__ void diag2(float2 (&v)[NR], const float2* d, u32 t0, 
     e[s] = conj ? cconj(x) : x;
   }
 #pragma unroll
-  for (int r = 0; r < NR; ++r) v[r] = cmul(e[dsub<RB0, RB1>(r)], v[r]);
+  for (int r = 0; r < NR; ++r) cmul_ip(v[r], e[dsub<RB0, RB1>(r)]);
 }
 
 template <int NR, int RB0, int RB1, bool G>
@@ -214,10 +222,9 @@ __device__ __forceinline__ void diag2_bwd(float2 (&v)[NR], float2 (&w)[NR], cons
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
     const int s = dsub<RB0, RB1>(r);
-    const float2 y = cmul(e[s], v[r]);
-    v[r] = y;
-    if (G) g[s] = cfmac(w[r], y, g[s]);
-    w[r] = cmul(e[s], w[r]);
+    cmul_ip(v[r], e[s]);
+    if (G) g[s] = cfmac(w[r], v[r], g[s]);
+    cmul_ip(w[r], e[s]);
   }
   if (G) {
     // bin s holds sub-index (b0(s) << 1 | b1(s)); move to output entries
@@ -246,7 +253,7 @@ __device__ __forceinline__ void diag1(float2 (&v)[NR], const float2* d, u32 t, b
     e1 = cconj(e1);
   }
 #pragma unroll
-  for (int r = 0; r < NR; ++r) v[r] = cmul((RB >= 0 && ((r >> RB) & 1)) ? e1 : e0, v[r]);
+  for (int r = 0; r < NR; ++r) cmul_ip(v[r], (RB >= 0 && ((r >> RB) & 1)) ? e1 : e0);
 }
 
 template <int NR, int RB, bool G>
@@ -257,13 +264,12 @@ __device__ __forceinline__ void diag1_bwd(float2 (&v)[NR], float2 (&w)[NR], cons
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
     const bool hi = RB >= 0 && ((r >> RB) & 1);
-    const float2 y = cmul(hi ? e1 : e0, v[r]);
-    v[r] = y;
+    cmul_ip(v[r], hi ? e1 : e0);
     if (G) {
-      if (hi) g1 = cfmac(w[r], y, g1);
-      else g0 = cfmac(w[r], y, g0);
+      if (hi) g1 = cfmac(w[r], v[r], g1);
+      else g0 = cfmac(w[r], v[r], g0);
     }
-    w[r] = cmul(hi ? e1 : e0, w[r]);
+    cmul_ip(w[r], hi ? e1 : e0);
   }
   if (G) {
     if (RB >= 0) {
@@ -474,15 +480,15 @@ __device__ __forceinline__ float2 zrun_factor(const float2* m, u32 gthr, u32 zm)
 template <int NR>
 __device__ __forceinline__ void zrun_apply(float2 (&v)[NR], const float2 (&ph)[NR]) {
 #pragma unroll
-  for (int r = 0; r < NR; ++r) v[r] = cmul(ph[r], v[r]);
+  for (int r = 0; r < NR; ++r) cmul_ip(v[r], ph[r]);
 }
 template <int NR>
 __device__ __forceinline__ void zrun_unapply(float2 (&v)[NR], float2 (&w)[NR], const float2 (&ph)[NR]) {
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
     const float2 c = cconj(ph[r]);
-    v[r] = cmul(c, v[r]);
-    w[r] = cmul(c, w[r]);
+    cmul_ip(v[r], c);
+    cmul_ip(w[r], c);
   }
 }
 // t[c] = sum_r (-1)^{popc(r & c)} Im(conj(w_r) v_r)
