@@ -409,15 +409,14 @@ class Gen {
       rec->zm = op.zmask;
       rec->ny = op.nY;
       rec->zr = zr;
+      // a Pauli string's value is real: one real accumulation per amplitude
+      // pair component, signs and the (-i)^nY phase fixed at compile time
       if (meas()) {
-        b << "float2 acc = expectz<" << NR_ << ", " << op.xreg
-          << ">(v, op.zr); if (__popc(gthr & op.zm) & 1) acc = cneg(acc); acc = cmul(ypow(op.ny), acc); "
-             "float2 a1[1] = {acc};"
-          << reduce(1, "a1");
+        b << "float e = expect_real<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3)
+          << ">(v); if (__popc(gthr & op.zm) & 1) e = -e;" << reduce_real("e");
       } else {
-        b << "float2 cf = cmul(ypow(op.ny), make_float2(kp.coef[b * kp.coef_stride + op.off], 0.f)); if "
-             "(__popc(gthr & op.zm) & 1) cf = cneg(cf); paccz<"
-          << NR_ << ", " << op.xreg << ">(v, w, cf, op.zr);";
+        b << "float k = kp.coef[b * kp.coef_stride + op.off]; if (__popc(gthr & op.zm) & 1) k = -k; pacc_real<"
+          << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, w, k);";
       }
     }
     rec->sig = sig(b.str());

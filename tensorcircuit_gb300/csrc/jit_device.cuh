@@ -287,66 +287,53 @@ __device__ __forceinline__ void diag1_bwd(float2 (&v)[NR], float2 (&w)[NR], cons
 // __builtin_popcount)
 __host__ __device__ constexpr int tk_popc(unsigned x) { return x ? int(x & 1u) + tk_popc(x >> 1) : 0; }
 
-// sum_r conj(v[r]) (-1)^{popc(r & ZR)} v[r ^ X]  (the run-time sign of the
-// thread's fixed bits is applied by the caller)
-template <int NR, int X, int ZR>
-__device__ __forceinline__ float2 expect(const float2 (&v)[NR]) {
-  float2 acc = czero();
+// A Pauli string's contribution over this thread's registers, as the one
+// real number the term needs: P has (-1)^{popc(r & ZR)} (-i)^NY on the
+// pairs (r, r ^ X), so <v|P|v> restricted to the registers is
+// sgn(NY) * Re or Im of z = sum_r (-1)^{popc(r & ZR)} conj(v_r) v_{r^X}
+// (Re for even NY, Im for odd; sgn = + for NY % 4 in {0, 1}).  Two FMAs per
+// amplitude with the signs folded at compile time.
+template <int NR, int X, int ZR, int NY>
+__device__ __forceinline__ float expect_real(const float2 (&v)[NR]) {
+  constexpr bool IMZ = (NY & 1) != 0;
+  float acc = 0.f;
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
     const float2 t = v[r ^ X];
-    const float cx = fmaf(v[r].x, t.x, v[r].y * t.y);
-    const float cy = fmaf(v[r].x, t.y, -v[r].y * t.x);
-    if (tk_popc(r & ZR) & 1) {
-      acc.x -= cx;
-      acc.y -= cy;
+    const bool neg = (tk_popc(r & ZR) & 1) != 0;
+    const float vx = neg ? -v[r].x : v[r].x;
+    const float vy = neg ? -v[r].y : v[r].y;
+    if (IMZ) {
+      acc = fmaf(vx, t.y, acc);
+      acc = fmaf(-vy, t.x, acc);
     } else {
-      acc.x += cx;
-      acc.y += cy;
+      acc = fmaf(vx, t.x, acc);
+      acc = fmaf(vy, t.y, acc);
     }
   }
-  return acc;
+  return ((NY & 3) <= 1) ? acc : -acc;
 }
 
-template <int NR, int X, int ZR>
-__device__ __forceinline__ void pacc(const float2 (&v)[NR], float2 (&w)[NR], float2 cf) {
-#pragma unroll
-  for (int r = 0; r < NR; ++r) {
-    const float2 c = (tk_popc(r & ZR) & 1) ? cneg(cf) : cf;
-    w[r] = cfma(c, v[r ^ X], w[r]);
-  }
-}
-
-// the same with the register sign mask zr known only at run time
-template <int NR, int X>
-__device__ __forceinline__ float2 expectz(const float2 (&v)[NR], int zr) {
-  float2 acc = czero();
+// w += k (-i)^NY P v on the registers (k real, the thread's sign folded in):
+// (-i)^NY k is real for even NY and imaginary for odd NY, so each component
+// takes one FMA, in place.
+template <int NR, int X, int ZR, int NY>
+__device__ __forceinline__ void pacc_real(const float2 (&v)[NR], float2 (&w)[NR], float k) {
+  const float kk = ((NY & 3) == 0 || (NY & 3) == 3) ? k : -k;
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
     const float2 t = v[r ^ X];
-    const float cx = fmaf(v[r].x, t.x, v[r].y * t.y);
-    const float cy = fmaf(v[r].x, t.y, -v[r].y * t.x);
-    const bool neg = __popc(r & zr) & 1;
-    acc.x += neg ? -cx : cx;
-    acc.y += neg ? -cy : cy;
+    const float q = (tk_popc(r & ZR) & 1) ? -kk : kk;
+    if ((NY & 1) == 0) {
+      // (-i)^NY = +-1: w += q t
+      w[r].x = fmaf(q, t.x, w[r].x);
+      w[r].y = fmaf(q, t.y, w[r].y);
+    } else {
+      // (-i)^NY = -+i: w += -i q t for NY % 4 == 1 (kk = -k folds the sign)
+      w[r].x = fmaf(-q, t.y, w[r].x);
+      w[r].y = fmaf(q, t.x, w[r].y);
+    }
   }
-  return acc;
-}
-
-template <int NR, int X>
-__device__ __forceinline__ void paccz(const float2 (&v)[NR], float2 (&w)[NR], float2 cf, int zr) {
-#pragma unroll
-  for (int r = 0; r < NR; ++r) {
-    const float2 c = (__popc(r & zr) & 1) ? cneg(cf) : cf;
-    w[r] = cfma(c, v[r ^ X], w[r]);
-  }
-}
-
-// (-i)^nY
-__device__ __forceinline__ float2 ypow(int nY) {
-  return (nY & 3) == 0 ? make_float2(1.f, 0.f)
-       : (nY & 3) == 1 ? make_float2(0.f, -1.f)
-       : (nY & 3) == 2 ? make_float2(-1.f, 0.f) : make_float2(0.f, 1.f);
 }
 
 // ----------------------------------------------------------------- Pauli rotations
@@ -355,13 +342,6 @@ __device__ __forceinline__ float2 ypow(int nY) {
 // rest of the Z/Y mask is folded into the thread sign `sgn`).
 // G psi [r] = c psi[r] + (-1)^{popc(r & ZR)} q psi[r ^ X],  q = -i s (-i)^NY (-1)^sgn;
 // G^H uses -q.
-template <int NY>
-__device__ __forceinline__ float2 ypowc() {
-  return (NY & 3) == 0 ? make_float2(1.f, 0.f)
-       : (NY & 3) == 1 ? make_float2(0.f, -1.f)
-       : (NY & 3) == 2 ? make_float2(-1.f, 0.f) : make_float2(0.f, 1.f);
-}
-
 // q = -i s (-i)^NY is purely imaginary for even NY and purely real for odd
 // NY, so the pair update a' = c a + q b needs four real operations per
 // amplitude: (c a.x - q b.y, c a.y + q b.x) or (c a.x + q b.x, c a.y + q b.y).
