@@ -318,7 +318,12 @@ class Gen {
       rec->zm = op.zmask;
       rec->ny = op.nY;
       rec->zr = zr;
-      b << "const float2 cs = ld(Mt + op.off); const u32 sg = __popc(gthr & op.zm) & 1u; ";
+      // the thread's part of the Z/Y parity; none when every Z/Y bit sits in
+      // a register (rx, ry, rxx, ...: no Z bits at all)
+      if ((op.zmask & ~(uint64_t)gr(l, NR_ - 1)) == 0)
+        b << "const float2 cs = ld(Mt + op.off); const u32 sg = 0u; ";
+      else
+        b << "const float2 cs = ld(Mt + op.off); const u32 sg = __popc(gthr & op.zm) & 1u; ";
       if (fwd()) {
         b << "prot<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, cs.x, cs.y, sg, false);";
       } else {
@@ -383,23 +388,58 @@ class Gen {
         }
         b << " add_walsh<" << NR_ << ">(a); zpacc_apply<" << NR_ << ">(v, w, a); }";
       } else {
-        b << "float2 ph[" << NR_ << "];\n#pragma unroll\n for (int c = 0; c < " << NR_
-          << "; ++c) ph[c] = make_float2(1.f, 0.f);";
+        // Class products of the run's entries, then the multiplicative
+        // Walsh-Hadamard transform into per-register phases.  Which entries
+        // are still exactly 1 is known here, so a class nobody touches costs
+        // nothing, and a butterfly against a 1 is a copy or a conjugate
+        // instead of two complex products.  An entry whose Z bits all sit in
+        // registers has a fixed thread parity (even): its factor is conj(u).
+        const uint32_t regbits = gr(l, NR_ - 1);
+        std::vector<bool> one(NR_, true);
+        b << "float2 ph[" << NR_ << "];";
         for (int e = 0; e < op.k; ++e) {
           const ZEnt& z = P_.zents[op.mat_off + e];
-          b << " ph[" << z.zreg << "] = cmul(ph[" << z.zreg << "], zrun_factor(Mt + " << z.mat_off << "ll, gthr, "
-            << z.zmask << "u));";
+          std::ostringstream f;
+          if ((z.zmask & ~regbits) == 0)
+            f << "cconj(ld(Mt + " << z.mat_off << "ll))";
+          else
+            f << "zrun_factor(Mt + " << z.mat_off << "ll, gthr, " << z.zmask << "u)";
+          if (one[z.zreg]) {
+            b << " ph[" << z.zreg << "] = " << f.str() << ";";
+            one[z.zreg] = false;
+          } else {
+            b << " ph[" << z.zreg << "] = cmul(ph[" << z.zreg << "], " << f.str() << ");";
+          }
         }
-        b << " mul_walsh<" << NR_ << ">(ph);";
+        for (int j = 1; j < NR_; j <<= 1)
+          for (int c = 0; c < NR_; ++c) {
+            if (c & j) continue;
+            const int d = c | j;
+            if (one[c] && one[d]) continue;
+            if (one[d]) {
+              b << " ph[" << d << "] = ph[" << c << "];";
+              one[d] = false;
+            } else if (one[c]) {
+              b << " ph[" << c << "] = ph[" << d << "]; ph[" << d << "] = cconj(ph[" << d << "]);";
+              one[c] = false;
+            } else {
+              b << " { const float2 x = ph[" << c << "], y = ph[" << d << "]; ph[" << c << "] = cmul(x, y); ph["
+                << d << "] = cmul(x, cconj(y)); }";
+            }
+          }
         if (fwd()) {
-          b << " zrun_apply<" << NR_ << ">(v, ph);";
+          for (int r = 0; r < NR_; ++r)
+            if (!one[r]) b << " cmul_ip(v[" << r << "], ph[" << r << "]);";
         } else {
           if (!slotted.empty()) {
             b << " { float t[" << NR_ << "]; zrun_grad<" << NR_ << ">(v, w, t);";
             emit_pairs();
             b << " }";
           }
-          b << " zrun_unapply<" << NR_ << ">(v, w, ph);";
+          for (int r = 0; r < NR_; ++r)
+            if (!one[r])
+              b << " { const float2 e = cconj(ph[" << r << "]); cmul_ip(v[" << r << "], e); cmul_ip(w[" << r
+                << "], e); }";
         }
       }
     } else if (op.kind == OP_EXPECT) {
@@ -411,12 +451,15 @@ class Gen {
       rec->zr = zr;
       // a Pauli string's value is real: one real accumulation per amplitude
       // pair component, signs and the (-i)^nY phase fixed at compile time
+      const bool thread_sign = (op.zmask & ~(uint64_t)gr(l, NR_ - 1)) != 0;
       if (meas()) {
-        b << "float e = expect_real<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3)
-          << ">(v); if (__popc(gthr & op.zm) & 1) e = -e;" << reduce_real("e");
+        b << "float e = expect_real<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v);";
+        if (thread_sign) b << " if (__popc(gthr & op.zm) & 1) e = -e;";
+        b << reduce_real("e");
       } else {
-        b << "float k = kp.coef[b * kp.coef_stride + op.off]; if (__popc(gthr & op.zm) & 1) k = -k; pacc_real<"
-          << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, w, k);";
+        b << "float k = kp.coef[b * kp.coef_stride + op.off];";
+        if (thread_sign) b << " if (__popc(gthr & op.zm) & 1) k = -k;";
+        b << " pacc_real<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, w, k);";
       }
     }
     rec->sig = sig(b.str());
