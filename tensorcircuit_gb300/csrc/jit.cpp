@@ -324,12 +324,15 @@ class Gen {
         b << "const float2 cs = ld(Mt + op.off); const u32 sg = 0u; ";
       else
         b << "const float2 cs = ld(Mt + op.off); const u32 sg = __popc(gthr & op.zm) & 1u; ";
+      // three in-place shears per component pair; a rotation with cos < 0
+      // toggles the tile's sign bit (applied when the tile is stored)
       if (fwd()) {
-        b << "prot<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, cs.x, cs.y, sg, false);";
+        b << "float k, t; pneg ^= shear_params(cs.x, prot_qv<" << (op.nY & 3) << ">(cs.y, sg, false), k, t); prot_sh<"
+          << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, k, t);";
       } else {
         const bool G = op.slot >= 0;
-        b << "float g = 0.f; prot_bwd<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ", "
-          << (G ? "true" : "false") << ">(v, w, cs.x, cs.y, sg, g);";
+        b << "float g = 0.f; pneg ^= prot_bwd_sh<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3)
+          << ", " << (G ? "true" : "false") << ">(v, w, cs.x, cs.y, sg, g);";
         if (G) b << reduce_real("g");
       }
     } else if (op.kind == OP_ZRUN) {
@@ -602,6 +605,7 @@ class Gen {
     out << "  float2 v[" << NR_ << "];\n";
     if (has_mu_) out << "  float2 w[" << NR_ << "];\n";
     out << "  u32 jt = 0u, gt = 0u, sjt = 0u;\n  (void)jt; (void)sjt;\n";
+    out << "  u32 pneg = 0u;  // the tile's sign: rotations taken as -(partner)\n  (void)pneg;\n";
     out << "#pragma unroll 1\n  for (int s = 0; s < " << NS << "; ++s) {\n";
     out << "    int ob = 0, oe = 0, sob = 0, soe = 0; bool useC = false;\n";
     out << "    switch (s) {\n" << cases.str() << "    default: break;\n    }\n";
@@ -623,6 +627,20 @@ class Gen {
           << "ull + tile] = t;\n      }\n      __syncthreads();\n    }\n";
     }
     out << "  }\n";
+    if ((fwd() || bwd()) && (store_psi || store_mu)) {
+      // undo the sign bit the shear rotations left on the whole tile
+      if (live) {
+        out << "  if (pneg) {\n#pragma unroll\n    for (int r = 0; r < " << NR_ << "; ++r) {";
+        if (store_psi) out << " v[r] = cneg(v[r]);";
+        if (store_mu && has_mu_) out << " w[r] = cneg(w[r]);";
+        out << " }\n  }\n";
+      } else if (in_smem) {
+        out << "  if (pneg) {\n    for (u32 i = tid; i < " << TILE << "u; i += " << NT_ << "u) {";
+        if (store_psi) out << " smp[i] = cneg(smp[i]);";
+        if (store_mu && has_mu_) out << " smu[i] = cneg(smu[i]);";
+        out << " }\n    __syncthreads();\n  }\n";
+      }
+    }
     if (store_psi || store_mu) {
       if (live) {
         if (cur.lanes_low) {

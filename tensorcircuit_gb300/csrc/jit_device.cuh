@@ -343,63 +343,72 @@ __device__ __forceinline__ void pacc_real(const float2 (&v)[NR], float2 (&w)[NR]
 // G psi [r] = c psi[r] + (-1)^{popc(r & ZR)} q psi[r ^ X],  q = -i s (-i)^NY (-1)^sgn;
 // G^H uses -q.
 // q = -i s (-i)^NY is purely imaginary for even NY and purely real for odd
-// NY, so the pair update a' = c a + q b needs four real operations per
-// amplitude: (c a.x - q b.y, c a.y + q b.x) or (c a.x + q b.x, c a.y + q b.y).
-template <int NR, int X, int ZR, int NY>
-__device__ __forceinline__ void prot(float2 (&v)[NR], float c, float s, u32 sgn, bool adj) {
-  constexpr bool QIM = (NY & 1) == 0;
-  float qv = ((NY & 3) <= 1) ? -s : s;  // the nonzero component of q
+// NY, so the pair update a' = c a + q b, b' = c b + q' a splits into plane
+// rotations [[c, -tau], [tau, c]] of two real components (tau = +-q:
+// (a.x, b.y) and (a.y, b.x) for imaginary q, (a.x, b.x) and (a.y, b.y) for
+// real q, (v.x, v.y) for X = 0).  Paeth's
+// decomposition x -= k y; y += tau x; x -= k y with k = tau / (1 + c) does
+// it with three FMAs per component pair instead of two products and two
+// FMAs, each in place.  |k|, |tau| <= 1 needs c >= 0: a rotation with
+// c < 0 is applied as -(the rotation by phi - pi), and the -1 -- the same
+// for every amplitude of the tile -- is kept as one sign bit per thread and
+// applied when the tile is stored.
+
+// q's nonzero component for this thread (sign of P, adjoint, thread parity).
+template <int NY>
+__device__ __forceinline__ float prot_qv(float s, u32 sgn, bool adj) {
+  float qv = ((NY & 3) <= 1) ? -s : s;
   if (adj ^ (sgn != 0u)) qv = -qv;
-  // Cross terms first (products into temporaries), then one FMA per
-  // component that reads the component's own old value last: every result
-  // can take the register of the value it replaces, so the op loop's
-  // register arrays need no copies at the end of the body.
+  return qv;
+}
+
+// Shear parameters (k, t) of the rotation with cosine c and sine q; returns
+// 1 when the rotation is taken as the negative of its c >= 0 partner.
+__device__ __forceinline__ u32 shear_params(float c, float q, float& k, float& t) {
+  const u32 neg = c < 0.f ? 1u : 0u;
+  t = neg ? -q : q;
+  k = t * __frcp_rn(1.f + fabsf(c));
+  return neg;
+}
+
+// (x, y) <- [[c, -tau], [tau, c]] (x, y) with tau = t (flip = false) or -t.
+__device__ __forceinline__ void shear3(float& x, float& y, float k, float t, bool flip) {
+  const float kk = flip ? k : -k;
+  const float tt = flip ? -t : t;
+  x = fmaf(kk, y, x);
+  y = fmaf(tt, x, y);
+  x = fmaf(kk, y, x);
+}
+
+template <int NR, int X, int ZR, int NY>
+__device__ __forceinline__ void prot_sh(float2 (&v)[NR], float k, float t) {
+  constexpr bool QIM = (NY & 1) == 0;
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
-    const float qr = (tk_popc(r & ZR) & 1) ? -qv : qv;
+    const bool sr = (tk_popc(r & ZR) & 1) != 0;  // qr = -qv
     if (X == 0) {
-      if (QIM) {
-        const float px = qr * v[r].y, py = qr * v[r].x;
-        v[r].x = fmaf(c, v[r].x, -px);
-        v[r].y = fmaf(c, v[r].y, py);
-      } else {
-        const float f = c + qr;
-        v[r].x = f * v[r].x;
-        v[r].y = f * v[r].y;
-      }
+      shear3(v[r].x, v[r].y, k, t, sr);
     } else {
       const int r2 = r ^ X;
       if (r2 < r) continue;
-      const float q2 = (tk_popc(r2 & ZR) & 1) ? -qv : qv;
       if (QIM) {
-        const float pax = qr * v[r2].y, pay = qr * v[r2].x;
-        const float pbx = q2 * v[r].y, pby = q2 * v[r].x;
-        v[r].x = fmaf(c, v[r].x, -pax);
-        v[r].y = fmaf(c, v[r].y, pay);
-        v[r2].x = fmaf(c, v[r2].x, -pbx);
-        v[r2].y = fmaf(c, v[r2].y, pby);
+        shear3(v[r].x, v[r2].y, k, t, sr);
+        shear3(v[r].y, v[r2].x, k, t, !sr);
       } else {
-        const float pax = qr * v[r2].x, pay = qr * v[r2].y;
-        const float pbx = q2 * v[r].x, pby = q2 * v[r].y;
-        v[r].x = fmaf(c, v[r].x, pax);
-        v[r].y = fmaf(c, v[r].y, pay);
-        v[r2].x = fmaf(c, v[r2].x, pbx);
-        v[r2].y = fmaf(c, v[r2].y, pby);
+        shear3(v[r].x, v[r2].x, k, t, !sr);
+        shear3(v[r].y, v[r2].y, k, t, !sr);
       }
     }
   }
 }
 
 // Adjoint step: g = Im <mu|P|psi> over this thread's amplitudes (psi, mu
-// after the gate), then psi <- G^H psi, mu <- G^H mu.
+// after the gate), then psi <- G^H psi, mu <- G^H mu by shears; returns the
+// sign bit of the step (see above).
 template <int NR, int X, int ZR, int NY, bool G>
-__device__ __forceinline__ void prot_bwd(float2 (&v)[NR], float2 (&w)[NR], float c, float s, u32 sgn, float& g) {
+__device__ __forceinline__ u32 prot_bwd_sh(float2 (&v)[NR], float2 (&w)[NR], float c, float s, u32 sgn, float& g) {
   if (G) {
-    // g = Im(pt z), z = sum_r s(r) conj(w_r) v_{r^X}, pt = (+-)(-i)^NY: only
-    // Im z (even NY) or Re z (odd NY) is needed
     constexpr bool IMZ = (NY & 1) == 0;
-    // two FMAs per amplitude: the parity sign of register r is a
-    // compile-time constant, so it folds into the operands' signs
     float zc = 0.f;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
@@ -415,12 +424,14 @@ __device__ __forceinline__ void prot_bwd(float2 (&v)[NR], float2 (&w)[NR], float
         zc = fmaf(wy, t.y, zc);
       }
     }
-    // Im(pt z): NY%4 = 0 -> z.y, 1 -> -z.x, 2 -> -z.y, 3 -> z.x
     g = ((NY & 3) == 0 || (NY & 3) == 3) ? zc : -zc;
     if (sgn) g = -g;
   }
-  prot<NR, X, ZR, NY>(v, c, s, sgn, true);
-  prot<NR, X, ZR, NY>(w, c, s, sgn, true);
+  float k, t;
+  const u32 ng = shear_params(c, prot_qv<NY>(s, sgn, true), k, t);
+  prot_sh<NR, X, ZR, NY>(v, k, t);
+  prot_sh<NR, X, ZR, NY>(w, k, t);
+  return ng;
 }
 
 // ------------------------------------------------- runs of Z-string rotations
