@@ -312,6 +312,7 @@ class Gen {
         }
       }
     } else if (op.kind == OP_PROT) {
+      rec->pad = 1;  // the op loop prefetches this entry one op ahead
       int zr = 0;
       for (int i = 0; i < l.R; ++i)
         if (gbit(l.reg_tile[i]) & op.zmask) zr |= 1 << i;
@@ -320,10 +321,12 @@ class Gen {
       rec->zr = zr;
       // the thread's part of the Z/Y parity; none when every Z/Y bit sits in
       // a register (rx, ry, rxx, ...: no Z bits at all)
+      // (the forward loop prefetched the entry one op ahead into csc)
+      b << (fwd() ? "const float2 cs = csc; " : "const float2 cs = ld(Mt + op.off); ");
       if ((op.zmask & ~(uint64_t)gr(l, NR_ - 1)) == 0)
-        b << "const float2 cs = ld(Mt + op.off); const u32 sg = 0u; ";
+        b << "const u32 sg = 0u; ";
       else
-        b << "const float2 cs = ld(Mt + op.off); const u32 sg = __popc(gthr & op.zm) & 1u; ";
+        b << "const u32 sg = __popc(gthr & op.zm) & 1u; ";
       // three in-place shears per component pair; a rotation with cos < 0
       // toggles the tile's sign bit (applied when the tile is stored)
       if (fwd()) {
@@ -570,7 +573,7 @@ class Gen {
     for (size_t i = 0; i < recs.size(); ++i) {
       const OpRec& r = recs[i];
       out << (i ? ", " : "") << "{" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
-          << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", 0}";
+          << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}";
     }
     out << "};\n";
     out << "__constant__ int SO_" << pi << "[" << std::max<size_t>(so.size(), 2) << "] = {";
@@ -610,7 +613,17 @@ class Gen {
     out << "    int ob = 0, oe = 0, sob = 0, soe = 0; bool useC = false;\n";
     out << "    switch (s) {\n" << cases.str() << "    default: break;\n    }\n";
     out << "    const u32 gthr = base | gt; (void)gthr;\n    float2 C = cone(); (void)C;\n";
+    // forward: rotation entries (records with pad = 1) are loaded one op
+    // ahead, so the global load overlaps the previous op's arithmetic (in the
+    // adjoint, which holds twice the state, the extra live registers cost
+    // more than the hidden latency: measured 9.25 -> 9.59 ms)
+    if (fwd())
+      out << "    float2 csn = czero();\n    if (ob < oe && OPS_" << pi << "[ob].pad) csn = ld(Mt + OPS_" << pi
+          << "[ob].off);\n";
     out << "#pragma unroll 1\n    for (int o = ob; o < oe; ++o) {\n      const OpRec op = OPS_" << pi << "[o];\n";
+    if (fwd())
+      out << "      const float2 csc = csn; (void)csc;\n      if (o + 1 < oe && OPS_" << pi << "[o + 1].pad) csn = ld(Mt + OPS_"
+          << pi << "[o + 1].off);\n";
     out << "      switch (op.sig) {\n";
     for (size_t i = 0; i < sig_body_.size(); ++i)
       out << "        case " << i << ": { " << sig_body_[i] << " } break;\n";
