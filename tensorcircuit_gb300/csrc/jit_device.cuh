@@ -371,35 +371,43 @@ __device__ __forceinline__ u32 shear_params(float c, float q, float& k, float& t
   return neg;
 }
 
-// (x, y) <- [[c, -tau], [tau, c]] (x, y) with tau = t (flip = false) or -t.
-__device__ __forceinline__ void shear3(float& x, float& y, float k, float t, bool flip) {
-  const float kk = flip ? k : -k;
-  const float tt = flip ? -t : t;
-  x = fmaf(kk, y, x);
-  y = fmaf(tt, x, y);
-  x = fmaf(kk, y, x);
+// One of the three shears (step 0 and 2: x += -+k y, step 1: y += +-t x).
+template <int STEP>
+__device__ __forceinline__ void shear_step(float& x, float& y, float k, float t, bool flip) {
+  if (STEP == 1) y = fmaf(flip ? -t : t, x, y);
+  else x = fmaf(flip ? k : -k, y, x);
 }
 
-template <int NR, int X, int ZR, int NY>
-__device__ __forceinline__ void prot_sh(float2 (&v)[NR], float k, float t) {
+// The rotation of every register pair, issued as three sweeps (all first
+// shears, then all second, then all third): each sweep has 16 independent
+// FMAs, so the three dependent steps of one pair never wait on each other.
+template <int NR, int X, int ZR, int NY, int STEP>
+__device__ __forceinline__ void prot_sh_sweep(float2 (&v)[NR], float k, float t) {
   constexpr bool QIM = (NY & 1) == 0;
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
     const bool sr = (tk_popc(r & ZR) & 1) != 0;  // qr = -qv
     if (X == 0) {
-      shear3(v[r].x, v[r].y, k, t, sr);
+      shear_step<STEP>(v[r].x, v[r].y, k, t, sr);
     } else {
       const int r2 = r ^ X;
       if (r2 < r) continue;
       if (QIM) {
-        shear3(v[r].x, v[r2].y, k, t, sr);
-        shear3(v[r].y, v[r2].x, k, t, !sr);
+        shear_step<STEP>(v[r].x, v[r2].y, k, t, sr);
+        shear_step<STEP>(v[r].y, v[r2].x, k, t, !sr);
       } else {
-        shear3(v[r].x, v[r2].x, k, t, !sr);
-        shear3(v[r].y, v[r2].y, k, t, !sr);
+        shear_step<STEP>(v[r].x, v[r2].x, k, t, !sr);
+        shear_step<STEP>(v[r].y, v[r2].y, k, t, !sr);
       }
     }
   }
+}
+
+template <int NR, int X, int ZR, int NY>
+__device__ __forceinline__ void prot_sh(float2 (&v)[NR], float k, float t) {
+  prot_sh_sweep<NR, X, ZR, NY, 0>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 1>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 2>(v, k, t);
 }
 
 // Adjoint step: g = Im <mu|P|psi> over this thread's amplitudes (psi, mu
@@ -429,8 +437,13 @@ __device__ __forceinline__ u32 prot_bwd_sh(float2 (&v)[NR], float2 (&w)[NR], flo
   }
   float k, t;
   const u32 ng = shear_params(c, prot_qv<NY>(s, sgn, true), k, t);
-  prot_sh<NR, X, ZR, NY>(v, k, t);
-  prot_sh<NR, X, ZR, NY>(w, k, t);
+  // psi and mu sweeps interleaved: 32 independent FMAs per step
+  prot_sh_sweep<NR, X, ZR, NY, 0>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 0>(w, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 1>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 1>(w, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 2>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 2>(w, k, t);
   return ng;
 }
 
