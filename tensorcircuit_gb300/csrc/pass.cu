@@ -49,6 +49,23 @@ __device__ __forceinline__ float2 ldm(const float2* p) {
   return __ldg(reinterpret_cast<const float2*>(p));
 }
 
+// v <- p v in place (cross products first, then one FMA per component that
+// reads its own old value last: the op loop's register arrays need no copies)
+__device__ __forceinline__ void cmul_ip(float2& v, float2 p) {
+  const float tx = p.y * v.y, ty = p.y * v.x;
+  v.x = fmaf(p.x, v.x, -tx);
+  v.y = fmaf(p.x, v.y, ty);
+}
+
+// sum of one real value over the first nl lanes (gradients are real)
+__device__ __forceinline__ float warp_sum1(float v, int nl) {
+  const unsigned mask = nl >= 32 ? 0xffffffffu : ((1u << nl) - 1u);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    if (o < nl) v += __shfl_xor_sync(mask, v, o);
+  return v;
+}
+
 // Sum over the lanes of a warp; blocks smaller than a warp (tiny tiles) use
 // only their nl = blockDim.x lanes.
 __device__ __forceinline__ float2 warp_sum(float2 v, int nl) {
@@ -843,8 +860,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
             float g = dispatch_prot_dot<R>(op.xreg, v, w, zr, qim);
             if (ny == 1 || ny == 2) g = -g;
             if (sg) g = -g;
-            const float2 t = warp_sum(make_float2(g, 0.f), nl);
-            if (lane == 0) sm_slot[warp * A.max_slots + op.slot] = t;
+            const float t = warp_sum1(g, nl);
+            if (lane == 0) sm_slot[warp * A.max_slots + op.slot] = make_float2(t, 0.f);
           }
           dispatch_prot<R>(op.xreg, v, cs.x, -qv, zr, qim);
           dispatch_prot<R>(op.xreg, w, cs.x, -qv, zr, qim);
@@ -860,8 +877,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
             const ZEnt ze = A.prog.zents[op.mat_off + e];
             float g = class_pick<R>(t, ze.zreg);
             if (__popc(gthr & ze.zmask) & 1) g = -g;
-            const float2 s = warp_sum(make_float2(g, 0.f), nl);
-            if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = s;
+            const float s = warp_sum1(g, nl);
+            if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = make_float2(s, 0.f);
           }
         } else if (MODE == MODE_PACC) {
           // mu += (sum_t c_t s_t(x)) psi: class sums, one transform
@@ -891,7 +908,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
           mul_walsh<R>(ph);
           if (MODE == MODE_FWD) {
 #pragma unroll
-            for (int r = 0; r < NR; ++r) v[r] = cmul(ph[r], v[r]);
+            for (int r = 0; r < NR; ++r) cmul_ip(v[r], ph[r]);
           } else {
             if (op.slot >= 0) {
               // dL/dphi_e = sum_x s_e(x) Im(conj(mu_x) psi_x) at the run's output
@@ -904,15 +921,15 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
                 if (ze.slot < 0) continue;
                 float g = class_pick<R>(t, ze.zreg);
                 if (__popc(gthr & ze.zmask) & 1) g = -g;
-                const float2 s = warp_sum(make_float2(g, 0.f), nl);
-                if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = s;
+                const float s = warp_sum1(g, nl);
+                if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = make_float2(s, 0.f);
               }
             }
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
               const float2 c = cconj(ph[r]);
-              v[r] = cmul(c, v[r]);
-              w[r] = cmul(c, w[r]);
+              cmul_ip(v[r], c);
+              cmul_ip(w[r], c);
             }
           }
         }
