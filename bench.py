@@ -963,7 +963,7 @@ def run_warmstart(args, rank, world):
     adjoint Adam (``--instances`` chains x 300 steps), the 31-256-256-186
     network trained with the project's kernels, then held-out chains
     optimised for 300 steps from the network's angles and from random ones,
-    judged against the exact free-fermion ground energy."""
+    scored against the exact free-fermion ground energy."""
     import torch
 
     import tensorcircuit_gb300 as tc

@@ -8,7 +8,7 @@ energy.  A small network (31 -> 256 -> 256 -> 186, GELU, float32 weights,
 bfloat16 activations) learns to map couplings (J, h) to good starting
 angles from optimised angles that the simulator itself produces; at
 inference its output replaces the random starting point, which stays the
-fallback.  The exact ground energy (free fermions, float64) judges both.
+fallback.  Both are scored against the exact ground energy (free fermions, float64).
 
 Everything on the GPU is this project's code: the energies and gradients
 come from the engine's batched adjoint sweep (``backend.vvag``), the
