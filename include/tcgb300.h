@@ -197,6 +197,23 @@ int tcg_sample(const void* psi, int32_t nqubits, int64_t batch, const float* u,
                int64_t u_stride, int64_t nshots, int64_t* out, void* scratch,
                size_t scratch_bytes, void* stream);
 
+/* Replaces: the Monte-Carlo step of Circuit._general_kraus_2
+ * (tensorcircuit/circuit.py:635-694): branch probabilities
+ * p_i = sum_s Re(ev[b][s]) coef[i][s] (ev: complex64 [batch][nstrings] Pauli
+ * expectations, coef: fp32 [nkraus][nstrings] expansion of K_i^dag K_i), the
+ * pick of Circuit.unitary_kraus (tensorcircuit/circuit.py:541-556) from the
+ * uniform x[b * x_stride] (x_stride 0 shares one draw), and the rescale
+ * 1 / (sqrt(p_pick) + 1e-10) as complex64 (imaginary part 0).  p receives
+ * the fp32 [batch][nkraus] probabilities. */
+int tcg_kraus_pick(const void* ev, int32_t nstrings, const float* coef, int32_t nkraus,
+                   const float* x, int64_t x_stride, int64_t batch, int32_t* pick,
+                   void* scale, float* p, void* stream);
+/* Backward of tcg_kraus_pick: gev[b][s] = (g_b (-1 / (sqrt(p_r) + 1e-10)^2)
+ * / (2 sqrt(p_r)) coef[r][s], 0) for g_b = Re(gscale[b]), r = pick[b]. */
+int tcg_kraus_pick_backward(const void* gscale, const int32_t* pick, const float* p,
+                            int32_t nkraus, const float* coef, int32_t nstrings,
+                            int64_t batch, void* gev, void* stream);
+
 /* Replaces: BaseCircuit.probability (tensorcircuit/basecircuit.py:510-523):
  * p[a] = |psi[a]|^2 in fp32 (computed as re^2 + im^2). */
 int tcg_probability(const void* psi, int64_t len, float* p, void* stream);

@@ -99,6 +99,8 @@ SIGNATURES = [
     ("tcg_expect_pauli_noalloc", ctypes.c_int, [_P, _I32, _I64, ctypes.POINTER(TcgPauli), _I32, _P, _P]),
     ("tcg_sample_scratch_bytes", _SZ, [_I32, _I64]),
     ("tcg_sample", ctypes.c_int, [_P, _I32, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),
+    ("tcg_kraus_pick", ctypes.c_int, [_P, _I32, _P, _I32, _P, _I64, _I64, _P, _P, _P, _P]),
+    ("tcg_kraus_pick_backward", ctypes.c_int, [_P, _P, _P, _I32, _P, _I32, _I64, _P, _P]),
     ("tcg_probability", ctypes.c_int, [_P, _I64, _P, _P]),
     ("tcg_inner_scratch_bytes", _SZ, [_I64, _I64]),
     ("tcg_inner", ctypes.c_int, [_P, _P, _I64, _I64, _P, _P, _SZ, _P]),

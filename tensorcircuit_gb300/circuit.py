@@ -385,20 +385,26 @@ def _unitary_kraus_prep(mats: Sequence[np.ndarray], prob: Optional[Sequence[floa
     return r
 
 
+def _uniform(status: Any, dev: torch.device) -> torch.Tensor:
+    """The trajectory's uniform draw as fp32 on the device: ``status`` (its
+    real part), or a fresh draw when it is None."""
+    if status is None:
+        return torch.rand((), device=dev)
+    if isinstance(status, torch.Tensor):
+        x = torch.real(status) if status.is_complex() else status
+        x = x.to(device=dev, dtype=torch.float32)
+        if x.dim() > 0 and x.numel() == 1:
+            x = x.reshape(())
+        return x
+    return torch.full((), float(np.real(np.asarray(status).reshape(-1)[0])), dtype=torch.float32, device=dev)
+
+
 def _pick(status: Any, cum: torch.Tensor, dev: torch.device) -> torch.Tensor:
     """The Kraus pick of tensorcircuit/circuit.py:541-556: for a uniform x
     and cumulative probabilities c, int(sum_{i<l-1} sign(x - c_i) / 2 +
     (l - 1) / 2) -- the number of c_i below x plus half the number equal to
     x, truncated.  ``cum`` may carry batch dimensions."""
-    if status is None:
-        x = torch.rand((), device=dev)
-    elif isinstance(status, torch.Tensor):
-        x = torch.real(status) if status.is_complex() else status
-        x = x.to(device=dev, dtype=torch.float32)
-        if x.dim() > 0 and x.numel() == 1:
-            x = x.reshape(())
-    else:
-        x = torch.full((), float(np.real(np.asarray(status).reshape(-1)[0])), dtype=torch.float32, device=dev)
+    x = _uniform(status, dev)
     l = cum.shape[-1]
     if l == 1:
         return torch.zeros_like(x, dtype=torch.int32)
@@ -764,11 +770,18 @@ class Circuit:
             key, kdev, coef, diag = _kraus_prep(mats, k, dev)
         psi, psi_eng, anchor, run, n_eng = self._engine_state()
         spec = _kraus_spec(idx, n_eng)
-        ev = torch.real(eng.ExpectFn.apply(psi_eng, anchor, spec, run))
-        p = ev @ coef.t()
-        r = _pick(status, torch.cumsum(p, -1), dev)
-        pr = torch.sum(torch.where(r.unsqueeze(-1) == _arange(len(mats), dev), p, 0.0), -1)
-        scale = (1.0 / (torch.sqrt(pr) + 1e-10)).to(C64)
+        evc = eng.ExpectFn.apply(psi_eng, anchor, spec, run)
+        if is_t or with_prob:
+            # p itself is wanted (or depends on the operators' gradients):
+            # the same steps as torch operations
+            ev = torch.real(evc)
+            p = ev @ coef.t()
+            r = _pick(status, torch.cumsum(p, -1), dev)
+            pr = torch.sum(torch.where(r.unsqueeze(-1) == _arange(len(mats), dev), p, 0.0), -1)
+            scale = (1.0 / (torch.sqrt(pr) + 1e-10)).to(C64)
+        else:
+            # constant operators: probabilities, pick and rescale in one kernel
+            r, scale, p = eng.KrausPickFn.apply(evc, coef, _uniform(status, dev))
         ir = {"gatef": "general_kraus", "index": tuple(index), "name": name or "general_kraus", "split": None,
               "mpo": False, "parameters": {"status": status}}
         self._seg_ops += len(self._ops)

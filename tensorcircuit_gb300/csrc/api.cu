@@ -425,6 +425,24 @@ int tcg_sample(const void* psi, int32_t nqubits, int64_t batch, const float* u, 
                                scratch, as_stream(stream)));
 }
 
+int tcg_kraus_pick(const void* ev, int32_t nstrings, const float* coef, int32_t nkraus, const float* x,
+                   int64_t x_stride, int64_t batch, int32_t* pick, void* scale, float* p, void* stream) {
+  if (batch < 0 || nstrings < 1 || nkraus < 1 || x_stride < 0) return TCG_ERR_INVALID_ARG;
+  if (batch == 0) return TCG_OK;
+  if (!ev || !coef || !x || !pick || !scale || !p) return TCG_ERR_INVALID_ARG;
+  return cuda_rc(launch_kraus_pick(static_cast<const float2*>(ev), nstrings, coef, nkraus, x, x_stride, batch, pick,
+                                   static_cast<float2*>(scale), p, as_stream(stream)));
+}
+
+int tcg_kraus_pick_backward(const void* gscale, const int32_t* pick, const float* p, int32_t nkraus,
+                            const float* coef, int32_t nstrings, int64_t batch, void* gev, void* stream) {
+  if (batch < 0 || nstrings < 1 || nkraus < 1) return TCG_ERR_INVALID_ARG;
+  if (batch == 0) return TCG_OK;
+  if (!gscale || !pick || !p || !coef || !gev) return TCG_ERR_INVALID_ARG;
+  return cuda_rc(launch_kraus_pick_bwd(static_cast<const float2*>(gscale), pick, p, nkraus, coef, nstrings, batch,
+                                       static_cast<float2*>(gev), as_stream(stream)));
+}
+
 int tcg_probability(const void* psi, int64_t len, float* p, void* stream) {
   if (len < 0 || (len > 0 && (!psi || !p))) return TCG_ERR_INVALID_ARG;
   return cuda_rc(launch_probability(static_cast<const float2*>(psi), len, p, as_stream(stream)));

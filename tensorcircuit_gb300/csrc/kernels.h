@@ -122,4 +122,10 @@ size_t sample_scratch_bytes(int n, int64_t batch);
 cudaError_t launch_sample(const float2* psi, int n, int64_t batch, const float* u, int64_t u_stride,
                           int64_t nshots, int64_t* out, void* scratch, cudaStream_t st);
 
+// Monte-Carlo Kraus pick and its backward
+cudaError_t launch_kraus_pick(const float2* ev, int S, const float* coef, int K, const float* x, int64_t x_stride,
+                              int64_t B, int32_t* pick, float2* scale, float* p, cudaStream_t st);
+cudaError_t launch_kraus_pick_bwd(const float2* gscale, const int32_t* pick, const float* p, int K,
+                                  const float* coef, int S, int64_t B, float2* gev, cudaStream_t st);
+
 }  // namespace tcg

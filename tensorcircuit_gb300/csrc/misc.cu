@@ -441,4 +441,66 @@ cudaError_t launch_sample(const float2* psi, int n, int64_t batch, const float* 
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- Kraus pick
+// One thread per trajectory.  p_i = sum_s Re(ev_s) coef[i, s] (the Pauli
+// expansion of <K_i^dag K_i>), running sums c_i in index order, the pick
+// r = (int)(sum_{i<K-1} sign(x - c_i) / 2 + (K - 1) / 2) and the rescale
+// 1 / (sqrt(p_r) + 1e-10), written as a complex number with zero imaginary
+// part.  p (K floats per trajectory) is kept for the backward.
+__global__ void kraus_pick_kernel(const float2* __restrict__ ev, int S, const float* __restrict__ coef, int K,
+                                  const float* __restrict__ x, int64_t x_stride, int64_t B,
+                                  int32_t* __restrict__ pick, float2* __restrict__ scale, float* __restrict__ p) {
+  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const float2* e = ev + b * S;
+  float* pb = p + b * K;
+  const float xb = x[b * x_stride];
+  float c = 0.f, sg = 0.f;
+  for (int i = 0; i < K; ++i) {
+    float acc = 0.f;
+    for (int s = 0; s < S; ++s) acc = fmaf(e[s].x, coef[i * S + s], acc);
+    pb[i] = acc;
+    c += acc;
+    if (i < K - 1) {
+      const float d = xb - c;
+      sg += d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f);
+    }
+  }
+  int r = (int)(sg * 0.5f + float(K - 1) * 0.5f);
+  r = r < 0 ? 0 : (r > K - 1 ? K - 1 : r);
+  pick[b] = r;
+  scale[b] = make_float2(1.f / (sqrtf(pb[r]) + 1e-10f), 0.f);
+}
+
+// d/d Re(ev_s) of the rescale: g (-1 / (sqrt(p_r) + 1e-10)^2) / (2 sqrt(p_r))
+// coef[r, s]; the picks themselves carry no gradient.
+__global__ void kraus_pick_bwd_kernel(const float2* __restrict__ gscale, const int32_t* __restrict__ pick,
+                                      const float* __restrict__ p, int K, const float* __restrict__ coef, int S,
+                                      int64_t B, float2* __restrict__ gev) {
+  const int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int r = pick[b];
+  const float pr = p[b * K + r];
+  const float sq = sqrtf(pr);
+  const float den = sq + 1e-10f;
+  const float gp = -gscale[b].x / (den * den) / (2.f * sq);
+  for (int s = 0; s < S; ++s) gev[b * S + s] = make_float2(gp * coef[r * S + s], 0.f);
+}
+
+cudaError_t launch_kraus_pick(const float2* ev, int S, const float* coef, int K, const float* x, int64_t x_stride,
+                              int64_t B, int32_t* pick, float2* scale, float* p, cudaStream_t st) {
+  if (B <= 0) return cudaSuccess;
+  count_launch();
+  kraus_pick_kernel<<<(unsigned)((B + 127) / 128), 128, 0, st>>>(ev, S, coef, K, x, x_stride, B, pick, scale, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_kraus_pick_bwd(const float2* gscale, const int32_t* pick, const float* p, int K,
+                                  const float* coef, int S, int64_t B, float2* gev, cudaStream_t st) {
+  if (B <= 0) return cudaSuccess;
+  count_launch();
+  kraus_pick_bwd_kernel<<<(unsigned)((B + 127) / 128), 128, 0, st>>>(gscale, pick, p, K, coef, S, B, gev);
+  return cudaGetLastError();
+}
+
 }  // namespace tcg

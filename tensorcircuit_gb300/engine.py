@@ -365,6 +365,109 @@ class ExpectFn(torch.autograd.Function):
         return ExpectFn.apply(psi, anchor, spec, run), 0
 
 
+class KrausPickFn(torch.autograd.Function):
+    """Monte-Carlo branch choice of a general channel (``tcg_kraus_pick``):
+    (Pauli expectations ev [..., S] complex64, constant expansion coef
+    [K, S] fp32, uniforms x) -> (pick int32 [...], rescale 1 / (sqrt(p_pick)
+    + 1e-10) complex64 [...], p fp32 [..., K]).  Only the rescale carries a
+    gradient (to Re ev); the pick and p are constants of the trajectory."""
+
+    @staticmethod
+    def forward(ev: torch.Tensor, coef: torch.Tensor, x: torch.Tensor) -> Tuple[torch.Tensor, torch.Tensor,
+                                                                                  torch.Tensor]:
+        lib = nat.load()
+        S = ev.shape[-1]
+        K = coef.shape[0]
+        lead = tuple(torch.broadcast_shapes(ev.shape[:-1], x.shape))
+        e = ev.detach().expand(lead + (S,)).resolve_conj().resolve_neg().contiguous()
+        xd = x.detach().to(torch.float32)
+        if xd.numel() == 1:
+            xf, xs = xd.reshape(1).contiguous(), 0
+        else:
+            xf, xs = xd.expand(lead).contiguous(), 1
+        cf = coef.detach().to(torch.float32).contiguous()
+        B = e.numel() // S
+        pick = torch.empty(lead, dtype=torch.int32, device=ev.device)
+        scale = torch.empty(lead, dtype=C64, device=ev.device)
+        p = torch.empty(lead + (K,), dtype=torch.float32, device=ev.device)
+        nat.check(lib.tcg_kraus_pick(nat.ptr(e), S, nat.ptr(cf), K, nat.ptr(xf), xs, B, nat.ptr(pick),
+                                     nat.ptr(scale), nat.ptr(p), _stream()), "kraus pick")
+        return pick, scale, p
+
+    @staticmethod
+    def setup_context(ctx: Any, inputs: Tuple[Any, ...], output: Any) -> None:
+        ev, coef, _ = inputs
+        pick, _, p = output
+        ctx.mark_non_differentiable(pick, p)
+        ctx.save_for_backward(pick, p)
+        ctx.coef = coef.detach().to(torch.float32).contiguous()
+        ctx.ev_shape = ev.shape
+
+    @staticmethod
+    def backward(ctx: Any, g_pick: Any, g_scale: Any, g_p: Any) -> Any:
+        if g_scale is None:
+            return None, None, None
+        pick, p = ctx.saved_tensors
+        gev = KrausPickBwdFn.apply(g_scale, pick, p, ctx.coef)
+        if gev.shape != ctx.ev_shape:
+            gev = gev.sum_to_size(ctx.ev_shape)
+        return gev, None, None
+
+    @staticmethod
+    def vmap(info: Any, in_dims: Tuple[Any, ...], ev: torch.Tensor, coef: torch.Tensor, x: torch.Tensor) -> Any:
+        ed, cd, xd = in_dims
+        if cd is not None:
+            raise NotImplementedError("KrausPickFn: batched Kraus expansions")
+        if ed is None and xd is None:
+            return KrausPickFn.apply(ev, coef, x), (None, None, None)
+        ev = ev.movedim(ed, 0) if ed is not None else ev.unsqueeze(0)
+        x = x.movedim(xd, 0) if xd is not None else x.unsqueeze(0)
+        return KrausPickFn.apply(ev, coef, x), (0, 0, 0)
+
+
+class KrausPickBwdFn(torch.autograd.Function):
+    """Backward of :class:`KrausPickFn` (``tcg_kraus_pick_backward``):
+    (rescale cotangent [...], pick [...], p [..., K], coef [K, S]) -> the
+    cotangent of ev [..., S].  A Function of its own so that, like the
+    adjoint sweep, it runs on plain tensors under ``vmap``."""
+
+    @staticmethod
+    def forward(gscale: torch.Tensor, pick: torch.Tensor, p: torch.Tensor, coef: torch.Tensor) -> torch.Tensor:
+        lib = nat.load()
+        K, S = coef.shape
+        lead = tuple(torch.broadcast_shapes(gscale.shape, pick.shape, p.shape[:-1]))
+        gs = gscale.detach().to(C64).expand(lead).resolve_conj().resolve_neg().contiguous()
+        pk = pick.expand(lead).contiguous()
+        pp = p.expand(lead + (K,)).contiguous()
+        cf = coef.detach().to(torch.float32).contiguous()
+        gev = torch.empty(lead + (S,), dtype=C64, device=gs.device)
+        nat.check(lib.tcg_kraus_pick_backward(nat.ptr(gs), nat.ptr(pk), nat.ptr(pp), K, nat.ptr(cf), S, gs.numel(),
+                                              nat.ptr(gev), _stream()), "kraus pick backward")
+        return gev
+
+    @staticmethod
+    def setup_context(ctx: Any, inputs: Tuple[Any, ...], output: Any) -> None:
+        pass
+
+    @staticmethod
+    def backward(ctx: Any, *grads: Any) -> Any:
+        raise NotImplementedError("second derivatives through the Kraus pick are not supported")
+
+    @staticmethod
+    def vmap(info: Any, in_dims: Tuple[Any, ...], gscale: torch.Tensor, pick: torch.Tensor, p: torch.Tensor,
+             coef: torch.Tensor) -> Any:
+        gd, kd, pd, cd = in_dims
+        if cd is not None:
+            raise NotImplementedError("KrausPickBwdFn: batched Kraus expansions")
+        if gd is None and kd is None and pd is None:
+            return KrausPickBwdFn.apply(gscale, pick, p, coef), None
+
+        def mv(x: torch.Tensor, d: Optional[int]) -> torch.Tensor:
+            return x.movedim(d, 0) if d is not None else x.unsqueeze(0)
+
+        return KrausPickBwdFn.apply(mv(gscale, gd), mv(pick, kd), mv(p, pd), coef), 0
+
+
 class SampleFn(torch.autograd.Function):
     """Inverse-CDF sampling with given uniforms (``tcg_sample``); int64 out."""
 

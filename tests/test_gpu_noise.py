@@ -330,3 +330,63 @@ def test_noisy_vvag_graph_replay_matches_eager(tc):
         np.testing.assert_allclose(_np(g1), _np(g0), rtol=1e-4, atol=1e-5)
     assert jf.capture_errors() == []
     assert any(e["graph"] is not None for e in jf.cache.values())
+
+
+def _pick_torch(ev, coef, x):
+    """The general-channel branch step as fp32 torch operations (the steps of
+    tensorcircuit/circuit.py:541-556 and :682-687)."""
+    p = torch.real(ev) @ coef.t()
+    cum = torch.cumsum(p, -1)
+    l = cum.shape[-1]
+    if l == 1:
+        r = torch.zeros(p.shape[:-1], dtype=torch.int32, device=p.device)
+    else:
+        s = torch.sign(x.unsqueeze(-1) - cum[..., : l - 1]).sum(-1)
+        r = (s * 0.5 + (l - 1) * 0.5).to(torch.int32)
+    pr = torch.gather(p, -1, r.long().unsqueeze(-1)).squeeze(-1)
+    return r, (1.0 / (torch.sqrt(pr) + 1e-10)).to(torch.complex64), p
+
+
+@pytest.mark.parametrize("nk,ns", [(1, 4), (2, 4), (4, 16)])
+def test_kraus_pick_kernel_matches_torch_steps(tc, nk, ns):
+    """tcg_kraus_pick against the same steps in torch: picks exact (ties
+    x == c_i included: dyadic inputs make every sum exact), rescale and p
+    within 1e-6 relative, the gradient to Re(ev) within 1e-5, and the vmap
+    rule equal to the unbatched call."""
+    from tensorcircuit_gb300 import engine as eng
+
+    rng = np.random.default_rng(40 + nk)
+    dev = torch.device("cuda")
+    B = 257
+    ev_np = rng.integers(1, 9, (B, ns)) / 8.0 + 1j * rng.standard_normal((B, ns))
+    coef_np = rng.integers(1, 5, (nk, ns)) / (16.0 * ns)
+    ev = torch.as_tensor(ev_np.astype(np.complex64), device=dev)
+    coef = torch.as_tensor(coef_np.astype(np.float32), device=dev)
+    cum = np.cumsum(np.real(ev_np) @ coef_np.T, -1)
+    x_np = rng.random(B) * cum[:, -1]
+    x_np[:40] = cum[:40, max(nk - 3, 0)]   # ties with a running sum
+    x = torch.as_tensor(x_np.astype(np.float32), device=dev)
+    w = torch.as_tensor(rng.standard_normal(B).astype(np.float32), device=dev)
+
+    e1 = ev.clone().requires_grad_(True)
+    r1, s1, p1 = eng.KrausPickFn.apply(e1, coef, x)
+    (g1,) = torch.autograd.grad((torch.real(s1) * w).sum(), e1)
+    e0 = ev.clone().requires_grad_(True)
+    r0, s0, p0 = _pick_torch(e0, coef, x)
+    (g0,) = torch.autograd.grad((torch.real(s0) * w).sum(), e0)
+
+    assert torch.equal(r1, r0)
+    if nk > 1:
+        assert len(set(_np(r1).tolist())) > 1
+    np.testing.assert_allclose(_np(p1), _np(p0), rtol=1e-6)
+    np.testing.assert_allclose(_np(s1), _np(s0), rtol=1e-6)
+    np.testing.assert_allclose(_np(g1), _np(g0), rtol=1e-5, atol=1e-6)
+    assert float(torch.abs(torch.imag(g1)).max()) == 0.0
+
+    rv, sv_, pv = torch.func.vmap(lambda e, xx: eng.KrausPickFn.apply(e, coef, xx))(ev, x)
+    assert torch.equal(rv, r1)
+    np.testing.assert_allclose(_np(sv_), _np(s1), rtol=0)
+    # one shared draw for every row (x_stride 0)
+    rs, _, _ = eng.KrausPickFn.apply(ev, coef, x[7])
+    r7, _, _ = _pick_torch(ev, coef, x[7].expand(B))
+    assert torch.equal(rs, r7)
