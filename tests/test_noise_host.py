@@ -130,3 +130,86 @@ def test_pauli_expansion_of_kraus_products():
         d = 1 << kk
         coef = np.array([[np.real(np.trace(m.conj().T @ m @ s)) / d for _, s in strings] for m in kraus])
         np.testing.assert_allclose(coef @ np.array(ev), nz.kraus_probs(psi, n, kraus, qubits), atol=1e-12)
+
+
+class _FakePickLib:
+    """Stands in for the library's two Kraus-pick entry points on CPU
+    tensors (the pointer helper is patched to pass tensors through), so the
+    autograd and vmap wiring around them can run without a GPU."""
+
+    def tcg_kraus_pick(self, e, S, cf, K_, xf, xs, B, pick, scale, p, st):
+        ev = e.reshape(B, S)
+        x = xf.reshape(-1).expand(B) if xs == 0 else xf.reshape(-1)
+        pp = torch.real(ev) @ cf.t()
+        r = _pick(x, torch.cumsum(pp, -1), torch.device("cpu"))
+        pr = torch.gather(pp, -1, r.long().unsqueeze(-1)).squeeze(-1)
+        pick.view(-1).copy_(r)
+        p.view(-1).copy_(pp.reshape(-1))
+        scale.view(-1).copy_((1.0 / (torch.sqrt(pr) + 1e-10)).to(torch.complex64))
+        return 0
+
+    def tcg_kraus_pick_backward(self, gs, pk, pp, K_, cf, S, B, gev, st):
+        r = pk.reshape(-1).long()
+        pr = pp.reshape(B, K_).gather(-1, r.unsqueeze(-1)).squeeze(-1)
+        den = torch.sqrt(pr) + 1e-10
+        gp = -gs.reshape(-1).real / (den * den) / (2 * torch.sqrt(pr))
+        gev.view(B, S).copy_((gp.unsqueeze(-1) * cf[r]).to(torch.complex64))
+        return 0
+
+
+def test_kraus_pick_functions_under_vmap_and_grad(monkeypatch):
+    """KrausPickFn / KrausPickBwdFn wiring: values and gradients of
+    vmap(grad_and_value(f)) through the Functions equal those of the same
+    steps written as torch operations -- batched and shared draws, batched
+    and unbatched expectations, two chained channels -- and every tensor
+    handed to the library has storage (no functorch wrapper reaches it)."""
+    from tensorcircuit_gb300 import _native as nat
+    from tensorcircuit_gb300 import engine as eng
+
+    monkeypatch.setattr(nat, "load", lambda: _FakePickLib())
+    monkeypatch.setattr(nat, "ptr", lambda t: (t.data_ptr(), t)[1])
+    monkeypatch.setattr(nat, "check", lambda rc, name: None)
+    monkeypatch.setattr(eng, "_stream", lambda: 0)
+    g = torch.Generator().manual_seed(3)
+    K_, S, B = 4, 16, 6
+    coef = torch.rand(K_, S, generator=g) * 0.1 + 0.01
+    W = torch.randn(S, S, generator=g) * 0.1
+    theta = torch.randn(S, generator=g)
+    a = torch.randn(B, S, generator=g)
+    xb = torch.rand(B, generator=g) * 3
+
+    def evf(t, shift):
+        re = torch.sigmoid(t @ W + shift)
+        return torch.complex(re, torch.zeros_like(re))
+
+    def step_torch(ev, x):
+        p = torch.real(ev) @ coef.t()
+        r = _pick(x, torch.cumsum(p, -1), torch.device("cpu"))
+        pr = torch.sum(torch.where(r.unsqueeze(-1) == torch.arange(K_), p, 0.0), -1)
+        return (1.0 / (torch.sqrt(pr) + 1e-10)).to(torch.complex64)
+
+    def step_fn(ev, x):
+        return eng.KrausPickFn.apply(ev, coef, x)[1]
+
+    def chained(step):
+        def f(t, shift, x):
+            s = step(evf(t, shift), x)
+            s2 = step(evf(t * torch.real(s), 0.0), x * 0.5)
+            return torch.real(s2) + 0.3 * torch.real(s)
+        return f
+
+    def shared(step):
+        return lambda t, shift: torch.real(step(evf(t, shift), torch.tensor(1.3)))
+
+    def unbatched_ev(step):
+        return lambda t, x: torch.real(step(evf(t, 0.0), x))
+
+    cases = [(chained, (None, 0, 0), (theta, a, xb)), (shared, (None, 0), (theta, a)),
+             (unbatched_ev, (None, 0), (theta, xb))]
+    for make, dims, args in cases:
+        vg = [torch.func.vmap(torch.func.grad_and_value(make(s)), in_dims=dims)(*args) for s in (step_fn, step_torch)]
+        torch.testing.assert_close(vg[0][1], vg[1][1], rtol=1e-6, atol=0)
+        torch.testing.assert_close(vg[0][0], vg[1][0], rtol=1e-5, atol=1e-7)
+    g1 = torch.func.grad(unbatched_ev(step_fn))(theta, xb[0])
+    g0 = torch.func.grad(unbatched_ev(step_torch))(theta, xb[0])
+    torch.testing.assert_close(g1, g0, rtol=1e-5, atol=1e-7)
