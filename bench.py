@@ -182,8 +182,9 @@ def gpu_plain_ad(sample_circuits=8, steps=2):
 def run_reference_arm(args, rank):
     if rank != 0:
         return
+    # about 3 s per step on 16 cores: at most 3 timed and 5 warm-up steps
     steps = max(1, min(args.steps, 3))
-    warmup = min(args.warmup, 1)
+    warmup = min(args.warmup, 5)
     cb = cpu_reference(steps, warmup)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True,
@@ -337,7 +338,7 @@ def run_gb300_arm(args, rank, world):
     cpu = None
     plain_ad = None
     if world == 1 and not args.no_cpu:
-        cpu = cpu_reference(steps=1, warmup=0)
+        cpu = cpu_reference(steps=1, warmup=1)
         plain_ad = gpu_plain_ad()
     line = {
         "metric": METRIC, "value": circ_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
