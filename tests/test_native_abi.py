@@ -41,4 +41,14 @@ def test_host_side_errors_without_gpu():
     assert lib.tcg_forward(None, None, 1, None, 0, None) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_sample(None, 10, 1, None, 0, 1, None, None, 0, None) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_sample_scratch_bytes(10, 2) >= 2 * 8 * 1024
+    # Kraus pick: bad sizes are refused, an empty batch is a no-op, and a
+    # non-empty batch without buffers is refused -- all before any launch
+    assert lib.tcg_kraus_pick(None, 4, None, 2, None, 0, -1, None, None, None, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_kraus_pick(None, 0, None, 2, None, 0, 1, None, None, None, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_kraus_pick(None, 4, None, 2, None, -1, 1, None, None, None, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_kraus_pick(None, 4, None, 2, None, 0, 0, None, None, None, None) == nat.TCG_OK
+    assert lib.tcg_kraus_pick(None, 4, None, 2, None, 0, 3, None, None, None, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_kraus_pick_backward(None, None, None, 0, None, 4, 1, None, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_kraus_pick_backward(None, None, None, 2, None, 4, 0, None, None) == nat.TCG_OK
+    assert lib.tcg_kraus_pick_backward(None, None, None, 2, None, 4, 5, None, None) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_launch_count() == 0
