@@ -5,7 +5,10 @@ Workload (one step): the hardware-efficient ansatz on n=20 qubits, 8 layers
 parameter vectors ~U[0, 2pi) (seed 2), energy of the TFIM
 H = -sum Z_i Z_{i+1} - 1.0 sum X_i, value and full gradient of every circuit
 through ``backend.vvag`` -- the reference's batched VQE step.  Synthetic
-inputs; states are complex64.
+inputs; states are complex64.  On one GPU the default run also times the
+large-circuit gate-application workload (n=28 Haar brick wall of depth 20,
+<Z0 Z27>, <X13>, 2^20 samples) and reports it under "brickwall_n28" in the
+same line, with its own forward-pass roofline, CPU baseline and e2e figure.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -361,6 +364,13 @@ def run_gb300_arm(args, rank, world):
         "gpu_launches": int(launches),
         "gpu_launches_per_step": int(launches_per_step),
     }
+    if world == 1 and not args.no_brickwall:
+        # the large-circuit gate-application workload (n=28 Haar brick wall),
+        # timed the same way after the batched step, reported beside it
+        bw = measure_brickwall(args, rank, world)
+        line["brickwall_n28"] = {k: bw[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup",
+                                                    "config", "roofline", "cpu_baseline", "e2e", "clocks",
+                                                    "gpu_launches", "gpu_launches_per_step")}
     print(json.dumps(line), flush=True)
 
 
@@ -400,8 +410,15 @@ def cpu_brickwall(n_cpu=22):
 
 
 def run_brickwall(args, rank, world):
+    line = measure_brickwall(args, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def measure_brickwall(args, rank, world):
     """Large single circuit: n=28 Haar brick wall (270 gates), then <Z0 Z27>,
-    <X13> and 2^20 samples from seeded uniforms, through the Circuit API."""
+    <X13> and 2^20 samples from seeded uniforms, through the Circuit API.
+    Returns the JSON line (rank 0) or None."""
     import torch
 
     import tensorcircuit_gb300 as tc
@@ -508,7 +525,7 @@ def run_brickwall(args, rank, world):
         "gpu_launches": int(launches_per_step * args.steps),
         "gpu_launches_per_step": int(launches_per_step),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 QB_COUNT, QB_SEED = 512, 5
@@ -1024,6 +1041,8 @@ def main():
     ap.add_argument("--gen-steps", type=int, default=2500,
                     help="warmstart: Adam steps that produce each training chain's target angles")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-brickwall", action="store_true",
+                    help="default workload: skip the nested n=28 brick-wall measurement")
     args = ap.parse_args()
     BATCH = args.batch
     BW_N = args.bw_qubits
