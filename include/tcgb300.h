@@ -101,6 +101,37 @@ int tcg_plan_create(int32_t nqubits, const tcg_gate* gates, int32_t ngates,
 int tcg_plan_destroy(tcg_plan* plan);
 int tcg_plan_get_stats(const tcg_plan* plan, tcg_plan_stats* out);
 
+/* Tensor-core passes (no reference counterpart; part of what replaces the
+ * per-gate contraction of tensorcircuit/cons.py:605-623).  A forward pass
+ * whose gates all act on its 12 local bits may run as fused blocks: each block
+ * is the product of consecutive gates on at most 6 bits, applied to every
+ * tile as a complex GEMM on the tensor cores (tcgen05, fp16 hi/lo operand
+ * split, fp32 accumulation).  Which passes do so follows the environment
+ * variable TCG_TC (0 none, 1 every pass that qualifies, unset the passes the
+ * planner's cost model prefers).  The plan then keeps one device buffer per
+ * device for a call's fused matrices (grown when a call's batch is larger).
+ * tcg_plan_tensor_passes returns how many forward passes take that path. */
+int tcg_plan_tensor_passes(const tcg_plan* plan);
+/* Sets the policy TCG_TC selects (0, 1 or 2 = cost model) for later calls of
+ * every plan; returns the previous one (another value only queries). */
+int32_t tcg_set_tensor_policy(int32_t policy);
+/* Synchronises the stream; TCG_ERR_TIMEOUT if a bounded device-side wait of
+ * an earlier tensor-core pass ran out of time (its results are then invalid),
+ * else TCG_OK.  Clears the flag. */
+int tcg_plan_check(const tcg_plan* plan, void* stream);
+/* Diagnostics (no reference counterpart): one tensor-core MMA probe,
+ * d[128][n] = a[128][k] b[n][k]^T for fp16 row-major a, b (device memory,
+ * k in {16, 32, 48, 64}, n a multiple of 32 up to 256), fp32 d, through the
+ * same shared-memory operand layout, descriptors and tensor-memory readback
+ * as the tensor-core passes.  *err (device) is set if its wait ran out. */
+int tcg_debug_tc_mma(const void* a, const void* b, float* d, int32_t k, int32_t n, unsigned int* err,
+                     void* stream);
+/* Diagnostics: host pointers to the fused-block program of a plan's forward
+ * sweep: arrays[0..3] = tensor-pass descriptors, blocks, source gates, the
+ * cost model's per-pass preference (int32); counts and element sizes in bytes
+ * likewise (all three arrays hold 4 elements). */
+int tcg_debug_tc_program(const tcg_plan* plan, const void** arrays, int64_t* counts, int64_t* sizes);
+
 /* Replaces: Circuit.wavefunction() (tensorcircuit/circuit.py:792-810), i.e.
  * the contractor loop of cons._base (tensorcircuit/cons.py:605-623).
  * psi [batch][2^n] holds the input states on entry and the output states on

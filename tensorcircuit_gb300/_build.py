@@ -21,7 +21,7 @@ OBJDIR = os.path.join(HERE, "lib", "obj")
 LIBNAME = "libtcgb300.so"
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["pass.cu", "misc.cu", "api.cu", "plan.cpp", "jit.cpp", "noalloc.cu", "batch.cu", "mlp.cu"]
+SOURCES = ["pass.cu", "misc.cu", "api.cu", "plan.cpp", "jit.cpp", "noalloc.cu", "batch.cu", "mlp.cu", "tcpass.cu"]
 HEADERS = ["engine.h", "kernels.h", "plan.h", "jit.h", "jit_device.cuh"]
 
 

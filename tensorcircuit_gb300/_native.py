@@ -87,6 +87,11 @@ SIGNATURES = [
     ("tcg_plan_create", ctypes.c_int, [_I32, ctypes.POINTER(TcgGate), _I32, ctypes.POINTER(TcgPlanOpts), ctypes.POINTER(_P)]),
     ("tcg_plan_destroy", ctypes.c_int, [_P]),
     ("tcg_plan_get_stats", ctypes.c_int, [_P, ctypes.POINTER(TcgPlanStats)]),
+    ("tcg_plan_tensor_passes", ctypes.c_int, [_P]),
+    ("tcg_set_tensor_policy", _I32, [_I32]),
+    ("tcg_plan_check", ctypes.c_int, [_P, _P]),
+    ("tcg_debug_tc_mma", ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
+    ("tcg_debug_tc_program", ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     ("tcg_forward", ctypes.c_int, [_P, _P, _I64, _P, _I64, _P]),
     ("tcg_backward_scratch_bytes", _SZ, [_P, _I64]),
     ("tcg_backward", ctypes.c_int, [_P, _P, _P, _I64, _P, _I64, _P, _I64, _P, _SZ, _P]),
@@ -182,6 +187,43 @@ def debug_program(handle: Any, which: int) -> dict:
         arr = (typ * cnts[i]).from_address(arrs[i])
         out[name] = [arr[j] for j in range(cnts[i])] if typ is not ctypes.c_uint32 else list(arr)
     return out
+
+class TcPassDesc(ctypes.Structure):
+    _fields_ = [("pass_", ctypes.c_int32), ("block_begin", ctypes.c_int32), ("block_end", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
+
+
+class TcBlock(ctypes.Structure):
+    _fields_ = [("bbits", ctypes.c_int32 * 6), ("cbits", ctypes.c_int32 * 6), ("gate_begin", ctypes.c_int32),
+                ("gate_end", ctypes.c_int32), ("slot", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class TcGate(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("k", ctypes.c_int32), ("pos", ctypes.c_int32 * 6),
+                ("xmask", ctypes.c_int32), ("zmask", ctypes.c_int32), ("nY", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("mat_off", ctypes.c_int64)]
+
+
+def debug_tc_program(handle: Any) -> dict:
+    """Copy of a plan's fused-block (tensor-core) program: pass descriptors,
+    blocks, source gates and the cost model's per-pass preference."""
+    lib = load()
+    arrs = (ctypes.c_void_p * 4)()
+    cnts = (ctypes.c_int64 * 4)()
+    szs = (ctypes.c_int64 * 4)()
+    check(lib.tcg_debug_tc_program(handle, arrs, cnts, szs), "debug_tc_program")
+    out = {}
+    for i, (name, typ) in enumerate([("passes", TcPassDesc), ("blocks", TcBlock), ("gates", TcGate),
+                                     ("prefer", ctypes.c_int32)]):
+        if ctypes.sizeof(typ) != szs[i]:
+            raise EngineError("record size mismatch for %s: %d vs %d" % (name, ctypes.sizeof(typ), szs[i]))
+        if cnts[i] == 0:
+            out[name] = []
+            continue
+        arr = (typ * cnts[i]).from_address(arrs[i])
+        out[name] = [arr[j] for j in range(cnts[i])] if typ is not ctypes.c_int32 else list(arr)
+    return out
+
 
 _lib: Optional[ctypes.CDLL] = None
 _lock = threading.Lock()

@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -80,6 +82,54 @@ int mplan_device(tcg_mplan* p, tcg_mplan::Dev* out) {
 
 constexpr uint32_t kDirectBlocks = 304;
 
+// Tensor-core passes: TCG_TC=0 never, TCG_TC=1 every pass that qualifies,
+// unset = the passes the planner's cost model prefers.
+std::atomic<int> g_tc_policy{-1};
+
+int tc_policy() {
+  int pol = g_tc_policy.load();
+  if (pol < 0) {
+    const char* e = std::getenv("TCG_TC");
+    pol = (e && e[0] == '0') ? 0 : (e && e[0] == '1') ? 1 : 2;
+    int expect = -1;
+    g_tc_policy.compare_exchange_strong(expect, pol);
+    pol = g_tc_policy.load();
+  }
+  return pol;
+}
+
+bool tc_use_pass(const Program* P, int ps) {
+  if (ps >= (int)P->tc_of_pass.size()) return false;
+  const int t = P->tc_of_pass[ps];
+  if (t < 0) return false;
+  const int pol = tc_policy();
+  return pol == 1 || (pol == 2 && P->tc_prefer[t]);
+}
+
+// Per-device buffer of one forward call's fused matrices: [0, 256) error
+// flag, then batch * slots blocks of kTcMatBytes, then batch * slots scales.
+int tc_scratch(Program* P, int64_t batch, unsigned int** err, uint8_t** fused, float** scales) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
+  const size_t nmat = size_t(batch) * size_t(P->tc_slots);
+  const size_t need = 256 + nmat * kTcMatBytes + nmat * sizeof(float) + 256;
+  std::lock_guard<std::mutex> lk(P->mu);
+  Program::TcScratch& ts = P->tc_scratch[dev];
+  if (ts.bytes < need) {
+    if (ts.base) cudaFree(ts.base);
+    ts.base = nullptr;
+    ts.bytes = 0;
+    if (cudaMalloc(&ts.base, need) != cudaSuccess) return TCG_ERR_OOM;
+    if (cudaMemset(ts.base, 0, 256) != cudaSuccess) return TCG_ERR_CUDA;
+    ts.bytes = need;
+  }
+  char* b = static_cast<char*>(ts.base);
+  *err = reinterpret_cast<unsigned int*>(b);
+  *fused = reinterpret_cast<uint8_t*>(b + 256);
+  *scales = reinterpret_cast<float*>(b + 256 + nmat * kTcMatBytes);
+  return TCG_OK;
+}
+
 // Runs every pass of a program direction: the specialised kernels when the
 // JIT policy selects them for this plan (see jit.cpp), else the generic
 // pass kernels of pass.cu.
@@ -98,6 +148,28 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
     }
   }
   const uint32_t ntiles = 1u << (a.n - P->L);
+  // tensor-core passes of a forward sweep: fuse this call's block matrices
+  bool any_tc = false;
+  unsigned int* tc_err = nullptr;
+  uint8_t* tc_fused = nullptr;
+  float* tc_scales = nullptr;
+  if (mode == MODE_FWD && !P->tc_passes.empty()) {
+    for (int ps = 0; ps < (int)P->passes.size(); ++ps) any_tc = any_tc || tc_use_pass(P, ps);
+    if (any_tc) {
+      int rc = tc_scratch(P, batch, &tc_err, &tc_fused, &tc_scales);
+      if (rc != TCG_OK) return rc;
+      rc = cuda_rc(launch_tc_fuse(a.prog.tc_blocks, (int)P->tc_blocks.size(), a.prog.tc_gates, a.mats, a.mat_stride,
+                                  batch, tc_fused, tc_scales, P->tc_slots, st));
+      if (rc != TCG_OK) return rc;
+    }
+  }
+  auto tc_launch = [&](int ps) -> int {
+    const TcPassDesc& d = P->tc_passes[P->tc_of_pass[ps]];
+    const DevPass& dp = P->passes[ps];
+    return cuda_rc(launch_tc_pass(dp, a.prog.runs + dp.runs_off, a.prog.tc_blocks + d.block_begin,
+                                  d.block_end - d.block_begin, a.psi, a.n, batch, tc_fused, tc_scales, P->tc_slots,
+                                  tc_err, st));
+  };
   if (jk) {
     KParams_Host kp;
     kp.psi = a.psi;
@@ -109,14 +181,15 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
     kp.coef = a.coef;
     kp.coef_stride = a.coef_stride;
     for (int ps = 0; ps < (int)P->passes.size(); ++ps) {
-      const int rc = cuda_rc(jit_launch(jk, ps, kp, ntiles, batch, a.n, st));
+      const int rc = (any_tc && tc_use_pass(P, ps)) ? tc_launch(ps)
+                                                    : cuda_rc(jit_launch(jk, ps, kp, ntiles, batch, a.n, st));
       if (rc != TCG_OK) return rc;
     }
     return TCG_OK;
   }
   for (int ps = 0; ps < (int)P->passes.size(); ++ps) {
     a.pass = ps;
-    const int rc = cuda_rc(launch_pass(mode, R, a, P->L, batch, st));
+    const int rc = (any_tc && tc_use_pass(P, ps)) ? tc_launch(ps) : cuda_rc(launch_pass(mode, R, a, P->L, batch, st));
     if (rc != TCG_OK) return rc;
   }
   return TCG_OK;
@@ -196,6 +269,7 @@ int tcg_plan_create(int32_t nqubits, const tcg_gate* gates, int32_t ngates, cons
   std::vector<PGate> fwd_gates = pg;
   for (PGate& g : fwd_gates) g.grad_off = -1;
   int rc = build_gate_program(nqubits, fwd_gates, po.tile_bits_fwd, kRFwd, false, po.max_stage_slots, &p->fwd);
+  if (rc == TCG_OK) plan_tensor_passes(&p->fwd, fwd_gates);
   if (rc == TCG_OK)
     rc = build_gate_program(nqubits, pg, po.tile_bits_bwd, kRBwd, true, po.max_stage_slots, &p->bwd);
   if (rc != TCG_OK) {
@@ -212,6 +286,61 @@ int tcg_plan_destroy(tcg_plan* plan) {
   program_free(&plan->bwd);
   delete plan;
   return TCG_OK;
+}
+
+int32_t tcg_set_tensor_policy(int32_t policy) {
+  const int prev = tc_policy();
+  if (policy >= 0 && policy <= 2) g_tc_policy.store(policy);
+  return prev;
+}
+
+int tcg_plan_tensor_passes(const tcg_plan* plan) {
+  if (!plan) return -1;
+  int c = 0;
+  for (int ps = 0; ps < (int)plan->fwd.passes.size(); ++ps) c += tc_use_pass(&plan->fwd, ps) ? 1 : 0;
+  return c;
+}
+
+int tcg_plan_check(const tcg_plan* plan, void* stream) {
+  if (!plan) return TCG_ERR_INVALID_ARG;
+  tcg_plan* p = const_cast<tcg_plan*>(plan);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
+  if (cudaStreamSynchronize(as_stream(stream)) != cudaSuccess) return TCG_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(p->fwd.mu);
+  auto it = p->fwd.tc_scratch.find(dev);
+  if (it == p->fwd.tc_scratch.end() || !it->second.base) return TCG_OK;
+  unsigned int flag = 0;
+  if (cudaMemcpy(&flag, it->second.base, sizeof(flag), cudaMemcpyDeviceToHost) != cudaSuccess) return TCG_ERR_CUDA;
+  if (flag) {
+    if (cudaMemset(it->second.base, 0, sizeof(flag)) != cudaSuccess) return TCG_ERR_CUDA;
+    return TCG_ERR_TIMEOUT;
+  }
+  return TCG_OK;
+}
+
+int tcg_debug_tc_program(const tcg_plan* plan, const void** arrays, int64_t* counts, int64_t* sizes) {
+  if (!plan || !arrays || !counts || !sizes) return TCG_ERR_INVALID_ARG;
+  const Program& p = plan->fwd;
+  arrays[0] = p.tc_passes.data();
+  arrays[1] = p.tc_blocks.data();
+  arrays[2] = p.tc_gates.data();
+  arrays[3] = p.tc_prefer.data();
+  counts[0] = (int64_t)p.tc_passes.size();
+  counts[1] = (int64_t)p.tc_blocks.size();
+  counts[2] = (int64_t)p.tc_gates.size();
+  counts[3] = (int64_t)p.tc_prefer.size();
+  sizes[0] = sizeof(TcPassDesc);
+  sizes[1] = sizeof(TcBlock);
+  sizes[2] = sizeof(TcGate);
+  sizes[3] = sizeof(int);
+  return TCG_OK;
+}
+
+int tcg_debug_tc_mma(const void* a, const void* b, float* d, int32_t k, int32_t n, unsigned int* err, void* stream) {
+  if (!a || !b || !d || !err) return TCG_ERR_INVALID_ARG;
+  if (k < 16 || k > 64 || k % 16 || n < 32 || n > 256 || n % 32) return TCG_ERR_INVALID_ARG;
+  return cuda_rc(launch_tc_mma_probe(a, b, d, k, n, err, as_stream(stream)));
 }
 
 int tcg_plan_get_stats(const tcg_plan* plan, tcg_plan_stats* out) {

@@ -92,6 +92,41 @@ struct SlotOut {
   int64_t out_off;   // per-circuit output offset (complex entries)
 };
 
+// ---- tensor-core passes (tcpass.cu).  A forward pass whose gates all act on
+// its 12 local bits can instead run as a short sequence of FUSED BLOCKS: each
+// block is the product of consecutive gates of the pass on at most 6 tile
+// bits, a 64 x 64 complex matrix applied to the tile as a complex GEMM on the
+// tensor cores (64 block entries x 64 columns per tile).
+constexpr int kTcTileBits = 12;   // tile bits of a tensor-core pass
+constexpr int kTcBlockBits = 6;   // qubits of one fused block
+constexpr int kTcMatBytes = 32768;  // one fused block: fp16 hi + lo planes, 16 KiB each
+
+// A source gate of a fused block, in block-bit form.
+struct TcGate {
+  int32_t kind;      // TCG_GATE_DENSE / TCG_GATE_DIAG / TCG_GATE_PAULI_ROT
+  int32_t k;
+  int32_t pos[6];    // block bit of gate qubit i (gate qubit 0 = sub-index MSB)
+  int32_t xmask;     // PAULI_ROT: block-bit mask of the X/Y factors
+  int32_t zmask;     // PAULI_ROT: block-bit mask of the Z/Y factors
+  int32_t nY;        // PAULI_ROT: number of Y factors
+  int32_t pad;
+  int64_t mat_off;   // per-circuit matrix offset (complex entries)
+};
+
+struct TcBlock {
+  int32_t bbits[6];  // tile bit of block-index bit i
+  int32_t cbits[6];  // tile bit of column-index bit i
+  int32_t gate_begin, gate_end;  // source gates, in application order
+  int32_t slot;      // fused-matrix slot (per circuit) of this block
+  int32_t pad;
+};
+
+struct TcPassDesc {
+  int32_t pass;      // pass index in the program
+  int32_t block_begin, block_end;
+  int32_t pad;
+};
+
 // Whole device program of one plan direction, in one device allocation.
 struct ProgramView {
   const DevPass* passes;
@@ -102,6 +137,9 @@ struct ProgramView {
   const int64_t* entries; // distinct accumulator outputs, for the final reduce
   int64_t nentries;
   const ZEnt* zents;      // entries of OP_ZRUN runs
+  const TcPassDesc* tc_passes;  // tensor-core passes (forward programs)
+  const TcBlock* tc_blocks;
+  const TcGate* tc_gates;
 };
 
 }  // namespace tcg

@@ -117,6 +117,16 @@ cudaError_t launch_inner(const float2* a, const float2* b, int64_t len, int64_t 
                          void* scratch, cudaStream_t st);
 size_t inner_scratch_bytes(int64_t len, int64_t batch);
 
+// tensor-core passes (tcpass.cu)
+cudaError_t launch_tc_fuse(const TcBlock* blocks, int nblocks, const TcGate* gates, const float2* mats,
+                           int64_t mat_stride, int64_t batch, uint8_t* fused, float* scales, int slots,
+                           cudaStream_t st);
+cudaError_t launch_tc_pass(const DevPass& pass, const uint32_t* runs_dev, const TcBlock* blocks_dev, int nblocks,
+                           float2* psi, int n, int64_t batch, const uint8_t* fused, const float* scales, int slots,
+                           unsigned int* err, cudaStream_t st);
+cudaError_t launch_tc_mma_probe(const void* A, const void* B, float* D, int K, int N, unsigned int* err,
+                                cudaStream_t st);
+
 // sampling
 size_t sample_scratch_bytes(int n, int64_t batch);
 cudaError_t launch_sample(const float2* psi, int n, int64_t batch, const float* u, int64_t u_stride,

@@ -439,6 +439,7 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
     uint64_t S = 0;
     for (int b = 0; b < L; ++b) S |= 1ull << b;
     std::vector<OpDraft> none;
+    P.pass_gates.emplace_back();
     return emit_pass(&P, n, L, R, S, none, max_slots);
   }
   auto need_of = [&](const PGate& g) -> uint64_t {
@@ -584,12 +585,200 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
       o.z = g.zmask;
       od.push_back(o);
     }
+    P.pass_gates.push_back(taken);
     int rc = emit_pass(&P, n, L, R, S, od, max_slots);
     if (rc != TCG_OK) return rc;
     rem.swap(left);
   }
   finish_entries(&P);
   return TCG_OK;
+}
+
+namespace {
+
+// Fuse the gates of one pass (tile-bit masks tb, in application order) into
+// blocks of at most kTcBlockBits tile bits.  A gate may join the open block
+// once every earlier gate it shares a bit with is placed or in the block;
+// gates that fit the block's bits are absorbed first, otherwise the ready
+// gate that widens the block least joins.  Returns the blocks (gate indices
+// in application order) and their bit sets.
+void fuse_pass_gates(const std::vector<uint32_t>& tb, std::vector<std::vector<int>>* blocks,
+                     std::vector<uint32_t>* sets) {
+  const int m = (int)tb.size();
+  std::vector<std::vector<int>> preds(m);
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < i; ++j)
+      if (tb[j] & tb[i]) preds[i].push_back(j);
+  std::vector<char> placed(m, 0), inb(m, 0);
+  int nplaced = 0;
+  while (nplaced < m) {
+    uint32_t S = 0;
+    std::vector<int> cur;
+    std::fill(inb.begin(), inb.end(), 0);
+    auto ready = [&](int i) {
+      if (placed[i] || inb[i]) return false;
+      for (int j : preds[i])
+        if (!placed[j] && !inb[j]) return false;
+      return true;
+    };
+    for (;;) {
+      bool changed = false;
+      for (int i = 0; i < m; ++i)
+        if (ready(i) && (tb[i] & ~S) == 0) {
+          inb[i] = 1;
+          cur.push_back(i);
+          changed = true;
+        }
+      if (changed) continue;
+      int best = -1, bc = kTcBlockBits + 1;
+      for (int i = 0; i < m; ++i)
+        if (ready(i)) {
+          const int c = popc64(S | tb[i]);
+          if (c <= kTcBlockBits && c < bc) {
+            bc = c;
+            best = i;
+          }
+        }
+      if (best < 0) break;
+      inb[best] = 1;
+      cur.push_back(best);
+      S |= tb[best];
+    }
+    std::sort(cur.begin(), cur.end());
+    for (int i : cur) placed[i] = 1;
+    nplaced += (int)cur.size();
+    blocks->push_back(cur);
+    sets->push_back(S);
+  }
+}
+
+// Order `bits` so that its first `want` entries fall in distinct bank classes
+// (tile bit t flips bank bit t mod 5 of the staging copy), drawing classes
+// from `allowed`; returns how many of them did.
+int order_for_banks(std::vector<int>& bits, int want, uint32_t allowed) {
+  std::vector<int> out, rest = bits;
+  uint32_t used = 0;
+  for (int slot = 0; slot < want; ++slot) {
+    int pick = -1;
+    for (size_t c = 0; c < rest.size(); ++c) {
+      const int cls = rest[c] % 5;
+      if ((allowed >> cls & 1u) && !(used >> cls & 1u)) {
+        pick = (int)c;
+        break;
+      }
+    }
+    if (pick < 0) break;
+    used |= 1u << (rest[pick] % 5);
+    out.push_back(rest[pick]);
+    rest.erase(rest.begin() + pick);
+  }
+  const int good = (int)out.size();
+  for (int t : rest) out.push_back(t);
+  bits = out;
+  return good;
+}
+
+}  // namespace
+
+void plan_tensor_passes(Program* P, const std::vector<PGate>& gates) {
+  P->tc_of_pass.assign(P->passes.size(), -1);
+  if (P->L != kTcTileBits) return;
+  for (size_t ps = 0; ps < P->passes.size() && ps < P->pass_gates.size(); ++ps) {
+    const DevPass& dp = P->passes[ps];
+    const std::vector<int>& gl = P->pass_gates[ps];
+    if (gl.empty()) continue;
+    int tile_of_gbit[64];
+    for (int i = 0; i < 64; ++i) tile_of_gbit[i] = -1;
+    for (int i = 0; i < dp.L; ++i) tile_of_gbit[dp.lbits[i]] = i;
+    bool ok = true;
+    int ndense2 = 0;
+    std::vector<uint32_t> tb(gl.size());
+    for (size_t i = 0; i < gl.size() && ok; ++i) {
+      const PGate& g = gates[gl[i]];
+      if (g.grad_off >= 0) ok = false;
+      uint32_t t = 0;
+      for (int q = 0; q < g.k; ++q) {
+        const int tt = tile_of_gbit[g.gbits[q]];
+        if (tt < 0) ok = false;
+        else t |= 1u << tt;
+      }
+      tb[i] = t;
+      if (g.kind == TCG_GATE_DENSE && g.k >= 2) ++ndense2;
+    }
+    if (!ok) continue;
+    std::vector<std::vector<int>> blocks;
+    std::vector<uint32_t> sets;
+    fuse_pass_gates(tb, &blocks, &sets);
+    TcPassDesc pd;
+    std::memset(&pd, 0, sizeof(pd));
+    pd.pass = (int)ps;
+    pd.block_begin = (int)P->tc_blocks.size();
+    for (size_t bi = 0; bi < blocks.size(); ++bi) {
+      // pad the block to 6 bits; choose the padding so that both bit orders
+      // avoid staging bank conflicts where possible
+      const uint32_t S = sets[bi];
+      std::vector<int> freeb;
+      for (int t = 0; t < kTcTileBits; ++t)
+        if (!(S >> t & 1u)) freeb.push_back(t);
+      const int need = kTcBlockBits - popc64(S);
+      uint32_t bestS = 0;
+      int bestscore = -1;
+      std::vector<int> bestb, bestc;
+      const int nf = (int)freeb.size();
+      for (uint32_t pick = 0; pick < (1u << nf); ++pick) {
+        if (popc64(pick) != need) continue;
+        uint32_t Sx = S;
+        for (int f = 0; f < nf; ++f)
+          if (pick >> f & 1u) Sx |= 1u << freeb[f];
+        std::vector<int> bb, cb;
+        for (int t = 0; t < kTcTileBits; ++t) ((Sx >> t & 1u) ? bb : cb).push_back(t);
+        const int score = order_for_banks(bb, 4, 0xFu) + order_for_banks(cb, 5, 0x1Fu);
+        if (score > bestscore) {
+          bestscore = score;
+          bestS = Sx;
+          bestb = bb;
+          bestc = cb;
+        }
+      }
+      (void)bestS;
+      TcBlock tbk;
+      std::memset(&tbk, 0, sizeof(tbk));
+      int blockpos_of_tile[32];
+      for (int i = 0; i < 32; ++i) blockpos_of_tile[i] = -1;
+      for (int i = 0; i < kTcBlockBits; ++i) {
+        tbk.bbits[i] = bestb[i];
+        tbk.cbits[i] = bestc[i];
+        blockpos_of_tile[bestb[i]] = i;
+      }
+      tbk.gate_begin = (int)P->tc_gates.size();
+      for (int gi : blocks[bi]) {
+        const PGate& g = gates[gl[gi]];
+        TcGate G;
+        std::memset(&G, 0, sizeof(G));
+        G.kind = g.kind;
+        G.k = g.k;
+        for (int q = 0; q < g.k; ++q) G.pos[q] = blockpos_of_tile[tile_of_gbit[g.gbits[q]]];
+        if (g.kind == TCG_GATE_PAULI_ROT) {
+          for (int b = 0; b < 64; ++b) {
+            if (g.xmask >> b & 1) G.xmask |= 1 << blockpos_of_tile[tile_of_gbit[b]];
+            if (g.zmask >> b & 1) G.zmask |= 1 << blockpos_of_tile[tile_of_gbit[b]];
+          }
+          G.nY = popc64(g.xmask & g.zmask);
+        }
+        G.mat_off = g.mat_off;
+        P->tc_gates.push_back(G);
+      }
+      tbk.gate_end = (int)P->tc_gates.size();
+      tbk.slot = P->tc_slots++;
+      P->tc_blocks.push_back(tbk);
+    }
+    pd.block_end = (int)P->tc_blocks.size();
+    P->tc_of_pass[ps] = (int)P->tc_passes.size();
+    P->tc_passes.push_back(pd);
+    // cost model: a block costs about as much as two register-path 4x4
+    // gates, so the tensor path pays when blocks absorb more than that
+    P->tc_prefer.push_back(ndense2 >= 2 * (int)blocks.size() ? 1 : 0);
+  }
 }
 
 int build_term_program(int n, const std::vector<tcg_pauli>& terms, int L, int R,
@@ -660,7 +849,10 @@ int program_device_view(Program* p, ProgramView* view) {
   size_t o_runs = al(o_so + p->slot_out.size() * sizeof(SlotOut));
   size_t o_ent = al(o_runs + p->runs.size() * sizeof(uint32_t));
   size_t o_z = al(o_ent + p->entries.size() * sizeof(int64_t));
-  size_t total = al(o_z + p->zents.size() * sizeof(ZEnt)) + 256;
+  size_t o_tcp = al(o_z + p->zents.size() * sizeof(ZEnt));
+  size_t o_tcb = al(o_tcp + p->tc_passes.size() * sizeof(TcPassDesc));
+  size_t o_tcg = al(o_tcb + p->tc_blocks.size() * sizeof(TcBlock));
+  size_t total = al(o_tcg + p->tc_gates.size() * sizeof(TcGate)) + 256;
   std::vector<char> host(total, 0);
   if (!p->passes.empty()) std::memcpy(host.data() + o_pass, p->passes.data(), p->passes.size() * sizeof(DevPass));
   if (!p->stages.empty()) std::memcpy(host.data() + o_stage, p->stages.data(), p->stages.size() * sizeof(DevStage));
@@ -669,6 +861,11 @@ int program_device_view(Program* p, ProgramView* view) {
   if (!p->runs.empty()) std::memcpy(host.data() + o_runs, p->runs.data(), p->runs.size() * sizeof(uint32_t));
   if (!p->entries.empty()) std::memcpy(host.data() + o_ent, p->entries.data(), p->entries.size() * sizeof(int64_t));
   if (!p->zents.empty()) std::memcpy(host.data() + o_z, p->zents.data(), p->zents.size() * sizeof(ZEnt));
+  if (!p->tc_passes.empty())
+    std::memcpy(host.data() + o_tcp, p->tc_passes.data(), p->tc_passes.size() * sizeof(TcPassDesc));
+  if (!p->tc_blocks.empty())
+    std::memcpy(host.data() + o_tcb, p->tc_blocks.data(), p->tc_blocks.size() * sizeof(TcBlock));
+  if (!p->tc_gates.empty()) std::memcpy(host.data() + o_tcg, p->tc_gates.data(), p->tc_gates.size() * sizeof(TcGate));
   void* d = nullptr;
   if (cudaMalloc(&d, total) != cudaSuccess) return TCG_ERR_OOM;
   if (cudaMemcpy(d, host.data(), total, cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -686,6 +883,9 @@ int program_device_view(Program* p, ProgramView* view) {
   c.view.entries = (const int64_t*)(b + o_ent);
   c.view.nentries = (int64_t)p->entries.size();
   c.view.zents = (const ZEnt*)(b + o_z);
+  c.view.tc_passes = (const TcPassDesc*)(b + o_tcp);
+  c.view.tc_blocks = (const TcBlock*)(b + o_tcb);
+  c.view.tc_gates = (const TcGate*)(b + o_tcg);
   p->dev[dev] = c;
   *view = c.view;
   return TCG_OK;
@@ -699,8 +899,13 @@ void program_free(Program* p) {
     cudaSetDevice(kv.first);
     cudaFree(kv.second.base);
   }
+  for (auto& kv : p->tc_scratch) {
+    cudaSetDevice(kv.first);
+    cudaFree(kv.second.base);
+  }
   cudaSetDevice(cur);
   p->dev.clear();
+  p->tc_scratch.clear();
 }
 
 }  // namespace tcg

@@ -35,6 +35,19 @@ struct Program {
   std::map<int, DevCopy> dev;
   std::mutex mu;
 
+  // tensor-core passes (forward programs; tcpass.cu): source gates per pass,
+  // the fused blocks of the passes that qualify, and per device a buffer for
+  // the fused matrices of one call (grown on demand) with an error flag
+  std::vector<std::vector<int>> pass_gates;
+  std::vector<TcPassDesc> tc_passes;
+  std::vector<TcBlock> tc_blocks;
+  std::vector<TcGate> tc_gates;
+  std::vector<int> tc_of_pass;     // per pass: index into tc_passes, or -1
+  std::vector<int> tc_prefer;      // per tensor pass: 1 if the cost model picks it
+  int tc_slots = 0;                // fused matrices per circuit
+  struct TcScratch { void* base = nullptr; size_t bytes = 0; };
+  std::map<int, TcScratch> tc_scratch;
+
   // specialised kernels per mode (jit.cpp), built on demand
   std::unique_ptr<JitKernels> jit[4];
   int calls[4] = {0, 0, 0, 0};
@@ -66,6 +79,10 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
 // X/Y bits cannot fit the register layout are returned in `direct`.
 int build_term_program(int n, const std::vector<tcg_pauli>& terms, int L, int R,
                        int max_slots, Program* out, std::vector<int>* direct);
+
+// Fuse the dense gates of every forward pass that qualifies into blocks of at
+// most kTcBlockBits tile bits (tensor-core passes, tcpass.cu).
+void plan_tensor_passes(Program* P, const std::vector<PGate>& gates);
 
 // Upload (once per device) and return the device view.
 int program_device_view(Program* p, ProgramView* view);

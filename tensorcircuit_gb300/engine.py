@@ -83,6 +83,17 @@ class GatePlan:
         self.prot_offs = [g[3] for g in gates if g[0] == nat.TCG_GATE_PAULI_ROT and g[3] >= 0]
         self._prot_mask: Dict[Any, torch.Tensor] = {}
 
+    def tensor_passes(self) -> int:
+        """Forward passes that run as fused blocks on the tensor cores under
+        the current policy (``TCG_TC`` / ``tcg_set_tensor_policy``)."""
+        return int(nat.load().tcg_plan_tensor_passes(self.handle))
+
+    def check(self, stream: Optional[int] = None) -> None:
+        """Synchronise and raise if a bounded device-side wait of a
+        tensor-core pass ran out of time (its results are then invalid)."""
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        nat.check(nat.load().tcg_plan_check(self.handle, st), "tensor-core pass")
+
     def prot_mask(self, device: torch.device) -> Optional[torch.Tensor]:
         if not self.prot_offs:
             return None
