@@ -45,7 +45,8 @@ enum {
   TCG_ERR_CUDA = 4,          /* a CUDA runtime call failed */
   TCG_ERR_SCRATCH = 5,       /* caller-provided scratch is too small */
   TCG_ERR_OOM = 6,           /* a host or device allocation failed */
-  TCG_ERR_TOO_LARGE = 7,     /* request exceeds a fixed internal capacity */
+  TCG_ERR_TOO_LARGE = 7,     /* request exceeds a fixed internal capacity (each
+                                entry point that returns it states its limit) */
   TCG_ERR_TIMEOUT = 8        /* a bounded device-side wait ran out of time */
 };
 
@@ -186,10 +187,10 @@ int tcg_expect_pauli(const tcg_mplan* plan, const void* psi, int64_t batch,
                      void* stream);
 
 /* Allocation-free Pauli expectations.  No counterpart in the reference: it
- * exists for callers that cannot allocate device memory -- code running while
- * a stream is captured into a CUDA graph (cudaMalloc is refused there), hosts
- * whose device memory lives in a pool this ABI cannot reach, and loops that
- * cannot afford cudaMalloc's implicit synchronisation.  Same result as
+ * exists for callers that cannot allocate device memory -- hosts whose device
+ * memory lives in a pool this ABI cannot reach (a runtime that hands over
+ * only pre-allocated buffers), and loops that cannot afford cudaMalloc's
+ * implicit synchronisation.  Same result as
  * tcg_expect_pauli (out[b][t] = <psi_b|P_t|psi_b>, complex128) without a plan
  * and without any allocation: the partial sums go to a fixed 8 MiB device
  * array inside the library.  Limits: nterms <= 64, batch <= 65535 and
@@ -328,6 +329,17 @@ int tcg_ubatch_stats(const tcg_ubatch* batch, int64_t* tiles, double* alg_bytes)
  * TCG_OK; clears the flag.  The flag lives in the scratch buffer: zero the
  * scratch once before its first use so that it starts clear. */
 int tcg_ubatch_check(tcg_ubatch* batch, void* scratch, void* stream);
+
+/* Limit of one device-side dependency wait of later calls (default 2 s);
+ * a wait that runs out makes the launch skip every later wait and finish,
+ * and tcg_ubatch_check report TCG_ERR_TIMEOUT. */
+int tcg_ubatch_set_wait_limit(tcg_ubatch* batch, uint64_t wait_ns);
+/* Diagnostics (no reference counterpart): overwrite the dependency count of
+ * segment `seg` of sweep `sweep` (0 forward, 1 adjoint, 2 measure, 3 Pauli
+ * accumulate) in the batch's device tables, so that tests can make a wait
+ * run out (a count no sweep reaches) without faulting anything: the results
+ * of the calls that follow are invalid. */
+int tcg_debug_ubatch_set_need(tcg_ubatch* batch, int32_t sweep, int32_t seg, uint32_t need);
 
 /* ---- learned warm start (no reference counterpart) ---------------------------
  * Kernels of the network that maps Hamiltonian couplings to circuit angles

@@ -116,6 +116,8 @@ SIGNATURES = [
     ("tcg_ubatch_value_and_grad", ctypes.c_int, [_P, _P, _P, _P, _P, _SZ, _P]),
     ("tcg_ubatch_stats", ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double)]),
     ("tcg_ubatch_check", ctypes.c_int, [_P, _P, _P]),
+    ("tcg_ubatch_set_wait_limit", ctypes.c_int, [_P, ctypes.c_uint64]),
+    ("tcg_debug_ubatch_set_need", ctypes.c_int, [_P, _I32, _I32, ctypes.c_uint32]),
     ("tcg_mlp_linear_forward", ctypes.c_int, [_P, _I32, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _I32, _P]),
     ("tcg_mlp_linear_backward", ctypes.c_int,
      [_P, _P, _I32, _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P, _P, _P]),

@@ -223,7 +223,7 @@ class UnevenBatch:
     """
 
     def __init__(self, specs: Sequence[Sequence[Any]], tile_bits: Optional[int] = None, graph: bool = True,
-                 device: Optional[torch.device] = None) -> None:
+                 device: Optional[torch.device] = None, wait_limit_ns: Optional[int] = None) -> None:
         self.device = device or eng.device()
         self.circuits = [BatchCircuit(*s) for s in specs]
         self.nparams = sum(bc.nparams for bc in self.circuits)
@@ -245,6 +245,9 @@ class UnevenBatch:
         if tile_bits > nmin:
             raise ValueError("tile_bits %d exceeds the smallest circuit (%d qubits)" % (tile_bits, nmin))
         self.h = _Handle(self.circuits, tile_bits, self.device)
+        if wait_limit_ns is not None:
+            # limit of one device-side dependency wait (default 2 s)
+            nat.check(nat.load().tcg_ubatch_set_wait_limit(self.h.handle, int(wait_limit_ns)), "wait limit")
         self.tile_bits = tile_bits
         self._p = torch.zeros(max(self.nparams, 1), dtype=torch.float32, device=self.device)
         self._e = torch.zeros(len(self.circuits), dtype=torch.float32, device=self.device)

@@ -1175,8 +1175,13 @@ class Circuit:
         return torch.sum(torch.conj(psi) * phi, -1)
 
     def probability(self) -> Tensor:
-        """|psi|^2 over the computational basis (basecircuit.py:510-523)."""
+        """|psi|^2 over the computational basis (basecircuit.py:510-523), by
+        the engine's probability kernel (computed as re^2 + im^2; the
+        reference squares abs(psi), which can differ in the last bit),
+        differentiable through its autograd Function."""
         s = self.wavefunction()
+        if s.is_cuda:
+            return eng.ProbabilityFn.apply(s)
         return torch.abs(s) ** 2
 
     def amplitude(self, l: Union[str, Tensor]) -> Tensor:

@@ -213,8 +213,7 @@ const char* tcg_status_string(int32_t s) {
     case TCG_ERR_SCRATCH: return "scratch buffer too small";
     case TCG_ERR_OOM: return "allocation failed";
     case TCG_ERR_TOO_LARGE:
-      return "request exceeds a fixed internal capacity (tcg_expect_pauli_noalloc: nterms <= 64, "
-             "batch <= 65535, batch * nterms <= 6898)";
+      return "request exceeds a fixed internal capacity of the entry point (see its limits in tcgb300.h)";
     case TCG_ERR_TIMEOUT: return "a bounded device-side wait ran out of time (results invalid)";
     default: return "unknown status";
   }

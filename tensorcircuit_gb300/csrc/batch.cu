@@ -107,6 +107,7 @@ struct tcg_ubatch {
   int nsegs[4] = {0, 0, 0, 0};
   int64_t n_energy_tasks = 0, n_grad_tasks = 0;
   bool lite = true;  // every program fits the lighter persistent body
+  unsigned long long wait_ns = 2000000000ull;  // limit of one dependency wait
 
   // device tables (one allocation)
   void* dtab = nullptr;
@@ -560,6 +561,7 @@ int tcg_ubatch_value_and_grad(tcg_ubatch* batch, const float* params, float* ene
     bl.done = cnt + mode * cw + 1;
     bl.err = err;
     bl.sticky = sticky;
+    bl.wait_ns = B->wait_ns;
     return rc_of(launch_batch(mode, bl, B->L, B->max_slots[mode], B->lite, st));
   };
   auto reduce = [&](const RedTask* tasks, int64_t ntasks, const RedItem* items, float* out) -> int {
@@ -589,6 +591,23 @@ int tcg_ubatch_stats(const tcg_ubatch* batch, int64_t* tiles, double* alg_bytes)
     if (alg_bytes) alg_bytes[m] = double(batch->nitems[m]) * double(int64_t(1) << batch->L) * per_amp[m];
   }
   return TCG_OK;
+}
+
+int tcg_ubatch_set_wait_limit(tcg_ubatch* batch, uint64_t wait_ns) {
+  if (!batch || wait_ns == 0) return TCG_ERR_INVALID_ARG;
+  batch->wait_ns = wait_ns;
+  return TCG_OK;
+}
+
+int tcg_debug_ubatch_set_need(tcg_ubatch* batch, int32_t sweep, int32_t seg, uint32_t need) {
+  if (!batch || sweep < 0 || sweep > 3 || seg < 0 || seg >= batch->nsegs[sweep]) return TCG_ERR_INVALID_ARG;
+  int cur = 0;
+  if (cudaGetDevice(&cur) != cudaSuccess) return TCG_ERR_CUDA;
+  if (cudaSetDevice(batch->device) != cudaSuccess) return TCG_ERR_CUDA;
+  BatchSeg* s = const_cast<BatchSeg*>(batch->segs[sweep]) + seg;
+  const cudaError_t e = cudaMemcpy(&s->need, &need, sizeof(need), cudaMemcpyHostToDevice);
+  cudaSetDevice(cur);
+  return e == cudaSuccess ? TCG_OK : TCG_ERR_CUDA;
 }
 
 int tcg_ubatch_check(tcg_ubatch* batch, void* scratch, void* stream) {

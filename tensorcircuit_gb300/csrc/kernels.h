@@ -83,6 +83,7 @@ struct BatchLaunch {
   unsigned int* done;   // per-circuit completed tiles, zero at launch
   unsigned int* err;    // this call: a dependency wait ran out of time (zero at launch)
   unsigned int* sticky; // set with err; cleared only by the caller's check
+  unsigned long long wait_ns;  // limit of one dependency wait
 };
 // L: tile bits shared by every program of the launch; max_slots: largest
 // stage slot count over the circuits.

@@ -1,11 +1,10 @@
 // noalloc.cu — Pauli expectations that allocate nothing.
 //
-// Some callers cannot allocate device memory: code that runs while a stream
-// is being captured into a CUDA graph (cudaMalloc is not a stream operation
-// and is refused there), hosts whose device memory belongs to a pool this
-// C ABI cannot reach (a binding that hands over only pre-allocated buffers),
-// and latency-critical loops where cudaMalloc's implicit device
-// synchronisation is not acceptable.  tcg_expect_pauli_noalloc serves them:
+// Some callers cannot allocate device memory: hosts whose device memory
+// belongs to a pool this C ABI cannot reach (a binding or runtime that hands
+// over only pre-allocated buffers and forbids allocations of its own), and
+// latency-critical loops where cudaMalloc's implicit device synchronisation
+// is not acceptable.  tcg_expect_pauli_noalloc serves them:
 // the caller passes the state and the output, and the per-block partial sums
 // live in a fixed file-scope device array instead of caller or library
 // allocations.  No plan is needed (the terms travel as a kernel argument).

@@ -1020,7 +1020,7 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 // running, so waits end; the limit only guards against a broken schedule.
 // After a time-out every later wait is skipped (results are then invalid and
 // the error flag says so) so the launch still finishes.
-constexpr unsigned long long kBatchWaitNs = 2000000000ull;
+constexpr unsigned long long kBatchWaitNs = 2000000000ull;  // default dependency-wait limit
 
 template <int MODE, int R, bool LITE>
 __global__ void __launch_bounds__(256, LITE ? 2 : 1) batch_kernel(BatchLaunch BL) {
@@ -1086,7 +1086,7 @@ __global__ void __launch_bounds__(256, LITE ? 2 : 1) batch_kernel(BatchLaunch BL
           unsigned spins = 0;
           while (ld_acquire_u32(dn) < need) {
             __nanosleep(100);
-            if ((++spins & 63u) == 0u && (global_ns() - t0 > kBatchWaitNs || ld_acquire_u32(BL.err) != 0u)) {
+            if ((++spins & 63u) == 0u && (global_ns() - t0 > BL.wait_ns || ld_acquire_u32(BL.err) != 0u)) {
               atomicOr(BL.err, 1u);
               atomicOr(BL.sticky, 1u);
               break;

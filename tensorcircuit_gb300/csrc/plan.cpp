@@ -596,6 +596,9 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
 
 namespace {
 
+constexpr double kTcMsPerBlock = 1.5;     // tensor-core pass, per fused block
+constexpr double kRegMsPerDense2 = 0.2;   // register path, per 4x4 gate
+
 // Fuse the gates of one pass (tile-bit masks tb, in application order) into
 // blocks of at most kTcBlockBits tile bits.  A gate may join the open block
 // once every earlier gate it shares a bit with is placed or in the block;
@@ -775,9 +778,11 @@ void plan_tensor_passes(Program* P, const std::vector<PGate>& gates) {
     pd.block_end = (int)P->tc_blocks.size();
     P->tc_of_pass[ps] = (int)P->tc_passes.size();
     P->tc_passes.push_back(pd);
-    // cost model: a block costs about as much as two register-path 4x4
-    // gates, so the tensor path pays when blocks absorb more than that
-    P->tc_prefer.push_back(ndense2 >= 2 * (int)blocks.size() ? 1 : 0);
+    // cost model from GB300 timings at 2^28 amplitudes per pass: a fused
+    // block costs about kTcMsPerBlock, a 4x4 gate on the register path
+    // about kRegMsPerDense2 (both include their share of the pass's HBM
+    // traffic); the tensor path runs where it is estimated faster
+    P->tc_prefer.push_back(kTcMsPerBlock * (double)blocks.size() < kRegMsPerDense2 * (double)ndense2 ? 1 : 0);
   }
 }
 

@@ -21,7 +21,8 @@
 //     rescaled the same way before each block (per tile, from its largest
 //     component), so nothing overflows and the low halves stay normal.
 //
-// Data path per tile (one CTA, 256 threads, two CTAs per SM): the tile is
+// Data path per tile (one CTA, 256 threads, two CTAs per SM, 256 tensor-memory
+// columns each: per plane a main and a correction accumulator): the tile is
 // read from HBM once into an fp32 staging copy in shared memory; per block
 // the threads write the split B planes (K-major canonical layout, 16-byte
 // core-matrix rows), one thread issues 24 tcgen05.mma (M=128, N=64, K=16)
@@ -170,6 +171,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
       : "r"(taddr));
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+// 16 consecutive columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -373,7 +386,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
   const uint8_t* fused_b = a.fused + b * a.slots * (int64_t)kTcMatBytes;
   const float* scales_b = a.scales + b * a.slots;
 
-  if (warp == 0) tmem_alloc(sbase + kSmX, 128);
+  if (warp == 0) tmem_alloc(sbase + kSmX, 256);
   if (tid == 0) {
     mbar_init(bar_mat, 1);
     mbar_init(bar_mma, 1);
@@ -456,21 +469,26 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
         sx[1] = 1;
       } else {
         ph_mat ^= 1;
+        // per plane p: main accumulator (hi x hi) at column 128p, correction
+        // accumulator (hi x lo + lo x hi) at 128p + 64.  The tensor core's fp32
+        // accumulation truncates; keeping the small corrections apart means the
+        // main value takes 3 accumulating steps instead of 11 (the epilogue
+        // adds the two with round-to-nearest).
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-          const uint32_t d = tmem + 64u * p;
+          const uint32_t dm = tmem + 128u * p, dc = dm + 64u;
           const uint32_t bh = sbase + kSmB + p * 16384u, bl = bh + 8192u;
 #pragma unroll
           for (int s = 0; s < 4; ++s)
-            mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
+            mma_f16(dm, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
                     make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, s > 0);
 #pragma unroll
           for (int s = 0; s < 4; ++s)
-            mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
-                    make_desc(bl + s * 2 * kLboB, kLboB, 128), idesc, 1);
+            mma_f16(dc, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
+                    make_desc(bl + s * 2 * kLboB, kLboB, 128), idesc, s > 0);
 #pragma unroll
           for (int s = 0; s < 4; ++s)
-            mma_f16(d, make_desc(sbase + kSmA + 16384 + s * 2 * kLboA, kLboA, 128),
+            mma_f16(dc, make_desc(sbase + kSmA + 16384 + s * 2 * kLboA, kLboA, 128),
                     make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, 1);
         }
         mma_commit(bar_mma);
@@ -501,11 +519,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
     // ---- epilogue: D -> combined outputs -> staging (natural order)
     {
       const int q = warp & 3, hcol = warp >> 2;
-      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + 32u * hcol;
-      float d1[32], d2[32];
-      tmem_ld32(ta, d1);
-      tmem_ld32(ta + 64u, d2);
-      tmem_wait_ld();
       const float inv = sxinv * __ldg(scales_b + blk.slot);
       const int row = 32 * q + lane;
       const uint32_t ti = tj[row >> 1];
@@ -513,11 +526,22 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
       const float sgn = (row & 1) ? 1.f : -1.f;
       float m = 0.f;
 #pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const float other = __shfl_xor_sync(0xffffffffu, d2[c], 1);
-        const float y = fmaf(sgn, other, d1[c]) * inv;
-        sp[swz(ti | tn[32 * hcol + c])] = y;
-        m = fmaxf(m, fabsf(y));
+      for (int half = 0; half < 2; ++half) {
+        const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + 32u * hcol + 16u * half;
+        float m1[16], c1[16], m2[16], c2[16];
+        tmem_ld16(ta, m1);
+        tmem_ld16(ta + 64u, c1);
+        tmem_ld16(ta + 128u, m2);
+        tmem_ld16(ta + 192u, c2);
+        tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const float d1 = m1[c] + c1[c], d2 = m2[c] + c2[c];
+          const float other = __shfl_xor_sync(0xffffffffu, d2, 1);
+          const float y = fmaf(sgn, other, d1) * inv;
+          sp[swz(ti | tn[32 * hcol + 16 * half + c])] = y;
+          m = fmaxf(m, fabsf(y));
+        }
       }
       m = warp_max(m);
       if (lane == 0) wmax[warp] = m;
@@ -548,7 +572,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_free(tmem, 128);
+    tmem_free(tmem, 256);
   }
 }
 
@@ -633,6 +657,9 @@ cudaError_t launch_tc_pass(const DevPass& pass, const uint32_t* runs_dev, const 
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTotal);
+    if (e != cudaSuccess) return e;
+    // the largest shared-memory carveout, so that two CTAs fit on an SM
+    e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }

@@ -520,6 +520,32 @@ class SampleFn(torch.autograd.Function):
         return SampleFn.apply(psi, u, n, nshots), 0
 
 
+class ProbabilityFn(torch.autograd.Function):
+    """p = |psi|^2 by the engine's probability kernel (re^2 + im^2 in fp32);
+    backward dL/dpsi = 2 g psi in torch's complex convention.  The vmap rule
+    runs the kernel once over the whole batch."""
+
+    @staticmethod
+    def forward(psi: torch.Tensor) -> torch.Tensor:  # type: ignore[override]
+        return probability_native(psi)
+
+    @staticmethod
+    def setup_context(ctx: Any, inputs: Tuple[Any, ...], output: Any) -> None:
+        ctx.save_for_backward(inputs[0])
+
+    @staticmethod
+    def backward(ctx: Any, g: torch.Tensor) -> torch.Tensor:  # type: ignore[override]
+        (psi,) = ctx.saved_tensors
+        return 2.0 * g * psi
+
+    @staticmethod
+    def vmap(info: Any, in_dims: Tuple[Any, ...], psi: torch.Tensor) -> Tuple[torch.Tensor, Any]:
+        d = in_dims[0]
+        if d is None:
+            return ProbabilityFn.apply(psi), None
+        return ProbabilityFn.apply(psi.movedim(d, 0)), 0
+
+
 def probability_native(psi: torch.Tensor) -> torch.Tensor:
     """|psi|^2 through the engine kernel (no autograd)."""
     lib = nat.load()

@@ -16,30 +16,28 @@ import torch
 Tensor = Any
 
 
+_PS_CODES = (("x", 1), ("y", 2), ("z", 3))
+
+
 def ps2xyz(ps: List[int]) -> Dict[str, List[int]]:
-    xyz: Dict[str, List[int]] = {"x": [], "y": [], "z": []}
-    for i, j in enumerate(ps):
-        if j == 1:
-            xyz["x"].append(i)
-        if j == 2:
-            xyz["y"].append(i)
-        if j == 3:
-            xyz["z"].append(i)
-    return xyz
+    """Per-qubit Pauli codes (0 = I, 1 = X, 2 = Y, 3 = Z) to the qubit lists
+    of each letter (tensorcircuit/quantum.py:1025-1045)."""
+    codes = np.asarray(ps).reshape(-1)
+    return {name: [int(i) for i in np.flatnonzero(codes == code)] for name, code in _PS_CODES}
 
 
 def xyz2ps(xyz: Dict[str, List[int]], n: Optional[int] = None) -> List[int]:
+    """Qubit lists per letter to per-qubit codes (tensorcircuit/quantum.py:
+    1048-1068).  Only qubits 0..n-1 count; a qubit listed under several
+    letters keeps the first of x, y, z."""
+    lists = {name: [int(i) for i in xyz.get(name, [])] for name, _ in _PS_CODES}
     if n is None:
-        n = max(xyz.get("x", []) + xyz.get("y", []) + xyz.get("z", [])) + 1
-    ps = [0 for _ in range(n)]
-    for i in range(n):
-        if i in xyz.get("x", []):
-            ps[i] = 1
-        elif i in xyz.get("y", []):
-            ps[i] = 2
-        elif i in xyz.get("z", []):
-            ps[i] = 3
-    return ps
+        n = max(lists["x"] + lists["y"] + lists["z"]) + 1
+    codes = np.zeros(n, dtype=np.int64)
+    for name, code in reversed(_PS_CODES):  # x written last, so it wins
+        idx = [i for i in lists[name] if 0 <= i < n]
+        codes[idx] = code
+    return [int(c) for c in codes]
 
 
 def _t(x: Any) -> torch.Tensor:

@@ -6,7 +6,8 @@ the reference's test asserts, with the reference file:line it comes from.
 The values are copied from the assertions in those test files (read as
 text; the reference cannot be imported in this environment).  Both the CPU
 oracle (tests/test_oracle_kats.py) and the GPU engine
-(tests/test_gpu_kats.py) are checked against them.
+(tests/test_gpu_engine.py, test_engine_reference_kats) are checked
+against them.
 """
 
 import numpy as np

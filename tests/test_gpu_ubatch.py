@@ -163,3 +163,32 @@ def test_uneven_batch_small_circuits_and_errors(tc):
         batch.UnevenBatch(specs, tile_bits=7, graph=False)  # wider than the 6-qubit circuits
     with pytest.raises(ValueError):
         ub.value_and_grad(np.zeros(3, np.float32))  # wrong parameter count
+
+
+def test_uneven_batch_wait_limit_runs_out_and_is_reported(tc):
+    """The persistent kernel's bounded dependency wait, made to run out
+    without faulting anything: a dependency count no sweep reaches is written
+    into the first segment's descriptor from the host and the wait limit is
+    1 ms.  The launch must finish, tcg_ubatch_check must report
+    TCG_ERR_TIMEOUT once (the flag then clears), and with the count restored
+    the batch computes correct values again."""
+    from tensorcircuit_gb300 import _native as nat
+    from tensorcircuit_gb300 import batch, templates
+
+    lib = nat.load()
+    rng = np.random.default_rng(23)
+    specs = [batch.qaoa_spec(n, templates.random_regular_graph(3, n, rng), 2) for n in (8, 10, 12)]
+    ub = batch.UnevenBatch(specs, tile_bits=6, graph=False, wait_limit_ns=1_000_000)
+    params = torch.tensor(np.concatenate([rng.uniform(0, np.pi, sp[2]) for sp in specs]), dtype=torch.float32)
+    e0, g0 = ub.value_and_grad(params)
+    ub.check()
+    nat.check(lib.tcg_debug_ubatch_set_need(ub.h.handle, 0, 0, 0xFFFFFFF0), "inject")
+    ub.value_and_grad(params)
+    torch.cuda.synchronize()
+    with pytest.raises(RuntimeError, match="ran out of time"):
+        ub.check()
+    ub.check()  # the flag was cleared by the check that reported it
+    nat.check(lib.tcg_debug_ubatch_set_need(ub.h.handle, 0, 0, 0), "restore")
+    e1, g1 = ub.value_and_grad(params)
+    ub.check()
+    assert torch.equal(e1, e0) and torch.equal(g1, g0)
