@@ -993,7 +993,7 @@ def run_warmstart(args, rank, world):
     l0 = lib.tcg_launch_count()
     with ClockSampler(dev.index) as clk:
         r = ws.study(n_train=args.instances, n_test=args.held_out, steps=300, gen_steps=args.gen_steps,
-                     epochs=args.epochs)
+                     epochs=args.epochs, plateau_chains=args.plateau_chains, plateau_steps=args.plateau_steps)
     launches = lib.tcg_launch_count() - l0
     if rank != 0:
         return
@@ -1004,7 +1004,8 @@ def run_warmstart(args, rank, world):
         "ms_per_step": 1e3 * sum(r["seconds"].values()), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 simulator / bf16 network activations", "data": "synthetic",
         "config": {"workload": "tfim_n16_hea6_warmstart", "train_chains": args.instances,
-                   "held_out": args.held_out, "epochs": args.epochs, "gen_steps": args.gen_steps, "seed": 6},
+                   "held_out": args.held_out, "epochs": args.epochs, "gen_steps": args.gen_steps, "seed": 6,
+                   "plateau_chains": args.plateau_chains, "plateau_steps": args.plateau_steps},
         "study": r,
         "generation_throughput": {"value": gen_evals / r["seconds"]["generate"],
                                   "unit": "n=16 energy+gradient evaluations/s"},
@@ -1035,7 +1036,9 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="hea: parameter vectors per step (64 is the configured workload; smaller "
                          "batches are for profiler captures)")
-    ap.add_argument("--instances", type=int, default=8192, help="warmstart: training chains")
+    ap.add_argument("--instances", type=int, default=20000, help="warmstart: training chains")
+    ap.add_argument("--plateau-chains", type=int, default=64, help="warmstart: held-out chains of the long runs")
+    ap.add_argument("--plateau-steps", type=int, default=5000, help="warmstart: Adam steps of the long runs")
     ap.add_argument("--held-out", type=int, default=1000, help="warmstart: held-out chains")
     ap.add_argument("--epochs", type=int, default=200, help="warmstart: network training epochs")
     ap.add_argument("--gen-steps", type=int, default=2500,

@@ -236,8 +236,29 @@ def steps_to(rel: np.ndarray, level: float) -> np.ndarray:
     return first
 
 
+LEVELS = (0.1, 0.05, 0.03, 0.02, 0.01, 5e-3, 2e-3, 1e-3)
+
+
+def level_table(rel_w: np.ndarray, rel_r: np.ndarray) -> Dict[str, Any]:
+    """Per relative-error level: the fraction of chains each start reaches it
+    in, and -- over the chains where both do -- the median Adam steps and
+    their ratio (random / warm)."""
+    out = {}
+    for lv in LEVELS:
+        sw, sr = steps_to(rel_w, lv), steps_to(rel_r, lv)
+        both = (sw < rel_w.shape[0]) & (sr < rel_r.shape[0])
+        row: Dict[str, Any] = {"reached_warm": float(np.mean(sw < rel_w.shape[0])),
+                               "reached_random": float(np.mean(sr < rel_r.shape[0])),
+                               "chains_both": int(both.sum())}
+        if both.any():
+            mw, mr = float(np.median(sw[both])), float(np.median(sr[both]))
+            row.update({"median_steps_warm": mw, "median_steps_random": mr, "ratio": mr / max(mw, 1.0)})
+        out["%g" % lv] = row
+    return out
+
+
 def study(n_train: int, n_test: int, steps: int = 300, gen_steps: int = 300, epochs: int = 200,
-          seed: int = 6, lr: float = 0.02) -> Dict[str, Any]:
+          seed: int = 6, lr: float = 0.02, plateau_chains: int = 0, plateau_steps: int = 0) -> Dict[str, Any]:
     """Generate training angles with the simulator, train the network, and
     compare warm-started and randomly started searches on held-out chains."""
     import time
@@ -267,6 +288,24 @@ def study(n_train: int, n_test: int, steps: int = 300, gen_steps: int = 300, epo
     s_r = steps_to(rel_r, level)
     gen_e0 = free_fermion_e0(Jtr, htr)
     checkpoints = sorted({k for k in (0, 10, 50, 100, 200, steps) if k <= steps})
+    plateau = None
+    if plateau_chains > 0 and plateau_steps > 0:
+        # long runs on the first held-out chains: where each start levels off
+        # and how many steps each needs to every level both reach
+        k = min(plateau_chains, n_test)
+        _, pw = search.run(Jte[:k], hte[:k], warm[:k], plateau_steps)
+        _, pr = search.run(Jte[:k], hte[:k], rand[:k], plateau_steps)
+        lw, lr_ = relative_errors(pw, e0[:k]), relative_errors(pr, e0[:k])
+        pcts = (10, 25, 50, 75, 90)
+        plateau = {
+            "chains": k, "steps": plateau_steps,
+            "final_rel_err_percentiles_warm": {str(q): float(np.percentile(lw[-1], q)) for q in pcts},
+            "final_rel_err_percentiles_random": {str(q): float(np.percentile(lr_[-1], q)) for q in pcts},
+            "best_rel_err_min_warm": float(lw.min()), "best_rel_err_min_random": float(lr_.min()),
+            "median_rel_err_at": {str(c): {"warm": float(np.median(lw[c])), "random": float(np.median(lr_[c]))}
+                                  for c in (0, 100, 300, 1000, 2000, 3000, plateau_steps) if c <= plateau_steps},
+            "levels": level_table(lw, lr_),
+        }
     return {
         "n_train": n_train, "n_test": n_test, "steps": steps, "gen_steps": gen_steps, "epochs": epochs,
         "train_rel_err_median": float(np.median(np.abs((hist_tr[-1] - gen_e0) / gen_e0))),
@@ -284,5 +323,7 @@ def study(n_train: int, n_test: int, steps: int = 300, gen_steps: int = 300, epo
         "step_ratio": float(np.median(s_r) / max(np.median(s_w), 1.0)),
         "reached_1e-3_warm": float(np.mean(rel_w.min(0) <= 1e-3)),
         "reached_1e-3_random": float(np.mean(rel_r.min(0) <= 1e-3)),
+        "levels": level_table(rel_w, rel_r),
+        "plateau": plateau,
         "seconds": {"generate": t_gen, "fit": t_fit, "evaluate": time.perf_counter() - t0 - t_gen - t_fit},
     }
