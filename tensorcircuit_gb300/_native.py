@@ -192,12 +192,13 @@ def debug_program(handle: Any, which: int) -> dict:
 
 class TcPassDesc(ctypes.Structure):
     _fields_ = [("pass_", ctypes.c_int32), ("block_begin", ctypes.c_int32), ("block_end", ctypes.c_int32),
-                ("pad", ctypes.c_int32)]
+                ("ldpair", ctypes.c_int32), ("ldaddr", ctypes.c_uint32 * 12)]
 
 
 class TcBlock(ctypes.Structure):
     _fields_ = [("bbits", ctypes.c_int32 * 6), ("cbits", ctypes.c_int32 * 6), ("gate_begin", ctypes.c_int32),
-                ("gate_end", ctypes.c_int32), ("slot", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("gate_end", ctypes.c_int32), ("slot", ctypes.c_int32), ("pairbit", ctypes.c_int32),
+                ("raddr", ctypes.c_uint32 * 64), ("caddr", ctypes.c_uint32 * 64)]
 
 
 class TcGate(ctypes.Structure):

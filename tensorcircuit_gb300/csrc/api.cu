@@ -107,12 +107,13 @@ bool tc_use_pass(const Program* P, int ps) {
 }
 
 // Per-device buffer of one forward call's fused matrices: [0, 256) error
-// flag, then batch * slots blocks of kTcMatBytes, then batch * slots scales.
-int tc_scratch(Program* P, int64_t batch, unsigned int** err, uint8_t** fused, float** scales) {
+// flag, then batch * slots blocks of kTcMatBytes, then batch * slots
+// {1 / matrix scale, gain bound} pairs.
+int tc_scratch(Program* P, int64_t batch, unsigned int** err, uint8_t** fused, float2** scales) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
   const size_t nmat = size_t(batch) * size_t(P->tc_slots);
-  const size_t need = 256 + nmat * kTcMatBytes + nmat * sizeof(float) + 256;
+  const size_t need = 256 + nmat * kTcMatBytes + nmat * sizeof(float2) + 256;
   std::lock_guard<std::mutex> lk(P->mu);
   Program::TcScratch& ts = P->tc_scratch[dev];
   if (ts.bytes < need) {
@@ -126,7 +127,7 @@ int tc_scratch(Program* P, int64_t batch, unsigned int** err, uint8_t** fused, f
   char* b = static_cast<char*>(ts.base);
   *err = reinterpret_cast<unsigned int*>(b);
   *fused = reinterpret_cast<uint8_t*>(b + 256);
-  *scales = reinterpret_cast<float*>(b + 256 + nmat * kTcMatBytes);
+  *scales = reinterpret_cast<float2*>(b + 256 + nmat * kTcMatBytes);
   return TCG_OK;
 }
 
@@ -152,7 +153,7 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
   bool any_tc = false;
   unsigned int* tc_err = nullptr;
   uint8_t* tc_fused = nullptr;
-  float* tc_scales = nullptr;
+  float2* tc_scales = nullptr;
   if (mode == MODE_FWD && !P->tc_passes.empty()) {
     for (int ps = 0; ps < (int)P->passes.size(); ++ps) any_tc = any_tc || tc_use_pass(P, ps);
     if (any_tc) {
@@ -166,9 +167,8 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
   auto tc_launch = [&](int ps) -> int {
     const TcPassDesc& d = P->tc_passes[P->tc_of_pass[ps]];
     const DevPass& dp = P->passes[ps];
-    return cuda_rc(launch_tc_pass(dp, a.prog.runs + dp.runs_off, a.prog.tc_blocks + d.block_begin,
-                                  d.block_end - d.block_begin, a.psi, a.n, batch, tc_fused, tc_scales, P->tc_slots,
-                                  tc_err, st));
+    return cuda_rc(launch_tc_pass(dp, d, a.prog.runs + dp.runs_off, a.prog.tc_blocks + d.block_begin, a.psi, a.n,
+                                  batch, tc_fused, tc_scales, P->tc_slots, tc_err, st));
   };
   if (jk) {
     KParams_Host kp;

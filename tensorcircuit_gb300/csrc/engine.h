@@ -113,18 +113,34 @@ struct TcGate {
   int64_t mat_off;   // per-circuit matrix offset (complex entries)
 };
 
+// Operand planes of a block in shared memory (bytes): re hi, re lo, im hi,
+// im lo; the im planes sit 64 bytes further so that re and im rows of one
+// store fall in different banks.  The fp32 copy of a tile before it goes
+// back to HBM uses the same region: re at 0, im at kTcPlaneIm.
+constexpr uint32_t kTcPlaneLo = 8192;
+constexpr uint32_t kTcPlaneIm = 16448;
+constexpr uint32_t kTcBRegion = 32832;
+
 struct TcBlock {
   int32_t bbits[6];  // tile bit of block-index bit i
   int32_t cbits[6];  // tile bit of column-index bit i
   int32_t gate_begin, gate_end;  // source gates, in application order
   int32_t slot;      // fused-matrix slot (per circuit) of this block
-  int32_t pad;
+  int32_t pairbit;   // column bit whose two values share one 32-bit word of
+                     // the next block's planes (-1: 16-bit stores)
+  // Where the epilogue writes output (block entry i, column n): byte offset
+  // raddr[i] ^ caddr[n] in the next block's operand planes, or, after the
+  // pass's last block, in the fp32 tile copy.  Both maps are linear over
+  // GF(2) (a bit permutation, then the staging swizzle), hence the XOR.
+  uint32_t raddr[64];
+  uint32_t caddr[64];
 };
 
 struct TcPassDesc {
   int32_t pass;      // pass index in the program
   int32_t block_begin, block_end;
-  int32_t pad;
+  int32_t ldpair;    // tile bit 0 is the first block's K bit 0: 32-bit stores
+  uint32_t ldaddr[12];  // operand-plane byte offset of tile bit t, first block
 };
 
 // Whole device program of one plan direction, in one device allocation.

@@ -120,11 +120,11 @@ size_t inner_scratch_bytes(int64_t len, int64_t batch);
 
 // tensor-core passes (tcpass.cu)
 cudaError_t launch_tc_fuse(const TcBlock* blocks, int nblocks, const TcGate* gates, const float2* mats,
-                           int64_t mat_stride, int64_t batch, uint8_t* fused, float* scales, int slots,
+                           int64_t mat_stride, int64_t batch, uint8_t* fused, float2* scales, int slots,
                            cudaStream_t st);
-cudaError_t launch_tc_pass(const DevPass& pass, const uint32_t* runs_dev, const TcBlock* blocks_dev, int nblocks,
-                           float2* psi, int n, int64_t batch, const uint8_t* fused, const float* scales, int slots,
-                           unsigned int* err, cudaStream_t st);
+cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const uint32_t* runs_dev,
+                           const TcBlock* blocks_dev, float2* psi, int n, int64_t batch, const uint8_t* fused,
+                           const float2* scales, int slots, unsigned int* err, cudaStream_t st);
 cudaError_t launch_tc_mma_probe(const void* A, const void* B, float* D, int K, int N, unsigned int* err,
                                 cudaStream_t st);
 

@@ -655,30 +655,128 @@ void fuse_pass_gates(const std::vector<uint32_t>& tb, std::vector<std::vector<in
   }
 }
 
-// Order `bits` so that its first `want` entries fall in distinct bank classes
-// (tile bit t flips bank bit t mod 5 of the staging copy), drawing classes
-// from `allowed`; returns how many of them did.
-int order_for_banks(std::vector<int>& bits, int want, uint32_t allowed) {
-  std::vector<int> out, rest = bits;
-  uint32_t used = 0;
-  for (int slot = 0; slot < want; ++slot) {
-    int pick = -1;
-    for (size_t c = 0; c < rest.size(); ++c) {
-      const int cls = rest[c] % 5;
-      if ((allowed >> cls & 1u) && !(used >> cls & 1u)) {
-        pick = (int)c;
-        break;
+// Byte-address bit, in a block's fp16 operand planes (K-major canonical
+// layout: element (row n, k) at (k & 7) * 2 + (n & 7) * 16 + (k >> 3) * 1024
+// + (n >> 3) * 128), of block-index bit i and of column bit i.
+constexpr int kKAddrBit[6] = {1, 2, 3, 10, 11, 12};
+constexpr int kNAddrBit[6] = {4, 5, 6, 7, 8, 9};
+
+uint32_t plane_bit(const TcBlock& b, int t) {
+  for (int i = 0; i < kTcBlockBits; ++i) {
+    if (b.bbits[i] == t) return 1u << kKAddrBit[i];
+    if (b.cbits[i] == t) return 1u << kNAddrBit[i];
+  }
+  return 0;
+}
+
+uint32_t plane_off(const TcBlock& b, uint32_t tile_off) {
+  uint32_t o = 0;
+  for (int t = 0; t < kTcTileBits; ++t)
+    if (tile_off >> t & 1u) o ^= plane_bit(b, t);
+  return o;
+}
+
+uint32_t expand6(uint32_t v, const int32_t* bits) {
+  uint32_t o = 0;
+  for (int i = 0; i < 6; ++i) o |= (v >> i & 1u) << bits[i];
+  return o;
+}
+
+inline uint32_t staging_swz(uint32_t t) { return t ^ (((t >> 5) ^ (t >> 10)) & 31u); }
+
+// Bit orders of the blocks of one pass (full[b] = the block's 6 tile bits).
+// The epilogue of block b writes, per lane, output rows that differ in
+// block bits 0..3 of b; those stores avoid bank conflicts when the four bits
+// are, in block b+1's planes, K bits 1, 2 and column bits 0, 1 (byte-address
+// bits 2..5), so block b+1 takes them there where it can.  Two outputs that
+// differ only in a column bit of b which is block b+1's K bit 0 share one
+// 32-bit word (the pairing bit, kept at a column position <= 3).  The first
+// block orders tile bits 0..5 the same way for the load of the tile.
+void order_tc_blocks(const std::vector<uint32_t>& full, std::vector<TcBlock>* out) {
+  const int m = (int)full.size();
+  std::vector<int> prev4;
+  int pair_in = -1;
+  for (int b = 0; b < m; ++b) {
+    const uint32_t B = full[b], Cs = ((1u << kTcTileBits) - 1) & ~B;
+    int bb[6], cb[6];
+    for (int i = 0; i < 6; ++i) bb[i] = cb[i] = -1;
+    auto has = [&](const int* v, int t) {
+      for (int i = 0; i < 6; ++i)
+        if (v[i] == t) return true;
+      return false;
+    };
+    std::vector<int> want;
+    int nslots = 2;
+    if (b == 0) {
+      if (B & 1u) bb[0] = 0;
+      want = {1, 2, 3, 4, 5};
+      nslots = 3;
+    } else {
+      if (pair_in >= 0) bb[0] = pair_in;
+      want = prev4;
+    }
+    int ki = 0, ni = 0;
+    for (int t : want) {
+      if (t < 0 || has(bb, t) || has(cb, t)) continue;
+      if ((B >> t & 1u) && ki < 2) bb[1 + ki++] = t;
+      else if ((Cs >> t & 1u) && ni < nslots) cb[ni++] = t;
+    }
+    int pair_out = -1;
+    if (b + 1 < m) {
+      const uint32_t cand = Cs & full[b + 1];
+      for (int pos = 0; pos < 4 && pair_out < 0; ++pos)
+        if (cb[pos] >= 0 && (cand >> cb[pos] & 1u)) pair_out = cb[pos];
+      for (int t = 0; t < kTcTileBits && pair_out < 0; ++t)
+        if ((cand >> t & 1u) && !has(cb, t))
+          for (int pos = 0; pos < 4; ++pos)
+            if (cb[pos] < 0) {
+              cb[pos] = t;
+              pair_out = t;
+              break;
+            }
+    }
+    for (int t = 0; t < kTcTileBits; ++t) {
+      int* v = (B >> t & 1u) ? bb : cb;
+      if (has(v, t)) continue;
+      for (int i = 0; i < 6; ++i)
+        if (v[i] < 0) {
+          v[i] = t;
+          break;
+        }
+    }
+    TcBlock& tb = (*out)[b];
+    std::memset(&tb, 0, sizeof(tb));
+    for (int i = 0; i < 6; ++i) {
+      tb.bbits[i] = bb[i];
+      tb.cbits[i] = cb[i];
+    }
+    prev4 = {bb[0], bb[1], bb[2], bb[3]};
+    pair_in = pair_out;
+  }
+}
+
+// Epilogue address tables of every block and the load table of the pass.
+void tc_tables(std::vector<TcBlock>* tbs, TcPassDesc* pd) {
+  const int m = (int)tbs->size();
+  for (int b = 0; b < m; ++b) {
+    TcBlock& t = (*tbs)[b];
+    t.pairbit = -1;
+    for (uint32_t v = 0; v < 64; ++v) {
+      const uint32_t tr = expand6(v, t.bbits), tc = expand6(v, t.cbits);
+      if (b + 1 < m) {
+        t.raddr[v] = plane_off((*tbs)[b + 1], tr);
+        t.caddr[v] = plane_off((*tbs)[b + 1], tc);
+      } else {
+        t.raddr[v] = staging_swz(tr) * 4u;
+        t.caddr[v] = staging_swz(tc) * 4u;
       }
     }
-    if (pick < 0) break;
-    used |= 1u << (rest[pick] % 5);
-    out.push_back(rest[pick]);
-    rest.erase(rest.begin() + pick);
+    if (b + 1 < m)
+      for (int pos = 0; pos < 4; ++pos)
+        if (plane_bit((*tbs)[b + 1], t.cbits[pos]) == 2u) t.pairbit = pos;
   }
-  const int good = (int)out.size();
-  for (int t : rest) out.push_back(t);
-  bits = out;
-  return good;
+  for (int t = 0; t < kTcTileBits; ++t) pd->ldaddr[t] = plane_bit((*tbs)[0], t);
+  pd->ldpair = pd->ldaddr[0] == 2u ? 1 : 0;
 }
 
 }  // namespace
@@ -716,45 +814,23 @@ void plan_tensor_passes(Program* P, const std::vector<PGate>& gates) {
     std::memset(&pd, 0, sizeof(pd));
     pd.pass = (int)ps;
     pd.block_begin = (int)P->tc_blocks.size();
-    for (size_t bi = 0; bi < blocks.size(); ++bi) {
-      // pad the block to 6 bits; choose the padding so that both bit orders
-      // avoid staging bank conflicts where possible
-      const uint32_t S = sets[bi];
-      std::vector<int> freeb;
-      for (int t = 0; t < kTcTileBits; ++t)
-        if (!(S >> t & 1u)) freeb.push_back(t);
-      const int need = kTcBlockBits - popc64(S);
-      uint32_t bestS = 0;
-      int bestscore = -1;
-      std::vector<int> bestb, bestc;
-      const int nf = (int)freeb.size();
-      for (uint32_t pick = 0; pick < (1u << nf); ++pick) {
-        if (popc64(pick) != need) continue;
-        uint32_t Sx = S;
-        for (int f = 0; f < nf; ++f)
-          if (pick >> f & 1u) Sx |= 1u << freeb[f];
-        std::vector<int> bb, cb;
-        for (int t = 0; t < kTcTileBits; ++t) ((Sx >> t & 1u) ? bb : cb).push_back(t);
-        const int score = order_for_banks(bb, 4, 0xFu) + order_for_banks(cb, 5, 0x1Fu);
-        if (score > bestscore) {
-          bestscore = score;
-          bestS = Sx;
-          bestb = bb;
-          bestc = cb;
-        }
-      }
-      (void)bestS;
-      TcBlock tbk;
-      std::memset(&tbk, 0, sizeof(tbk));
+    const int m = (int)blocks.size();
+    // pad every block to 6 tile bits (identity on the extra bits)
+    std::vector<uint32_t> full(m);
+    for (int b = 0; b < m; ++b) {
+      uint32_t Sx = sets[b];
+      for (int t = 0; t < kTcTileBits && popc64(Sx) < kTcBlockBits; ++t) Sx |= 1u << t;
+      full[b] = Sx;
+    }
+    std::vector<TcBlock> tbs(m);
+    order_tc_blocks(full, &tbs);
+    for (int b = 0; b < m; ++b) {
+      TcBlock& tbk = tbs[b];
       int blockpos_of_tile[32];
       for (int i = 0; i < 32; ++i) blockpos_of_tile[i] = -1;
-      for (int i = 0; i < kTcBlockBits; ++i) {
-        tbk.bbits[i] = bestb[i];
-        tbk.cbits[i] = bestc[i];
-        blockpos_of_tile[bestb[i]] = i;
-      }
+      for (int i = 0; i < kTcBlockBits; ++i) blockpos_of_tile[tbk.bbits[i]] = i;
       tbk.gate_begin = (int)P->tc_gates.size();
-      for (int gi : blocks[bi]) {
+      for (int gi : blocks[b]) {
         const PGate& g = gates[gl[gi]];
         TcGate G;
         std::memset(&G, 0, sizeof(G));
@@ -762,9 +838,9 @@ void plan_tensor_passes(Program* P, const std::vector<PGate>& gates) {
         G.k = g.k;
         for (int q = 0; q < g.k; ++q) G.pos[q] = blockpos_of_tile[tile_of_gbit[g.gbits[q]]];
         if (g.kind == TCG_GATE_PAULI_ROT) {
-          for (int b = 0; b < 64; ++b) {
-            if (g.xmask >> b & 1) G.xmask |= 1 << blockpos_of_tile[tile_of_gbit[b]];
-            if (g.zmask >> b & 1) G.zmask |= 1 << blockpos_of_tile[tile_of_gbit[b]];
+          for (int bit = 0; bit < 64; ++bit) {
+            if (g.xmask >> bit & 1) G.xmask |= 1 << blockpos_of_tile[tile_of_gbit[bit]];
+            if (g.zmask >> bit & 1) G.zmask |= 1 << blockpos_of_tile[tile_of_gbit[bit]];
           }
           G.nY = popc64(g.xmask & g.zmask);
         }
@@ -773,8 +849,9 @@ void plan_tensor_passes(Program* P, const std::vector<PGate>& gates) {
       }
       tbk.gate_end = (int)P->tc_gates.size();
       tbk.slot = P->tc_slots++;
-      P->tc_blocks.push_back(tbk);
     }
+    tc_tables(&tbs, &pd);
+    for (const TcBlock& t : tbs) P->tc_blocks.push_back(t);
     pd.block_end = (int)P->tc_blocks.size();
     P->tc_of_pass[ps] = (int)P->tc_passes.size();
     P->tc_passes.push_back(pd);

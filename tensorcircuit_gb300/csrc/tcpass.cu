@@ -21,16 +21,14 @@
 //     rescaled the same way before each block (per tile, from its largest
 //     component), so nothing overflows and the low halves stay normal.
 //
-// Data path per tile (one CTA, 256 threads, two CTAs per SM, 256 tensor-memory
-// columns each: per plane a main and a correction accumulator): the tile is
-// read from HBM once into an fp32 staging copy in shared memory; per block
-// the threads write the split B planes (K-major canonical layout, 16-byte
-// core-matrix rows), one thread issues 24 tcgen05.mma (M=128, N=64, K=16)
-// into tensor memory and commits them to an mbarrier, the fused matrix of the
-// NEXT block streams in with one bulk TMA copy (cp.async.bulk) while the
-// epilogue reads D back (tcgen05.ld), combines the planes and writes the
-// staging copy in natural order; after the last block the tile goes back to
-// HBM once.  All device-side waits are bounded (%globaltimer); a wait that
+// Data path per tile (one CTA, 256 threads, three CTAs per SM): the tile is
+// read from HBM once and written, split, into the first block's operand
+// planes (K-major canonical layout); per block one thread issues 24
+// tcgen05.mma (M=128, N=64, K=16) into tensor memory and commits them to an
+// mbarrier, the fused matrix of the NEXT block streams in with one bulk TMA
+// copy (cp.async.bulk) while the epilogue reads D back (tcgen05.ld) and
+// writes the next block's operand planes straight from registers; after the
+// last block the tile goes back to HBM once.  All device-side waits are bounded (%globaltimer); a wait that
 // runs out sets an error flag (tcg_plan_check reports it), waits once more
 // for the copies it issued, frees its tensor memory and ends the CTA.
 //
@@ -53,15 +51,13 @@ namespace {
 constexpr int kTcThreads = 256;
 constexpr unsigned long long kTcWaitNs = 2000000000ull;  // 2 s per wait
 
-// shared-memory map of the pass kernel (bytes)
-constexpr uint32_t kSmA = 0;             // fused block: hi plane, lo plane (16 KiB each)
-constexpr uint32_t kSmB = 32768;         // B planes: re_hi, re_lo, im_hi, im_lo (8 KiB each)
-constexpr uint32_t kSmS = 65536;         // staging: re (4096 floats), pad 16 floats, im
-constexpr uint32_t kStIm = 4096 + 16;    // im plane offset in floats (flips bank bit 4)
-constexpr uint32_t kSmT = kSmS + (4096 + 16 + 4096) * 4;  // tables tj[64], tn[64]
-constexpr uint32_t kSmW = kSmT + 512;    // warp maxima [8]
-constexpr uint32_t kSmM = kSmW + 64;     // mbarriers: matrix copy, MMA completion
-constexpr uint32_t kSmX = kSmM + 16;     // tensor-memory base address, abort flag
+// shared-memory map of the pass kernel (bytes): three CTAs fit on an SM
+constexpr uint32_t kSmA = 0;                  // fused block: hi plane, lo plane (16 KiB each)
+constexpr uint32_t kSmB = 32768;              // operand planes, or the fp32 tile copy
+constexpr uint32_t kSmT = kSmB + kTcBRegion;  // epilogue address tables raddr[64], caddr[64]
+constexpr uint32_t kSmW = kSmT + 512;         // warp maxima [8]
+constexpr uint32_t kSmM = kSmW + 32;          // mbarriers: matrix copy, MMA completion
+constexpr uint32_t kSmX = kSmM + 16;          // tensor-memory base, abort flag, copy in flight
 constexpr uint32_t kSmTotal = kSmX + 16;
 
 // canonical K-major, no-swizzle layout of a 16-bit operand: core matrices of
@@ -205,13 +201,6 @@ __device__ __forceinline__ void pow2_scale(float m, float& s, float& inv) {
   inv = __uint_as_float((uint32_t)(127 - es) << 23);
 }
 
-__device__ __forceinline__ uint32_t expand_bits(uint32_t v, const int32_t (&bits)[6]) {
-  uint32_t o = 0;
-#pragma unroll
-  for (int i = 0; i < 6; ++i) o |= ((v >> i) & 1u) << bits[i];
-  return o;
-}
-
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -228,10 +217,11 @@ __device__ __forceinline__ float warp_max(float v) {
 __global__ void __launch_bounds__(256) tc_fuse_kernel(const TcBlock* __restrict__ blocks,
                                                        const TcGate* __restrict__ gates,
                                                        const float2* __restrict__ mats, int64_t mat_stride,
-                                                       uint8_t* __restrict__ fused, float* __restrict__ scales,
+                                                       uint8_t* __restrict__ fused, float2* __restrict__ scales,
                                                        int slots) {
   __shared__ float2 F[64 * 65];  // F[i * 65 + j]: row i (output), column j (input)
   __shared__ float red[8];
+  __shared__ float rowsum[64];
   const TcBlock blk = blocks[blockIdx.x];
   const int64_t b = blockIdx.y;
   const int tid = threadIdx.x;
@@ -333,8 +323,19 @@ __global__ void __launch_bounds__(256) tc_fuse_kernel(const TcBlock* __restrict_
   for (int w = 1; w < 8; ++w) mx = fmaxf(mx, red[w]);
   float s, inv;
   pow2_scale(mx, s, inv);
+  // bound on the block's gain in one component: max_i sum_j |Re F_ij| + |Im F_ij|
+  if (tid < 64) {
+    float r = 0.f;
+    for (int j = 0; j < 64; ++j) r += fabsf(F[tid * 65 + j].x) + fabsf(F[tid * 65 + j].y);
+    rowsum[tid] = r;
+  }
+  __syncthreads();
   const int64_t slot = b * slots + blk.slot;
-  if (tid == 0) scales[slot] = inv;
+  if (tid == 0) {
+    float r = 0.f;
+    for (int i = 0; i < 64; ++i) r = fmaxf(r, rowsum[i]);
+    scales[slot] = make_float2(inv, r);
+  }
   uint8_t* out = fused + slot * kTcMatBytes;
   __half* hi = reinterpret_cast<__half*>(out);
   __half* lo = reinterpret_cast<__half*>(out + kTcMatBytes / 2);
@@ -360,19 +361,66 @@ struct TcArgs {
   const uint32_t* runs;
   const TcBlock* blocks;
   int nblocks;
+  int ldpair;
+  uint32_t ldaddr[12];
   const uint8_t* fused;
-  const float* scales;
+  const float2* scales;
   int slots;
   unsigned int* err;
 };
 
-__global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) {
+namespace {
+
+// v = hi + lo, both fp16, at plane byte offset p (lo plane kTcPlaneLo further)
+__device__ __forceinline__ void put1(uint8_t* p, float v) {
+  const __half h = __float2half_rn(v);
+  const __half l = __float2half_rn(v - __half2float(h));
+  *reinterpret_cast<__half*>(p) = h;
+  *reinterpret_cast<__half*>(p + kTcPlaneLo) = l;
+}
+// two values that share one 32-bit word (v0 at the lower address)
+__device__ __forceinline__ void put2(uint8_t* p, float v0, float v1) {
+  const __half2 hh = __floats2half2_rn(v0, v1);
+  const float2 hf = __half22float2(hh);
+  const __half2 ll = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
+  *reinterpret_cast<__half2*>(p) = hh;
+  *reinterpret_cast<__half2*>(p + kTcPlaneLo) = ll;
+}
+
+template <int P>
+__device__ __forceinline__ void put_pairs(uint8_t* pl, uint32_t R, const uint32_t* ct, const float (&v)[16]) {
+#pragma unroll
+  for (int c = 0; c < 16; ++c)
+    if (!((c >> P) & 1)) put2(pl + (R ^ ct[c]), v[c], v[c | (1 << P)]);
+}
+
+}  // namespace
+
+// One tile of a tensor-core pass: 4096 amplitudes, every fused block of the
+// pass, one read and one write of the tile in HBM.  256 threads, three CTAs
+// per SM (66 KiB of shared memory, 128 tensor-memory columns each).
+//
+// Per block: one thread waits for the block's matrix (bulk copy), issues 12
+// MMAs (M=128, N=64, K=16) per plane into one fp32 accumulator -- the two
+// correction products first, the main product last, so the tensor core's
+// truncating accumulation touches the full-size value only four times -- and
+// commits them; every warp waits, thread 0 streams in the next block's
+// matrix, and the epilogue turns D into the next block's split operand
+// planes directly: Re/Im combination (one lane shuffle), the exact
+// power-of-two rescale, fp16 hi/lo split, stores at raddr[i] ^ caddr[n]
+// (two values per 32-bit word where the next block's K bit 0 is one of this
+// block's column bits).  The scale for the next block comes from a bound
+// (2 x max row sum of |F| x the input's largest component), so no extra
+// reduction pass is needed; the exact largest output is reduced alongside
+// for the block after.  The last block writes fp32 values in natural order,
+// which go back to HBM as one coalesced store of the tile.
+__global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
-  float* st = reinterpret_cast<float*>(smem + kSmS);
-  uint32_t* tj = reinterpret_cast<uint32_t*>(smem + kSmT);
-  uint32_t* tn = tj + 64;
+  uint8_t* bp = smem + kSmB;
+  uint32_t* rtab = reinterpret_cast<uint32_t*>(smem + kSmT);
+  uint32_t* ctab = rtab + 64;
   float* wmax = reinterpret_cast<float*>(smem + kSmW);
   const uint32_t bar_mat = sbase + kSmM, bar_mma = sbase + kSmM + 8;
   volatile uint32_t* sx = reinterpret_cast<volatile uint32_t*>(smem + kSmX);
@@ -384,14 +432,15 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
     if ((tile >> i) & 1u) base |= 1u << a.nlbits[i];
   float2* psi = a.psi + b * ((int64_t)1 << a.n);
   const uint8_t* fused_b = a.fused + b * a.slots * (int64_t)kTcMatBytes;
-  const float* scales_b = a.scales + b * a.slots;
+  const float2* scales_b = a.scales + b * a.slots;
 
-  if (warp == 0) tmem_alloc(sbase + kSmX, 256);
+  if (warp == 0) tmem_alloc(sbase + kSmX, 128);
   if (tid == 0) {
     mbar_init(bar_mat, 1);
     mbar_init(bar_mma, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sx[1] = 0;
+    sx[2] = 0;
   }
   fence_async_smem();
   tc_fence_before();
@@ -399,66 +448,62 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
   tc_fence_after();
   const uint32_t tmem = sx[0];
   uint32_t ph_mat = 0, ph_mma = 0;
-  bool mat_pending = false, mma_pending = false;
-
   if (tid == 0) {  // first block's matrix
+    sx[2] = 1;
     mbar_expect_tx(bar_mat, kTcMatBytes);
     bulk_g2s(sbase + kSmA, fused_b + (int64_t)a.blocks[0].slot * kTcMatBytes, kTcMatBytes, bar_mat);
   }
-  mat_pending = true;
 
-  // tile -> staging (natural tile order, swizzled), largest component
+  // ---- the tile: 8 float4 (16 amplitudes) per thread, its largest component
+  float4 xv[8];
   float lmax = 0.f;
-  for (uint32_t i = tid; i < 2048u; i += kTcThreads) {
-    const uint32_t j = 2 * i;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const uint32_t j = 2u * (uint32_t)(tid + kTcThreads * u);
     const uint32_t off = __ldg(a.runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
-    const float4 q = __ldcg(reinterpret_cast<const float4*>(psi + (base | off)));
-    st[swz(j)] = q.x;
-    st[kStIm + swz(j)] = q.y;
-    st[swz(j + 1)] = q.z;
-    st[kStIm + swz(j + 1)] = q.w;
-    lmax = fmaxf(lmax, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
+    xv[u] = __ldcg(reinterpret_cast<const float4*>(psi + (base | off)));
+    lmax = fmaxf(lmax, fmaxf(fmaxf(fabsf(xv[u].x), fabsf(xv[u].y)), fmaxf(fabsf(xv[u].z), fabsf(xv[u].w))));
   }
   lmax = warp_max(lmax);
   if (lane == 0) wmax[warp] = lmax;
   __syncthreads();
-  float sxs, sxinv;
+  float max_in = wmax[0];
+  for (int w = 1; w < 8; ++w) max_in = fmaxf(max_in, wmax[w]);
+  float s_in, sinv_in;
+  pow2_scale(max_in, s_in, sinv_in);
+  // ---- first block's operand planes: the plane offset is linear in the
+  // tile offset 2 * (tid + 256 u) + e
   {
-    float m = wmax[0];
-    for (int w = 1; w < 8; ++w) m = fmaxf(m, wmax[w]);
-    pow2_scale(m, sxs, sxinv);
+    uint32_t tb = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if ((tid >> k) & 1) tb ^= a.ldaddr[1 + k];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const uint32_t ad = tb ^ ((u & 1) ? a.ldaddr[9] : 0u) ^ ((u & 2) ? a.ldaddr[10] : 0u) ^
+                          ((u & 4) ? a.ldaddr[11] : 0u);
+      const float r0 = xv[u].x * s_in, i0 = xv[u].y * s_in, r1 = xv[u].z * s_in, i1 = xv[u].w * s_in;
+      if (a.ldpair) {
+        put2(bp + ad, r0, r1);
+        put2(bp + kTcPlaneIm + ad, i0, i1);
+      } else {
+        const uint32_t ad1 = ad ^ a.ldaddr[0];
+        put1(bp + ad, r0);
+        put1(bp + ad1, r1);
+        put1(bp + kTcPlaneIm + ad, i0);
+        put1(bp + kTcPlaneIm + ad1, i1);
+      }
+    }
   }
 
   const uint32_t idesc = make_idesc(128, 64);
   bool abort = false;
-  for (int bi = 0; bi < a.nblocks && !abort; ++bi) {
-    const TcBlock blk = a.blocks[bi];
-    if (tid < 64) tj[tid] = expand_bits((uint32_t)tid, blk.bbits);
-    else if (tid < 128) tn[tid - 64] = expand_bits((uint32_t)(tid - 64), blk.cbits);
-    __syncthreads();
-    // ---- split B planes: task = (plane p, column n, k-group k8)
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int id = tid + kTcThreads * u;
-      const int n = id & 63, k8 = (id >> 6) & 7, p = id >> 9;
-      const float* sp = st + (p ? kStIm : 0u);
-      const uint32_t tcol = tn[n];
-      uint32_t h[4], l[4];
-#pragma unroll
-      for (int r = 0; r < 8; r += 2) {
-        const float v0 = sp[swz(tj[8 * k8 + r] | tcol)] * sxs;
-        const float v1 = sp[swz(tj[8 * k8 + r + 1] | tcol)] * sxs;
-        const __half2 hh = __floats2half2_rn(v0, v1);
-        const float2 hf = __half22float2(hh);
-        const __half2 ll = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
-        h[r >> 1] = *reinterpret_cast<const uint32_t*>(&hh);
-        l[r >> 1] = *reinterpret_cast<const uint32_t*>(&ll);
-      }
-      const uint32_t off = kmajor_off((uint32_t)n, (uint32_t)(8 * k8), kLboB);
-      uint8_t* pb = smem + kSmB + (uint32_t)p * 16384u;
-      *reinterpret_cast<uint4*>(pb + off) = make_uint4(h[0], h[1], h[2], h[3]);
-      *reinterpret_cast<uint4*>(pb + 8192 + off) = make_uint4(l[0], l[1], l[2], l[3]);
-    }
+  for (int bi = 0; bi < a.nblocks; ++bi) {
+    const TcBlock& blk = a.blocks[bi];
+    const bool last = bi + 1 == a.nblocks;
+    if (tid < 64) rtab[tid] = blk.raddr[tid];
+    else if (tid < 128) ctab[tid - 64] = blk.caddr[tid - 64];
+    const float2 sc = __ldg(scales_b + blk.slot);  // {1 / matrix scale, gain bound}
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -466,113 +511,122 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
     if (tid == 0) {
       tc_fence_after();
       if (!mbar_wait(bar_mat, ph_mat, kTcWaitNs)) {
-        sx[1] = 1;
+        sx[1] = 1;  // nothing is committed: the waits below run out as well
       } else {
         ph_mat ^= 1;
-        // per plane p: main accumulator (hi x hi) at column 128p, correction
-        // accumulator (hi x lo + lo x hi) at 128p + 64.  The tensor core's fp32
-        // accumulation truncates; keeping the small corrections apart means the
-        // main value takes 3 accumulating steps instead of 11 (the epilogue
-        // adds the two with round-to-nearest).
+        sx[2] = 0;
 #pragma unroll
         for (int p = 0; p < 2; ++p) {
-          const uint32_t dm = tmem + 128u * p, dc = dm + 64u;
-          const uint32_t bh = sbase + kSmB + p * 16384u, bl = bh + 8192u;
+          const uint32_t d = tmem + 64u * p;
+          const uint32_t bh = sbase + kSmB + p * kTcPlaneIm, bl = bh + kTcPlaneLo;
 #pragma unroll
           for (int s = 0; s < 4; ++s)
-            mma_f16(dm, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
-                    make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, s > 0);
-#pragma unroll
-          for (int s = 0; s < 4; ++s)
-            mma_f16(dc, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
+            mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
                     make_desc(bl + s * 2 * kLboB, kLboB, 128), idesc, s > 0);
 #pragma unroll
           for (int s = 0; s < 4; ++s)
-            mma_f16(dc, make_desc(sbase + kSmA + 16384 + s * 2 * kLboA, kLboA, 128),
+            mma_f16(d, make_desc(sbase + kSmA + 16384 + s * 2 * kLboA, kLboA, 128),
+                    make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, 1);
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+            mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
                     make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, 1);
         }
         mma_commit(bar_mma);
       }
     }
-    __syncthreads();
-    if (sx[1]) {  // the matrix copy did not arrive: nothing was issued
-      abort = true;
-      break;
+    uint32_t ok = 0;
+    if (lane == 0) ok = mbar_wait(bar_mma, ph_mma, kTcWaitNs) ? 1u : 0u;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) {
+      sx[1] = 1;
+    } else {
+      if (tid == 0 && !last) {  // the tensor core is done with A: next matrix
+        sx[2] = 1;
+        mbar_expect_tx(bar_mat, kTcMatBytes);
+        bulk_g2s(sbase + kSmA, fused_b + (int64_t)a.blocks[bi + 1].slot * kTcMatBytes, kTcMatBytes, bar_mat);
+      }
+      tc_fence_after();
+      // ---- epilogue
+      float s_out = 1.f, sinv_out = 1.f;
+      if (!last) pow2_scale(2.f * sc.y * max_in, s_out, sinv_out);
+      const float f = s_out * sc.x * sinv_in;
+      const int q = warp & 3, hc = warp >> 2;
+      const int row = 32 * q + lane;
+      const uint32_t R = rtab[row >> 1];
+      uint8_t* pl = bp + ((row & 1) ? kTcPlaneIm : 0u);
+      const float sgn = (row & 1) ? 1.f : -1.f;
+      const int pb = blk.pairbit;
+      float m = 0.f;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int col0 = 32 * hc + 16 * half;
+        const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0;
+        float d0[16], d1[16], v[16];
+        tmem_ld16(ta, d0);
+        tmem_ld16(ta + 64u, d1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          v[c] = fmaf(sgn, __shfl_xor_sync(0xffffffffu, d1[c], 1), d0[c]) * f;
+          m = fmaxf(m, fabsf(v[c]));
+        }
+        const uint32_t* ct = ctab + col0;
+        if (last) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) *reinterpret_cast<float*>(pl + (R ^ ct[c])) = v[c];
+        } else {
+          switch (pb) {
+            case 0: put_pairs<0>(pl, R, ct, v); break;
+            case 1: put_pairs<1>(pl, R, ct, v); break;
+            case 2: put_pairs<2>(pl, R, ct, v); break;
+            case 3: put_pairs<3>(pl, R, ct, v); break;
+            default:
+#pragma unroll
+              for (int c = 0; c < 16; ++c) put1(pl + (R ^ ct[c]), v[c]);
+          }
+        }
+      }
+      m = warp_max(m);
+      if (lane == 0) wmax[warp] = m * sinv_out;
+      s_in = s_out;
+      sinv_in = sinv_out;
     }
-    mat_pending = false;
-    mma_pending = true;
-    if (!mbar_wait(bar_mma, ph_mma, kTcWaitNs)) sx[1] = 1;
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
     if (sx[1]) {
       abort = true;
       break;
     }
     ph_mma ^= 1;
-    mma_pending = false;
-    tc_fence_after();
-    // ---- the tensor core is done with A and B: stream in the next matrix
-    if (tid == 0 && bi + 1 < a.nblocks) {
-      mbar_expect_tx(bar_mat, kTcMatBytes);
-      bulk_g2s(sbase + kSmA, fused_b + (int64_t)a.blocks[bi + 1].slot * kTcMatBytes, kTcMatBytes, bar_mat);
-    }
-    if (bi + 1 < a.nblocks) mat_pending = true;
-    // ---- epilogue: D -> combined outputs -> staging (natural order)
-    {
-      const int q = warp & 3, hcol = warp >> 2;
-      const float inv = sxinv * __ldg(scales_b + blk.slot);
-      const int row = 32 * q + lane;
-      const uint32_t ti = tj[row >> 1];
-      float* sp = st + ((row & 1) ? kStIm : 0u);
-      const float sgn = (row & 1) ? 1.f : -1.f;
-      float m = 0.f;
-#pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + 32u * hcol + 16u * half;
-        float m1[16], c1[16], m2[16], c2[16];
-        tmem_ld16(ta, m1);
-        tmem_ld16(ta + 64u, c1);
-        tmem_ld16(ta + 128u, m2);
-        tmem_ld16(ta + 192u, c2);
-        tmem_wait_ld();
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const float d1 = m1[c] + c1[c], d2 = m2[c] + c2[c];
-          const float other = __shfl_xor_sync(0xffffffffu, d2, 1);
-          const float y = fmaf(sgn, other, d1) * inv;
-          sp[swz(ti | tn[32 * hcol + 16 * half + c])] = y;
-          m = fmaxf(m, fabsf(y));
-        }
-      }
-      m = warp_max(m);
-      if (lane == 0) wmax[warp] = m;
-    }
-    tc_fence_before();
-    __syncthreads();
-    {
-      float m = wmax[0];
-      for (int w = 1; w < 8; ++w) m = fmaxf(m, wmax[w]);
-      pow2_scale(m, sxs, sxinv);
-    }
+    max_in = wmax[0];
+    for (int w = 1; w < 8; ++w) max_in = fmaxf(max_in, wmax[w]);
   }
 
   if (!abort) {
-    for (uint32_t i = tid; i < 2048u; i += kTcThreads) {
-      const uint32_t j = 2 * i;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const uint32_t j = 2u * (uint32_t)(tid + kTcThreads * u);
       const uint32_t off = __ldg(a.runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
-      const float4 q = make_float4(st[swz(j)], st[kStIm + swz(j)], st[swz(j + 1)], st[kStIm + swz(j + 1)]);
-      *reinterpret_cast<float4*>(psi + (base | off)) = q;
+      const uint32_t w0 = swz(j) * 4u, w1 = swz(j + 1) * 4u;
+      const float4 o = make_float4(*reinterpret_cast<const float*>(bp + w0),
+                                   *reinterpret_cast<const float*>(bp + kTcPlaneIm + w0),
+                                   *reinterpret_cast<const float*>(bp + w1),
+                                   *reinterpret_cast<const float*>(bp + kTcPlaneIm + w1));
+      *reinterpret_cast<float4*>(psi + (base | off)) = o;
     }
   } else {
     if (tid == 0) atomicExch(a.err, 1u);
-    // let the copies this CTA issued finish before its memory goes away
-    if (mat_pending) mbar_wait(bar_mat, ph_mat, kTcWaitNs);
-    if (mma_pending) mbar_wait(bar_mma, ph_mma, kTcWaitNs);
+    // let the copies and MMAs this CTA issued finish before its memory goes away
+    if (sx[2]) mbar_wait(bar_mat, ph_mat, kTcWaitNs);
+    mbar_wait(bar_mma, ph_mma, kTcWaitNs);
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_free(tmem, 256);
+    tmem_free(tmem, 128);
   }
 }
 
@@ -642,7 +696,7 @@ __global__ void __launch_bounds__(128) tc_mma_probe_kernel(const __half* __restr
 
 // ============================================================================
 cudaError_t launch_tc_fuse(const TcBlock* blocks, int nblocks, const TcGate* gates, const float2* mats,
-                           int64_t mat_stride, int64_t batch, uint8_t* fused, float* scales, int slots,
+                           int64_t mat_stride, int64_t batch, uint8_t* fused, float2* scales, int slots,
                            cudaStream_t st) {
   if (nblocks <= 0 || batch <= 0) return cudaSuccess;
   dim3 grid((unsigned)nblocks, (unsigned)batch);
@@ -651,14 +705,14 @@ cudaError_t launch_tc_fuse(const TcBlock* blocks, int nblocks, const TcGate* gat
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc_pass(const DevPass& pass, const uint32_t* runs_dev, const TcBlock* blocks_dev, int nblocks,
-                           float2* psi, int n, int64_t batch, const uint8_t* fused, const float* scales, int slots,
-                           unsigned int* err, cudaStream_t st) {
+cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const uint32_t* runs_dev,
+                           const TcBlock* blocks_dev, float2* psi, int n, int64_t batch, const uint8_t* fused,
+                           const float2* scales, int slots, unsigned int* err, cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTotal);
     if (e != cudaSuccess) return e;
-    // the largest shared-memory carveout, so that two CTAs fit on an SM
+    // the largest shared-memory carveout, so that three CTAs fit on an SM
     e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     attr_set = true;
@@ -671,7 +725,9 @@ cudaError_t launch_tc_pass(const DevPass& pass, const uint32_t* runs_dev, const 
   for (int i = 0; i < kMaxQubits; ++i) a.nlbits[i] = pass.nlbits[i];
   a.runs = runs_dev;
   a.blocks = blocks_dev;
-  a.nblocks = nblocks;
+  a.nblocks = desc.block_end - desc.block_begin;
+  a.ldpair = desc.ldpair;
+  for (int i = 0; i < 12; ++i) a.ldaddr[i] = desc.ldaddr[i];
   a.fused = fused;
   a.scales = scales;
   a.slots = slots;

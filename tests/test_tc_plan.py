@@ -53,36 +53,112 @@ def block_matrix(blk, gates, mats):
     return F
 
 
-def emulate_tc_pass(psi, P, blocks, gates, mats, n):
+PLANE_LO, PLANE_IM = 8192, 16448
+
+
+def kmajor_off(row, k, lbo=1024):
+    return (k & 7) * 2 + (row & 7) * 16 + (k >> 3) * lbo + (row >> 3) * 128
+
+
+def swz(t):
+    return t ^ (((t >> 5) ^ (t >> 10)) & 31)
+
+
+def emulate_tc_pass(psi, P, desc, blocks, gates, mats, n, stats=None):
+    """Replays the tensor-core pass kernel's data movement byte for byte:
+    the tile load through the pass's load table, operand planes read the way
+    the MMA descriptors address them (K-major canonical layout), the planar
+    complex GEMM, and the epilogue stores through each block's XOR tables
+    (two values per 32-bit word on the pairing bit) into the next block's
+    planes or the fp32 tile copy.  Values are kept exact (no fp16 split):
+    this checks addresses, not rounding."""
     lbits = [P.lbits[i] for i in range(P.L)]
     nl = [P.nlbits[i] for i in range(P.nnonlocal)]
     gl = dep(np.arange(1 << P.L), lbits)
+    ld = [desc.ldaddr[t] for t in range(12)]
+    mats_f = [block_matrix(blk, gates, mats) for blk in blocks]
     for blk in blocks:
         bb = [blk.bbits[i] for i in range(6)]
         cb = [blk.cbits[i] for i in range(6)]
         assert sorted(bb + cb) == list(range(12)), "block + column bits must partition the tile"
-    mats_f = [block_matrix(blk, gates, mats) for blk in blocks]
+    tid = np.arange(256)
+    tb = np.zeros(256, np.int64)
+    for k in range(8):
+        tb ^= np.where((tid >> k) & 1, ld[1 + k], 0)
     for tile in range(1 << (n - P.L)):
         base = int(dep(tile, nl))
         T = psi[base | gl].copy()
-        for blk, F in zip(blocks, mats_f):
-            tj = dep(np.arange(64), [blk.bbits[i] for i in range(6)])
-            tn = dep(np.arange(64), [blk.cbits[i] for i in range(6)])
-            idx = tj[:, None] | tn[None, :]
-            assert len(np.unique(idx)) == 4096
-            x = T[idx]
+        mem = {}
+
+        def put(off, v):
+            assert 0 <= off and off + 2 <= 32832 and (off % 2) == 0
+            mem[int(off)] = v
+
+        for u in range(8):
+            ad = tb ^ (ld[9] if u & 1 else 0) ^ (ld[10] if u & 2 else 0) ^ (ld[11] if u & 4 else 0)
+            j = 2 * (tid + 256 * u)
+            for t in range(256):
+                x0, x1 = T[j[t]], T[j[t] + 1]
+                a0 = int(ad[t])
+                a1 = a0 + 2 if desc.ldpair else a0 ^ ld[0]
+                put(a0, x0.real)
+                put(a1, x1.real)
+                put(PLANE_IM + a0, x0.imag)
+                put(PLANE_IM + a1, x1.imag)
+        for bi, (blk, F) in enumerate(zip(blocks, mats_f)):
+            last = bi + 1 == len(blocks)
+            k = np.arange(64)[:, None]
+            nn = np.arange(64)[None, :]
+            offs = kmajor_off(nn, k)
+            assert len(mem) == 2 * 4096, "every operand element written once"
+            xre = np.vectorize(lambda o: mem[int(o)])(offs)
+            xim = np.vectorize(lambda o: mem[PLANE_IM + int(o)])(offs)
             A = np.empty((128, 64))
             A[0::2] = F.real
             A[1::2] = F.imag
-            D1 = A @ x.real
-            D2 = A @ x.imag
-            y = (D1[0::2] - D2[1::2]) + 1j * (D2[0::2] + D1[1::2])
-            T[idx] = y
-        psi[base | gl] = T
+            D0, D1 = A @ xre, A @ xim
+            rows = np.arange(128)
+            sgn = np.where(rows & 1, 1.0, -1.0)[:, None]
+            V = D0 + sgn * D1[rows ^ 1]
+            R = np.array([blk.raddr[i] for i in range(64)])
+            C = np.array([blk.caddr[i] for i in range(64)])
+            mem = {}
+            pb = blk.pairbit
+            for row in range(128):
+                plane = PLANE_IM if row & 1 else 0
+                for col in range(64):
+                    off = plane + int(R[row >> 1] ^ C[col])
+                    if last:
+                        mem[off] = V[row, col]
+                    elif pb >= 0:
+                        if (col >> pb) & 1:
+                            continue
+                        partner = col | (1 << pb)
+                        assert (off & 2) == 0 and plane + int(R[row >> 1] ^ C[partner]) == off + 2
+                        mem[off] = V[row, col]
+                        mem[off + 2] = V[row, partner]
+                    else:
+                        mem[off] = V[row, col]
+            if stats is not None and not last:
+                # 4-byte-word banks of one store instruction: 32 lanes = 16 rows x re/im
+                worst = 1
+                for q in range(4):
+                    for col in range(0, 64, 1 if pb < 0 else 2):
+                        banks = {}
+                        for lane in range(32):
+                            row = 32 * q + lane
+                            off = (PLANE_IM if row & 1 else 0) + int(R[row >> 1] ^ C[col])
+                            banks.setdefault((off >> 2) & 31, set()).add(off >> 2)
+                        worst = max(worst, max(len(v) for v in banks.values()))
+                stats.append(worst)
+        out = np.empty(4096, np.complex128)
+        for j in range(4096):
+            out[j] = mem[swz(j) * 4] + 1j * mem[PLANE_IM + swz(j) * 4]
+        psi[base | gl] = out
     return psi
 
 
-def emulate_forward(n, entry, mats):
+def emulate_forward(n, entry, mats, stats=None):
     prog = nat.debug_program(entry.plan.handle, 0)
     tcp = nat.debug_tc_program(entry.plan.handle)
     by_pass = {d.pass_: d for d in tcp["passes"]}
@@ -92,7 +168,8 @@ def emulate_forward(n, entry, mats):
     for pi, P in enumerate(prog["passes"]):
         if pi in by_pass:
             d = by_pass[pi]
-            psi = emulate_tc_pass(psi, P, tcp["blocks"][d.block_begin:d.block_end], tcp["gates"], mats, n)
+            psi = emulate_tc_pass(psi, P, d, tcp["blocks"][d.block_begin:d.block_end], tcp["gates"], mats, n,
+                                  stats)
             used += 1
         else:
             one = dict(prog)
@@ -138,3 +215,15 @@ def test_tc_blocks_respect_six_bits_and_order():
                 used |= 1 << G.pos[q]
         assert bin(used).count("1") <= 6
     assert len(tcp["gates"]) == sum(b.gate_end - b.gate_begin for b in tcp["blocks"])
+
+
+def test_tc_epilogue_store_conflicts_brickwall():
+    """Bank conflicts of the epilogue's operand-plane stores (32 lanes = 16
+    output rows x re/im planes) for the n=16 brick wall: the block orders
+    keep them low."""
+    gl = templates.brickwall_gate_list(16, 12, 3)
+    c, entry, mats, n_eng = build_host(16, gl)
+    stats = []
+    emulate_forward(n_eng, entry, mats, stats)
+    print("epilogue store conflict ways per block:", stats)
+    assert stats and max(stats) <= 4
