@@ -596,8 +596,15 @@ int build_gate_program(int n, const std::vector<PGate>& gates, int L, int R,
 
 namespace {
 
-constexpr double kTcMsPerBlock = 1.5;     // tensor-core pass, per fused block
-constexpr double kRegMsPerDense2 = 0.2;   // register path, per 4x4 gate
+// Per-pass cost model (microseconds per pass over 2^26 amplitudes, fitted to
+// per-launch GB300 timings of brick-wall passes on both paths): a
+// tensor-core pass costs a fixed part (tile load, split, store) plus a
+// part per fused block; a register-path pass a fixed part plus a part per
+// dense gate of two or more qubits.
+constexpr double kTcBaseUs = 280.0;
+constexpr double kTcPerBlockUs = 135.0;
+constexpr double kRegBaseUs = 110.0;
+constexpr double kRegPerDense2Us = 47.0;
 
 // Fuse the gates of one pass (tile-bit masks tb, in application order) into
 // blocks of at most kTcBlockBits tile bits.  A gate may join the open block
@@ -855,11 +862,10 @@ void plan_tensor_passes(Program* P, const std::vector<PGate>& gates) {
     pd.block_end = (int)P->tc_blocks.size();
     P->tc_of_pass[ps] = (int)P->tc_passes.size();
     P->tc_passes.push_back(pd);
-    // cost model from GB300 timings at 2^28 amplitudes per pass: a fused
-    // block costs about kTcMsPerBlock, a 4x4 gate on the register path
-    // about kRegMsPerDense2 (both include their share of the pass's HBM
-    // traffic); the tensor path runs where it is estimated faster
-    P->tc_prefer.push_back(kTcMsPerBlock * (double)blocks.size() < kRegMsPerDense2 * (double)ndense2 ? 1 : 0);
+    // the tensor path runs where the cost model estimates it faster
+    const double t_tc = kTcBaseUs + kTcPerBlockUs * (double)blocks.size();
+    const double t_reg = kRegBaseUs + kRegPerDense2Us * (double)ndense2;
+    P->tc_prefer.push_back(t_tc < t_reg ? 1 : 0);
   }
 }
 
