@@ -21,9 +21,9 @@
 //     rescaled the same way before each block (per tile, from its largest
 //     component), so nothing overflows and the low halves stay normal.
 //
-// Data path per tile (persistent CTAs of 256 threads, two per SM): the tile
-// arrives by bulk copy while the previous tile computes and is written,
-// split, into the first block's operand planes (K-major canonical layout); per block one thread issues 24
+// Data path per tile (one CTA, 256 threads, three CTAs per SM): the tile is
+// read from HBM once and written, split, into the first block's operand
+// planes (K-major canonical layout); per block one thread issues 24
 // tcgen05.mma (M=128, N=64, K=16) into tensor memory and commits them to an
 // mbarrier, the fused matrix of the NEXT block streams in with one bulk TMA
 // copy (cp.async.bulk) while the epilogue reads D back (tcgen05.ld) and
@@ -51,15 +51,14 @@ namespace {
 constexpr int kTcThreads = 256;
 constexpr unsigned long long kTcWaitNs = 2000000000ull;  // 2 s per wait
 
-// shared-memory map of the pass kernel (bytes): two CTAs fit on an SM
-constexpr uint32_t kSmR = 0;                  // next tile as it arrives (natural order, 32 KiB)
-constexpr uint32_t kSmA = 32768;              // fused block: hi plane, lo plane (16 KiB each)
-constexpr uint32_t kSmB = 65536;              // operand planes, or the fp32 tile copy
+// shared-memory map of the pass kernel (bytes): three CTAs fit on an SM
+constexpr uint32_t kSmA = 0;                  // fused block: hi plane, lo plane (16 KiB each)
+constexpr uint32_t kSmB = 32768;              // operand planes, or the fp32 tile copy
 constexpr uint32_t kSmT = kSmB + kTcBRegion;  // epilogue address tables raddr[64], caddr[64]
 constexpr uint32_t kSmW = kSmT + 512;         // warp maxima [8]
-constexpr uint32_t kSmM = kSmW + 32;          // mbarriers: matrix copy, MMA completion, tile copy
-constexpr uint32_t kSmX = kSmM + 32;          // tensor-memory base and flags
-constexpr uint32_t kSmTotal = kSmX + 32;
+constexpr uint32_t kSmM = kSmW + 32;          // mbarriers: matrix copy, MMA completion
+constexpr uint32_t kSmX = kSmM + 16;          // tensor-memory base, abort flag, copy in flight
+constexpr uint32_t kSmTotal = kSmX + 16;
 
 // canonical K-major, no-swizzle layout of a 16-bit operand: core matrices of
 // 8 rows x 16 bytes (8 elements), rows 16 bytes apart; core matrices step
@@ -369,7 +368,6 @@ struct TcArgs {
   const uint8_t* fused;
   const float2* scales;
   int slots;
-  int64_t batch;
   unsigned int* err;
 };
 
@@ -400,267 +398,215 @@ __device__ __forceinline__ void put_pairs(uint8_t* pl, uint32_t R, const uint32_
 
 }  // namespace
 
-// One tensor-core pass, persistent: two CTAs per SM (97 KiB of shared
-// memory, 128 tensor-memory columns each) walk the tiles of all circuits of
-// the batch.  A tile is 4096 amplitudes; every fused block of the pass runs
-// on it between one read and one write of the tile in HBM.  While a tile's
-// blocks run, its successor streams into shared memory as 128 bulk copies of
-// its 256-byte runs, so the tile's HBM latency is hidden behind compute.
+// One tile of a tensor-core pass: 4096 amplitudes, every fused block of the
+// pass, one read and one write of the tile in HBM.  256 threads, three CTAs
+// per SM (66 KiB of shared memory, 128 tensor-memory columns each).
 //
 // Per block: one thread waits for the block's matrix (bulk copy), issues 12
 // MMAs (M=128, N=64, K=16) per plane into one fp32 accumulator -- the two
 // correction products first, the main product last, so the tensor core's
 // truncating accumulation touches the full-size value only four times -- and
-// commits them; every warp waits, thread 0 streams in the next matrix, and
-// the epilogue turns D into the next block's split operand planes directly:
-// Re/Im combination (one lane shuffle), the exact power-of-two rescale, fp16
-// hi/lo split, stores at raddr[i] ^ caddr[n] (two values per 32-bit word
-// where the next block's K bit 0 is one of this block's column bits).  The
-// scale for the next block comes from a bound (2 x max row sum of |F| x the
-// input's largest component), so no extra reduction pass is needed; the
-// exact largest output is reduced alongside for the block after.  The last
-// block writes fp32 values in natural order, which go back to HBM as one
-// coalesced store of the tile.
-__device__ __forceinline__ void issue_tile_copy(uint32_t raw, uint32_t bar, const float2* src, uint32_t base,
-                                                const uint32_t* runs, int lane) {
-  if (lane == 0) mbar_expect_tx(bar, 32768u);
-  __syncwarp();
-  for (int r = lane; r < 128; r += 32) bulk_g2s(raw + 256u * r, src + (base | __ldg(runs + r)), 256u, bar);
-}
-
-__global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) {
+// commits them; every warp waits, thread 0 streams in the next block's
+// matrix, and the epilogue turns D into the next block's split operand
+// planes directly: Re/Im combination (one lane shuffle), the exact
+// power-of-two rescale, fp16 hi/lo split, stores at raddr[i] ^ caddr[n]
+// (two values per 32-bit word where the next block's K bit 0 is one of this
+// block's column bits).  The scale for the next block comes from a bound
+// (2 x max row sum of |F| x the input's largest component), so no extra
+// reduction pass is needed; the exact largest output is reduced alongside
+// for the block after.  The last block writes fp32 values in natural order,
+// which go back to HBM as one coalesced store of the tile.
+__global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
   uint8_t* bp = smem + kSmB;
-  const uint8_t* raw = smem + kSmR;
   uint32_t* rtab = reinterpret_cast<uint32_t*>(smem + kSmT);
   uint32_t* ctab = rtab + 64;
   float* wmax = reinterpret_cast<float*>(smem + kSmW);
-  const uint32_t bar_mat = sbase + kSmM, bar_mma = sbase + kSmM + 8, bar_raw = sbase + kSmM + 16;
-  // sx[0] tensor-memory base, [1] abort, [2] matrix copy in flight,
-  // [3] tile copy in flight, [4] MMAs committed and not yet waited for
+  const uint32_t bar_mat = sbase + kSmM, bar_mma = sbase + kSmM + 8;
   volatile uint32_t* sx = reinterpret_cast<volatile uint32_t*>(smem + kSmX);
-  const int64_t total = (int64_t)a.ntiles * a.batch;
-  int64_t t = blockIdx.x;
-  if (t >= total) return;
 
-  auto base_of = [&](int64_t tt) {
-    const uint32_t tile = (uint32_t)(tt % a.ntiles);
-    uint32_t bs = 0;
-    for (uint32_t i = 0; i < a.nnonlocal; ++i)
-      if ((tile >> i) & 1u) bs |= 1u << a.nlbits[i];
-    return bs;
-  };
-  auto psi_of = [&](int64_t tt) { return a.psi + (tt / a.ntiles) * ((int64_t)1 << a.n); };
-  auto mat_of = [&](int64_t tt, int bi) {
-    return a.fused + ((tt / a.ntiles) * a.slots + a.blocks[bi].slot) * (int64_t)kTcMatBytes;
-  };
+  const uint32_t tile = blockIdx.x % a.ntiles;
+  const int64_t b = blockIdx.x / a.ntiles;
+  uint32_t base = 0;
+  for (uint32_t i = 0; i < a.nnonlocal; ++i)
+    if ((tile >> i) & 1u) base |= 1u << a.nlbits[i];
+  float2* psi = a.psi + b * ((int64_t)1 << a.n);
+  const uint8_t* fused_b = a.fused + b * a.slots * (int64_t)kTcMatBytes;
+  const float2* scales_b = a.scales + b * a.slots;
 
   if (warp == 0) tmem_alloc(sbase + kSmX, 128);
   if (tid == 0) {
     mbar_init(bar_mat, 1);
     mbar_init(bar_mma, 1);
-    mbar_init(bar_raw, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sx[1] = 0;
     sx[2] = 0;
-    sx[3] = 0;
-    sx[4] = 0;
   }
   fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = sx[0];
-  uint32_t ph_mat = 0, ph_mma = 0, ph_raw = 0;
-  if (warp == 0) {  // first tile and first block's matrix
-    if (lane == 0) sx[3] = 1;
-    issue_tile_copy(sbase + kSmR, bar_raw, psi_of(t), base_of(t), a.runs, lane);
-    if (lane == 0) {
-      sx[2] = 1;
-      mbar_expect_tx(bar_mat, kTcMatBytes);
-      bulk_g2s(sbase + kSmA, mat_of(t, 0), kTcMatBytes, bar_mat);
-    }
+  uint32_t ph_mat = 0, ph_mma = 0;
+  if (tid == 0) {  // first block's matrix
+    sx[2] = 1;
+    mbar_expect_tx(bar_mat, kTcMatBytes);
+    bulk_g2s(sbase + kSmA, fused_b + (int64_t)a.blocks[0].slot * kTcMatBytes, kTcMatBytes, bar_mat);
   }
-  const uint32_t idesc = make_idesc(128, 64);
-  bool abort = false;
 
-  for (; t < total; t += gridDim.x) {
-    const int64_t nxt = t + gridDim.x;
-    const uint32_t base = base_of(t);
-    float2* psi = psi_of(t);
-    const float2* scales_b = a.scales + (t / a.ntiles) * a.slots;
-    // ---- the tile, from shared memory: 8 float4 (16 amplitudes) per thread
-    uint32_t okr = 0;
-    if (lane == 0) okr = mbar_wait(bar_raw, ph_raw, kTcWaitNs) ? 1u : 0u;
-    okr = __shfl_sync(0xffffffffu, okr, 0);
-    float4 xv[8];
-    float lmax = 0.f;
-    if (!okr) {
-      sx[1] = 1;
-    } else {
+  // ---- the tile: 8 float4 (16 amplitudes) per thread, its largest component
+  float4 xv[8];
+  float lmax = 0.f;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        xv[u] = *reinterpret_cast<const float4*>(raw + 16u * (uint32_t)(tid + kTcThreads * u));
-        lmax = fmaxf(lmax, fmaxf(fmaxf(fabsf(xv[u].x), fabsf(xv[u].y)), fmaxf(fabsf(xv[u].z), fabsf(xv[u].w))));
+  for (int u = 0; u < 8; ++u) {
+    const uint32_t j = 2u * (uint32_t)(tid + kTcThreads * u);
+    const uint32_t off = __ldg(a.runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
+    xv[u] = __ldcg(reinterpret_cast<const float4*>(psi + (base | off)));
+    lmax = fmaxf(lmax, fmaxf(fmaxf(fabsf(xv[u].x), fabsf(xv[u].y)), fmaxf(fabsf(xv[u].z), fabsf(xv[u].w))));
+  }
+  lmax = warp_max(lmax);
+  if (lane == 0) wmax[warp] = lmax;
+  __syncthreads();
+  float max_in = wmax[0];
+  for (int w = 1; w < 8; ++w) max_in = fmaxf(max_in, wmax[w]);
+  float s_in, sinv_in;
+  pow2_scale(max_in, s_in, sinv_in);
+  // ---- first block's operand planes: the plane offset is linear in the
+  // tile offset 2 * (tid + 256 u) + e
+  {
+    uint32_t tb = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if ((tid >> k) & 1) tb ^= a.ldaddr[1 + k];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const uint32_t ad = tb ^ ((u & 1) ? a.ldaddr[9] : 0u) ^ ((u & 2) ? a.ldaddr[10] : 0u) ^
+                          ((u & 4) ? a.ldaddr[11] : 0u);
+      const float r0 = xv[u].x * s_in, i0 = xv[u].y * s_in, r1 = xv[u].z * s_in, i1 = xv[u].w * s_in;
+      if (a.ldpair) {
+        put2(bp + ad, r0, r1);
+        put2(bp + kTcPlaneIm + ad, i0, i1);
+      } else {
+        const uint32_t ad1 = ad ^ a.ldaddr[0];
+        put1(bp + ad, r0);
+        put1(bp + ad1, r1);
+        put1(bp + kTcPlaneIm + ad, i0);
+        put1(bp + kTcPlaneIm + ad1, i1);
       }
     }
-    lmax = warp_max(lmax);
-    if (lane == 0) wmax[warp] = lmax;
+  }
+
+  const uint32_t idesc = make_idesc(128, 64);
+  bool abort = false;
+  for (int bi = 0; bi < a.nblocks; ++bi) {
+    const TcBlock& blk = a.blocks[bi];
+    const bool last = bi + 1 == a.nblocks;
+    if (tid < 64) rtab[tid] = blk.raddr[tid];
+    else if (tid < 128) ctab[tid - 64] = blk.caddr[tid - 64];
+    const float2 sc = __ldg(scales_b + blk.slot);  // {1 / matrix scale, gain bound}
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    // ---- one thread: wait for the matrix, issue the MMAs, commit
+    if (tid == 0) {
+      tc_fence_after();
+      if (!mbar_wait(bar_mat, ph_mat, kTcWaitNs)) {
+        sx[1] = 1;  // nothing is committed: the waits below run out as well
+      } else {
+        ph_mat ^= 1;
+        sx[2] = 0;
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          const uint32_t d = tmem + 64u * p;
+          const uint32_t bh = sbase + kSmB + p * kTcPlaneIm, bl = bh + kTcPlaneLo;
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+            mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
+                    make_desc(bl + s * 2 * kLboB, kLboB, 128), idesc, s > 0);
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+            mma_f16(d, make_desc(sbase + kSmA + 16384 + s * 2 * kLboA, kLboA, 128),
+                    make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, 1);
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+            mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
+                    make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, 1);
+        }
+        mma_commit(bar_mma);
+      }
+    }
+    uint32_t ok = 0;
+    if (lane == 0) ok = mbar_wait(bar_mma, ph_mma, kTcWaitNs) ? 1u : 0u;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) {
+      sx[1] = 1;
+    } else {
+      if (tid == 0 && !last) {  // the tensor core is done with A: next matrix
+        sx[2] = 1;
+        mbar_expect_tx(bar_mat, kTcMatBytes);
+        bulk_g2s(sbase + kSmA, fused_b + (int64_t)a.blocks[bi + 1].slot * kTcMatBytes, kTcMatBytes, bar_mat);
+      }
+      tc_fence_after();
+      // ---- epilogue
+      float s_out = 1.f, sinv_out = 1.f;
+      if (!last) pow2_scale(2.f * sc.y * max_in, s_out, sinv_out);
+      const float f = s_out * sc.x * sinv_in;
+      const int q = warp & 3, hc = warp >> 2;
+      const int row = 32 * q + lane;
+      const uint32_t R = rtab[row >> 1];
+      uint8_t* pl = bp + ((row & 1) ? kTcPlaneIm : 0u);
+      const float sgn = (row & 1) ? 1.f : -1.f;
+      const int pb = blk.pairbit;
+      float m = 0.f;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int col0 = 32 * hc + 16 * half;
+        const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0;
+        float d0[16], d1[16], v[16];
+        tmem_ld16(ta, d0);
+        tmem_ld16(ta + 64u, d1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          v[c] = fmaf(sgn, __shfl_xor_sync(0xffffffffu, d1[c], 1), d0[c]) * f;
+          m = fmaxf(m, fabsf(v[c]));
+        }
+        const uint32_t* ct = ctab + col0;
+        if (last) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) *reinterpret_cast<float*>(pl + (R ^ ct[c])) = v[c];
+        } else {
+          switch (pb) {
+            case 0: put_pairs<0>(pl, R, ct, v); break;
+            case 1: put_pairs<1>(pl, R, ct, v); break;
+            case 2: put_pairs<2>(pl, R, ct, v); break;
+            case 3: put_pairs<3>(pl, R, ct, v); break;
+            default:
+#pragma unroll
+              for (int c = 0; c < 16; ++c) put1(pl + (R ^ ct[c]), v[c]);
+          }
+        }
+      }
+      m = warp_max(m);
+      if (lane == 0) wmax[warp] = m * sinv_out;
+      s_in = s_out;
+      sinv_in = sinv_out;
+    }
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
     if (sx[1]) {
       abort = true;
       break;
     }
-    ph_raw ^= 1;
-    if (warp == 0) {  // the buffer is free again: stream in the next tile
-      if (lane == 0) sx[3] = 0;
-      if (nxt < total) {
-        if (lane == 0) sx[3] = 1;
-        issue_tile_copy(sbase + kSmR, bar_raw, psi_of(nxt), base_of(nxt), a.runs, lane);
-      }
-    }
-    float max_in = wmax[0];
+    ph_mma ^= 1;
+    max_in = wmax[0];
     for (int w = 1; w < 8; ++w) max_in = fmaxf(max_in, wmax[w]);
-    float s_in, sinv_in;
-    pow2_scale(max_in, s_in, sinv_in);
-    // ---- first block's operand planes: the plane offset is linear in the
-    // tile offset 2 * (tid + 256 u) + e
-    {
-      uint32_t tb = 0;
-#pragma unroll
-      for (int k = 0; k < 8; ++k)
-        if ((tid >> k) & 1) tb ^= a.ldaddr[1 + k];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const uint32_t ad = tb ^ ((u & 1) ? a.ldaddr[9] : 0u) ^ ((u & 2) ? a.ldaddr[10] : 0u) ^
-                            ((u & 4) ? a.ldaddr[11] : 0u);
-        const float r0 = xv[u].x * s_in, i0 = xv[u].y * s_in, r1 = xv[u].z * s_in, i1 = xv[u].w * s_in;
-        if (a.ldpair) {
-          put2(bp + ad, r0, r1);
-          put2(bp + kTcPlaneIm + ad, i0, i1);
-        } else {
-          const uint32_t ad1 = ad ^ a.ldaddr[0];
-          put1(bp + ad, r0);
-          put1(bp + ad1, r1);
-          put1(bp + kTcPlaneIm + ad, i0);
-          put1(bp + kTcPlaneIm + ad1, i1);
-        }
-      }
-    }
+  }
 
-    for (int bi = 0; bi < a.nblocks; ++bi) {
-      const TcBlock& blk = a.blocks[bi];
-      const bool last = bi + 1 == a.nblocks;
-      if (tid < 64) rtab[tid] = blk.raddr[tid];
-      else if (tid < 128) ctab[tid - 64] = blk.caddr[tid - 64];
-      const float2 sc = __ldg(scales_b + blk.slot);  // {1 / matrix scale, gain bound}
-      fence_async_smem();
-      tc_fence_before();
-      __syncthreads();
-      // ---- one thread: wait for the matrix, issue the MMAs, commit
-      if (tid == 0) {
-        tc_fence_after();
-        if (!mbar_wait(bar_mat, ph_mat, kTcWaitNs)) {
-          sx[1] = 1;  // nothing is committed: the waits below run out as well
-        } else {
-          ph_mat ^= 1;
-          sx[2] = 0;
-#pragma unroll
-          for (int p = 0; p < 2; ++p) {
-            const uint32_t d = tmem + 64u * p;
-            const uint32_t bh = sbase + kSmB + p * kTcPlaneIm, bl = bh + kTcPlaneLo;
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-              mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
-                      make_desc(bl + s * 2 * kLboB, kLboB, 128), idesc, s > 0);
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-              mma_f16(d, make_desc(sbase + kSmA + 16384 + s * 2 * kLboA, kLboA, 128),
-                      make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, 1);
-#pragma unroll
-            for (int s = 0; s < 4; ++s)
-              mma_f16(d, make_desc(sbase + kSmA + s * 2 * kLboA, kLboA, 128),
-                      make_desc(bh + s * 2 * kLboB, kLboB, 128), idesc, 1);
-          }
-          mma_commit(bar_mma);
-          sx[4] = 1;
-        }
-      }
-      uint32_t ok = 0;
-      if (lane == 0) ok = mbar_wait(bar_mma, ph_mma, kTcWaitNs) ? 1u : 0u;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) {
-        sx[1] = 1;
-      } else {
-        // the tensor core is done with A: the next block's matrix, or the
-        // next tile's first one
-        if (tid == 0 && (!last || nxt < total)) {
-          sx[2] = 1;
-          mbar_expect_tx(bar_mat, kTcMatBytes);
-          bulk_g2s(sbase + kSmA, last ? mat_of(nxt, 0) : mat_of(t, bi + 1), kTcMatBytes, bar_mat);
-        }
-        tc_fence_after();
-        // ---- epilogue
-        float s_out = 1.f, sinv_out = 1.f;
-        if (!last) pow2_scale(2.f * sc.y * max_in, s_out, sinv_out);
-        const float f = s_out * sc.x * sinv_in;
-        const int q = warp & 3, hc = warp >> 2;
-        const int row = 32 * q + lane;
-        const uint32_t R = rtab[row >> 1];
-        uint8_t* pl = bp + ((row & 1) ? kTcPlaneIm : 0u);
-        const float sgn = (row & 1) ? 1.f : -1.f;
-        const int pb = blk.pairbit;
-        float m = 0.f;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          const int col0 = 32 * hc + 16 * half;
-          const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0;
-          float d0[16], d1[16], v[16];
-          tmem_ld16(ta, d0);
-          tmem_ld16(ta + 64u, d1);
-          tmem_wait_ld();
-#pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            v[c] = fmaf(sgn, __shfl_xor_sync(0xffffffffu, d1[c], 1), d0[c]) * f;
-            m = fmaxf(m, fabsf(v[c]));
-          }
-          const uint32_t* ct = ctab + col0;
-          if (last) {
-#pragma unroll
-            for (int c = 0; c < 16; ++c) *reinterpret_cast<float*>(pl + (R ^ ct[c])) = v[c];
-          } else {
-            switch (pb) {
-              case 0: put_pairs<0>(pl, R, ct, v); break;
-              case 1: put_pairs<1>(pl, R, ct, v); break;
-              case 2: put_pairs<2>(pl, R, ct, v); break;
-              case 3: put_pairs<3>(pl, R, ct, v); break;
-              default:
-#pragma unroll
-                for (int c = 0; c < 16; ++c) put1(pl + (R ^ ct[c]), v[c]);
-            }
-          }
-        }
-        m = warp_max(m);
-        if (lane == 0) wmax[warp] = m * sinv_out;
-        s_in = s_out;
-        sinv_in = sinv_out;
-      }
-      fence_async_smem();
-      tc_fence_before();
-      __syncthreads();
-      if (sx[1]) {
-        abort = true;
-        break;
-      }
-      if (tid == 0) sx[4] = 0;
-      ph_mma ^= 1;
-      max_in = wmax[0];
-      for (int w = 1; w < 8; ++w) max_in = fmaxf(max_in, wmax[w]);
-    }
-    if (abort) break;
-    // ---- the tile back to HBM
+  if (!abort) {
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const uint32_t j = 2u * (uint32_t)(tid + kTcThreads * u);
@@ -672,15 +618,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) 
                                    *reinterpret_cast<const float*>(bp + kTcPlaneIm + w1));
       *reinterpret_cast<float4*>(psi + (base | off)) = o;
     }
-    __syncthreads();  // the next tile's operand planes overwrite this copy
-  }
-
-  if (abort) {
+  } else {
     if (tid == 0) atomicExch(a.err, 1u);
     // let the copies and MMAs this CTA issued finish before its memory goes away
-    if (sx[3]) mbar_wait(bar_raw, ph_raw, kTcWaitNs);
     if (sx[2]) mbar_wait(bar_mat, ph_mat, kTcWaitNs);
-    if (sx[4]) mbar_wait(bar_mma, ph_mma, kTcWaitNs);
+    mbar_wait(bar_mma, ph_mma, kTcWaitNs);
   }
   tc_fence_before();
   __syncthreads();
@@ -772,7 +714,7 @@ cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const ui
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTotal);
     if (e != cudaSuccess) return e;
-    // the largest shared-memory carveout, so that two CTAs fit on an SM
+    // the largest shared-memory carveout, so that three CTAs fit on an SM
     e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     attr_set = true;
@@ -792,19 +734,7 @@ cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const ui
   a.scales = scales;
   a.slots = slots;
   a.err = err;
-  a.batch = batch;
-  // persistent: two CTAs per SM walk the tiles
-  static int sms[64] = {0};
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!sms[dev]) {
-    e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-  }
-  const int64_t total = (int64_t)a.ntiles * batch;
-  const int64_t grid = total < 2 * (int64_t)sms[dev] ? total : 2 * (int64_t)sms[dev];
+  const int64_t grid = (int64_t)a.ntiles * batch;
   tc_pass_kernel<<<(unsigned)grid, kTcThreads, kSmTotal, st>>>(a);
   count_launch();
   return cudaGetLastError();
