@@ -8,7 +8,9 @@ through ``backend.vvag`` -- the reference's batched VQE step.  Synthetic
 inputs; states are complex64.  On one GPU the default run also times the
 large-circuit gate-application workload (n=28 Haar brick wall of depth 20,
 <Z0 Z27>, <X13>, 2^20 samples) and reports it under "brickwall_n28" in the
-same line, with its own forward-pass roofline, CPU baseline and e2e figure.
+same line, with its own forward-pass roofline, CPU baseline and e2e figure,
+and the uneven batch (512 QAOA MaxCut circuits, n 12..24, one persistent
+launch per sweep) under "qaoa_uneven_512".
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -371,6 +373,13 @@ def run_gb300_arm(args, rank, world):
         line["brickwall_n28"] = {k: bw[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup",
                                                     "config", "roofline", "cpu_baseline", "e2e", "clocks",
                                                     "gpu_launches", "gpu_launches_per_step")}
+    if world == 1 and not args.no_qaoa:
+        # the uneven batch: 512 QAOA circuits in one persistent launch per sweep
+        qb = measure_qaoa(args, rank, world, nested=True)
+        qb["roofline"].pop("sweeps", None)
+        line["qaoa_uneven_512"] = {k: qb[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup",
+                                                      "config", "roofline", "cpu_baseline", "e2e", "clocks",
+                                                      "gpu_launches", "gpu_launches_per_step")}
     print(json.dumps(line), flush=True)
 
 
@@ -599,10 +608,18 @@ def per_circuit_loop(specs, params, sample=24):
 
 
 def run_qaoa(args, rank, world):
+    line = measure_qaoa(args, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def measure_qaoa(args, rank, world, nested=False):
     """Uneven batch: 512 QAOA MaxCut circuits (n ~ U{12,..,24} even, random
     3-regular graphs, p ~ U{1..6}, gamma, beta ~ U[0, pi), seed 5), energy
     and adjoint gradient of every circuit per step, one persistent launch per
-    sweep replayed from a CUDA graph, tile width autotuned."""
+    sweep replayed from a CUDA graph, tile width autotuned.  Returns the JSON
+    line (rank 0) or None; ``nested`` (inside the default run) leaves out the
+    per-circuit comparison loop."""
     import torch
 
     import tensorcircuit_gb300 as tc
@@ -668,7 +685,7 @@ def run_qaoa(args, rank, world):
     if rank != 0:
         return
     cpu = None if args.no_cpu else cpu_qaoa(specs, params)
-    loop = per_circuit_loop(specs, params)
+    loop = None if nested else per_circuit_loop(specs, params)
     ns = [s[0] for s in specs]
     line = {
         "metric": QB_METRIC, "value": QB_COUNT / (ms / 1e3), "unit": QB_UNIT, "n_gpus": world,
@@ -694,7 +711,7 @@ def run_qaoa(args, rank, world):
         "gpu_launches": int(launches_per_step * args.steps),
         "gpu_launches_per_step": int(launches_per_step),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 MC_N, MC_LAYERS, MC_GAMMA, MC_SEED = 10, 4, 0.15, 7
@@ -1046,6 +1063,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-brickwall", action="store_true",
                     help="default workload: skip the nested n=28 brick-wall measurement")
+    ap.add_argument("--no-qaoa", action="store_true",
+                    help="default workload: skip the nested 512-circuit uneven-batch measurement")
     args = ap.parse_args()
     BATCH = args.batch
     BW_N = args.bw_qubits
