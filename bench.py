@@ -516,11 +516,13 @@ def measure_brickwall(args, rank, world):
         "metric": BW_METRIC, "value": len(gl) / (ms / 1e3), "unit": BW_UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": {"workload": BW_WORKLOAD, "n_qubits": n, "depth": BW_DEPTH, "gates": len(gl),
+        "config": {"workload": BW_WORKLOAD if n == 28 else "brickwall_n%d_d20_haar" % n, "n_qubits": n, "depth": BW_DEPTH, "gates": len(gl),
                    "shots": BW_SHOTS, "seed": BW_SEED, "uniform_seed": BW_USEED,
                    "l2": "no flush: the 2 GiB state exceeds the 129 MB L2",
                    "fwd_passes": plan.npasses, "zz_0_27": float(zz.real), "x_13": float(x13.real)},
-        "roofline": {"bound": "hbm", "kernel": "forward pass (tcg_forward, one launch per pass)",
+        "roofline": {"bound": "hbm", "kernel": "forward pass (tcg_forward, one launch per pass: %d of %d passes "
+                                               "on tc_pass_kernel, fused blocks on the tensor cores)" %
+                                               (plan.tensor_passes(), plan.npasses),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": _traffic("brickwall_fwd_bytes_per_launch", n == 28),
                      "alg_bytes_per_launch": 16.0 * N,
