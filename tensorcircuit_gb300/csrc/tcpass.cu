@@ -48,15 +48,17 @@ namespace tcg {
 
 namespace {
 
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 512;
+constexpr int kTcWarps = kTcThreads / 32;
+constexpr int kTcLdIter = 4096 / (2 * kTcThreads);  // float4 loads per thread
 constexpr unsigned long long kTcWaitNs = 2000000000ull;  // 2 s per wait
 
 // shared-memory map of the pass kernel (bytes): three CTAs fit on an SM
 constexpr uint32_t kSmA = 0;                  // fused block: hi plane, lo plane (16 KiB each)
 constexpr uint32_t kSmB = 32768;              // operand planes, or the fp32 tile copy
 constexpr uint32_t kSmT = kSmB + kTcBRegion;  // epilogue address tables raddr[64], caddr[64]
-constexpr uint32_t kSmW = kSmT + 512;         // warp maxima [8]
-constexpr uint32_t kSmM = kSmW + 32;          // mbarriers: matrix copy, MMA completion
+constexpr uint32_t kSmW = kSmT + 512;         // warp maxima [kTcWarps]
+constexpr uint32_t kSmM = kSmW + 64;          // mbarriers: matrix copy, MMA completion
 constexpr uint32_t kSmX = kSmM + 16;          // tensor-memory base, abort flag, copy in flight
 constexpr uint32_t kSmTotal = kSmX + 16;
 
@@ -416,7 +418,7 @@ __device__ __forceinline__ void put_pairs(uint8_t* pl, uint32_t R, const uint32_
 // reduction pass is needed; the exact largest output is reduced alongside
 // for the block after.  The last block writes fp32 values in natural order,
 // which go back to HBM as one coalesced store of the tile.
-__global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) {
+__global__ void __launch_bounds__(kTcThreads, 2) tc_pass_kernel(const TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
@@ -456,11 +458,11 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
     bulk_g2s(sbase + kSmA, fused_b + (int64_t)a.blocks[0].slot * kTcMatBytes, kTcMatBytes, bar_mat);
   }
 
-  // ---- the tile: 8 float4 (16 amplitudes) per thread, its largest component
-  float4 xv[8];
+  // ---- the tile: kTcLdIter float4 (2 amplitudes each) per thread, its largest component
+  float4 xv[kTcLdIter];
   float lmax = 0.f;
 #pragma unroll
-  for (int u = 0; u < 8; ++u) {
+  for (int u = 0; u < kTcLdIter; ++u) {
     const uint32_t j = 2u * (uint32_t)(tid + kTcThreads * u);
     const uint32_t off = __ldg(a.runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
     xv[u] = __ldcg(reinterpret_cast<const float4*>(psi + (base | off)));
@@ -470,20 +472,23 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
   if (lane == 0) wmax[warp] = lmax;
   __syncthreads();
   float max_in = wmax[0];
-  for (int w = 1; w < 8; ++w) max_in = fmaxf(max_in, wmax[w]);
+  for (int w = 1; w < kTcWarps; ++w) max_in = fmaxf(max_in, wmax[w]);
   float s_in, sinv_in;
   pow2_scale(max_in, s_in, sinv_in);
   // ---- first block's operand planes: the plane offset is linear in the
-  // tile offset 2 * (tid + 256 u) + e
+  // tile offset 2 * (tid + kTcThreads u) + e
   {
+    constexpr int kTidBits = kTcThreads == 512 ? 9 : 8;
     uint32_t tb = 0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < kTidBits; ++k)
       if ((tid >> k) & 1) tb ^= a.ldaddr[1 + k];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const uint32_t ad = tb ^ ((u & 1) ? a.ldaddr[9] : 0u) ^ ((u & 2) ? a.ldaddr[10] : 0u) ^
-                          ((u & 4) ? a.ldaddr[11] : 0u);
+    for (int u = 0; u < kTcLdIter; ++u) {
+      uint32_t ad = tb;
+#pragma unroll
+      for (int k = 0; k < 11 - kTidBits; ++k)
+        if ((u >> k) & 1) ad ^= a.ldaddr[1 + kTidBits + k];
       const float r0 = xv[u].x * s_in, i0 = xv[u].y * s_in, r1 = xv[u].z * s_in, i1 = xv[u].w * s_in;
       if (a.ldpair) {
         put2(bp + ad, r0, r1);
@@ -553,6 +558,9 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
       float s_out = 1.f, sinv_out = 1.f;
       if (!last) pow2_scale(2.f * sc.y * max_in, s_out, sinv_out);
       const float f = s_out * sc.x * sinv_in;
+      // warp w reads tensor-memory lanes 32 (w % 4) ..; the 64 columns are
+      // shared by the kTcWarps / 4 warps of each lane quarter
+      constexpr int kCols = 64 / (kTcWarps / 4);
       const int q = warp & 3, hc = warp >> 2;
       const int row = 32 * q + lane;
       const uint32_t R = rtab[row >> 1];
@@ -561,8 +569,8 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
       const int pb = blk.pairbit;
       float m = 0.f;
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const int col0 = 32 * hc + 16 * half;
+      for (int half = 0; half < kCols / 16; ++half) {
+        const int col0 = kCols * hc + 16 * half;
         const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0;
         float d0[16], d1[16], v[16];
         tmem_ld16(ta, d0);
@@ -603,12 +611,12 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
     }
     ph_mma ^= 1;
     max_in = wmax[0];
-    for (int w = 1; w < 8; ++w) max_in = fmaxf(max_in, wmax[w]);
+    for (int w = 1; w < kTcWarps; ++w) max_in = fmaxf(max_in, wmax[w]);
   }
 
   if (!abort) {
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < kTcLdIter; ++u) {
       const uint32_t j = 2u * (uint32_t)(tid + kTcThreads * u);
       const uint32_t off = __ldg(a.runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
       const uint32_t w0 = swz(j) * 4u, w1 = swz(j + 1) * 4u;

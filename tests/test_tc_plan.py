@@ -81,9 +81,11 @@ def emulate_tc_pass(psi, P, desc, blocks, gates, mats, n, stats=None):
         bb = [blk.bbits[i] for i in range(6)]
         cb = [blk.cbits[i] for i in range(6)]
         assert sorted(bb + cb) == list(range(12)), "block + column bits must partition the tile"
-    tid = np.arange(256)
-    tb = np.zeros(256, np.int64)
-    for k in range(8):
+    NT = 512  # threads per CTA of the pass kernel: tile offset 2 * (tid + NT u) + e
+    tid_bits = NT.bit_length() - 1
+    tid = np.arange(NT)
+    tb = np.zeros(NT, np.int64)
+    for k in range(tid_bits):
         tb ^= np.where((tid >> k) & 1, ld[1 + k], 0)
     for tile in range(1 << (n - P.L)):
         base = int(dep(tile, nl))
@@ -94,10 +96,13 @@ def emulate_tc_pass(psi, P, desc, blocks, gates, mats, n, stats=None):
             assert 0 <= off and off + 2 <= 32832 and (off % 2) == 0
             mem[int(off)] = v
 
-        for u in range(8):
-            ad = tb ^ (ld[9] if u & 1 else 0) ^ (ld[10] if u & 2 else 0) ^ (ld[11] if u & 4 else 0)
-            j = 2 * (tid + 256 * u)
-            for t in range(256):
+        for u in range(4096 // (2 * NT)):
+            ad = tb.copy()
+            for k in range(11 - tid_bits):
+                if (u >> k) & 1:
+                    ad ^= ld[1 + tid_bits + k]
+            j = 2 * (tid + NT * u)
+            for t in range(NT):
                 x0, x1 = T[j[t]], T[j[t] + 1]
                 a0 = int(ad[t])
                 a1 = a0 + 2 if desc.ldpair else a0 ^ ld[0]
@@ -143,7 +148,7 @@ def emulate_tc_pass(psi, P, desc, blocks, gates, mats, n, stats=None):
                 # 4-byte-word banks of one store instruction: 32 lanes = 16 rows x re/im
                 worst = 1
                 for q in range(4):
-                    for col in range(0, 64, 1 if pb < 0 else 2):
+                    for col in range(0, 64):
                         banks = {}
                         for lane in range(32):
                             row = 32 * q + lane
