@@ -81,7 +81,7 @@ def emulate_tc_pass(psi, P, desc, blocks, gates, mats, n, stats=None):
         bb = [blk.bbits[i] for i in range(6)]
         cb = [blk.cbits[i] for i in range(6)]
         assert sorted(bb + cb) == list(range(12)), "block + column bits must partition the tile"
-    NT = 512  # threads per CTA of the pass kernel: tile offset 2 * (tid + NT u) + e
+    NT = 256  # threads per CTA of the pass kernel: tile offset 2 * (tid + NT u) + e
     tid_bits = NT.bit_length() - 1
     tid = np.arange(NT)
     tb = np.zeros(NT, np.int64)
