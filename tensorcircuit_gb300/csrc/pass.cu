@@ -1023,7 +1023,8 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 constexpr unsigned long long kBatchWaitNs = 2000000000ull;  // default dependency-wait limit
 
 template <int MODE, int R, bool LITE>
-__global__ void __launch_bounds__(256, LITE ? 2 : 1) batch_kernel(BatchLaunch BL) {
+__global__ void __launch_bounds__(256, LITE ? ((MODE == MODE_FWD || MODE == MODE_PACC) ? 3 : 2) : 1)
+    batch_kernel(BatchLaunch BL) {
   extern __shared__ __align__(16) float2 smem_raw[];
   __shared__ long long s_item;
   __shared__ int s_seg;
