@@ -375,27 +375,33 @@ struct TcArgs {
 
 namespace {
 
-// v = hi + lo, both fp16, at plane byte offset p (lo plane kTcPlaneLo further)
-__device__ __forceinline__ void put1(uint8_t* p, float v) {
-  const __half h = __float2half_rn(v);
-  const __half l = __float2half_rn(v - __half2float(h));
-  *reinterpret_cast<__half*>(p) = h;
-  *reinterpret_cast<__half*>(p + kTcPlaneLo) = l;
+// v = hi + lo, both fp16, at shared address a (the lo plane kTcPlaneLo further);
+// put2s: two values that share one 32-bit word (v0 at the lower address)
+__device__ __forceinline__ void st_sh32(uint32_t a, uint32_t v) {
+  asm volatile("st.shared.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
-// two values that share one 32-bit word (v0 at the lower address)
-__device__ __forceinline__ void put2(uint8_t* p, float v0, float v1) {
+__device__ __forceinline__ void st_sh16(uint32_t a, unsigned short v) {
+  asm volatile("st.shared.b16 [%0], %1;" ::"r"(a), "h"(v) : "memory");
+}
+__device__ __forceinline__ void put2s(uint32_t a, float v0, float v1) {
   const __half2 hh = __floats2half2_rn(v0, v1);
   const float2 hf = __half22float2(hh);
   const __half2 ll = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
-  *reinterpret_cast<__half2*>(p) = hh;
-  *reinterpret_cast<__half2*>(p + kTcPlaneLo) = ll;
+  st_sh32(a, *reinterpret_cast<const uint32_t*>(&hh));
+  st_sh32(a + kTcPlaneLo, *reinterpret_cast<const uint32_t*>(&ll));
+}
+__device__ __forceinline__ void put1s(uint32_t a, float v) {
+  const __half h = __float2half_rn(v);
+  const __half l = __float2half_rn(v - __half2float(h));
+  st_sh16(a, __half_as_ushort(h));
+  st_sh16(a + kTcPlaneLo, __half_as_ushort(l));
 }
 
 template <int P>
-__device__ __forceinline__ void put_pairs(uint8_t* pl, uint32_t R, const uint32_t* ct, const float (&v)[16]) {
+__device__ __forceinline__ void put_pairs(uint32_t pl, uint32_t R, const uint32_t (&ct)[16], const float (&v)[16]) {
 #pragma unroll
   for (int c = 0; c < 16; ++c)
-    if (!((c >> P) & 1)) put2(pl + (R ^ ct[c]), v[c], v[c | (1 << P)]);
+    if (!((c >> P) & 1)) put2s(pl + (R ^ ct[c]), v[c], v[c | (1 << P)]);
 }
 
 }  // namespace
@@ -490,15 +496,16 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
       for (int k = 0; k < 11 - kTidBits; ++k)
         if ((u >> k) & 1) ad ^= a.ldaddr[1 + kTidBits + k];
       const float r0 = xv[u].x * s_in, i0 = xv[u].y * s_in, r1 = xv[u].z * s_in, i1 = xv[u].w * s_in;
+      const uint32_t pb0 = sbase + kSmB;
       if (a.ldpair) {
-        put2(bp + ad, r0, r1);
-        put2(bp + kTcPlaneIm + ad, i0, i1);
+        put2s(pb0 + ad, r0, r1);
+        put2s(pb0 + kTcPlaneIm + ad, i0, i1);
       } else {
         const uint32_t ad1 = ad ^ a.ldaddr[0];
-        put1(bp + ad, r0);
-        put1(bp + ad1, r1);
-        put1(bp + kTcPlaneIm + ad, i0);
-        put1(bp + kTcPlaneIm + ad1, i1);
+        put1s(pb0 + ad, r0);
+        put1s(pb0 + ad1, r1);
+        put1s(pb0 + kTcPlaneIm + ad, i0);
+        put1s(pb0 + kTcPlaneIm + ad1, i1);
       }
     }
   }
@@ -564,7 +571,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
       const int q = warp & 3, hc = warp >> 2;
       const int row = 32 * q + lane;
       const uint32_t R = rtab[row >> 1];
-      uint8_t* pl = bp + ((row & 1) ? kTcPlaneIm : 0u);
+      const uint32_t pl = sbase + kSmB + ((row & 1) ? kTcPlaneIm : 0u);
       const float sgn = (row & 1) ? 1.f : -1.f;
       const int pb = blk.pairbit;
       float m = 0.f;
@@ -581,10 +588,18 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
           v[c] = fmaf(sgn, __shfl_xor_sync(0xffffffffu, d1[c], 1), d0[c]) * f;
           m = fmaxf(m, fabsf(v[c]));
         }
-        const uint32_t* ct = ctab + col0;
+        uint32_t ct[16];
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const uint4 c4 = *reinterpret_cast<const uint4*>(ctab + col0 + 4 * g);
+          ct[4 * g] = c4.x;
+          ct[4 * g + 1] = c4.y;
+          ct[4 * g + 2] = c4.z;
+          ct[4 * g + 3] = c4.w;
+        }
         if (last) {
 #pragma unroll
-          for (int c = 0; c < 16; ++c) *reinterpret_cast<float*>(pl + (R ^ ct[c])) = v[c];
+          for (int c = 0; c < 16; ++c) st_sh32(pl + (R ^ ct[c]), __float_as_uint(v[c]));
         } else {
           switch (pb) {
             case 0: put_pairs<0>(pl, R, ct, v); break;
@@ -593,7 +608,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
             case 3: put_pairs<3>(pl, R, ct, v); break;
             default:
 #pragma unroll
-              for (int c = 0; c < 16; ++c) put1(pl + (R ^ ct[c]), v[c]);
+              for (int c = 0; c < 16; ++c) put1s(pl + (R ^ ct[c]), v[c]);
           }
         }
       }
