@@ -105,12 +105,15 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+// One poll; a thread whose phase is not complete yet is suspended for up to
+// the hint (or until the phase completes), so waiting warps do not take issue
+// slots from the warps of the other CTAs on the SM.
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t phase) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(ok)
-      : "r"(bar), "r"(phase)
+      : "r"(bar), "r"(phase), "r"(20000u)
       : "memory");
   return ok != 0;
 }
