@@ -347,6 +347,97 @@ __device__ __forceinline__ float prot_dot(const float2 (&v)[1 << R], const float
 
 #define TCG_X16(M) M(0) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11) M(12) M(13) M(14) M(15)
 
+// Shear form of the same rotation (a rotation by (c, s) as three in-place
+// shears x -= k y, y += t x, x -= k y with k = s / (1 + c): three FMAs per
+// component pair instead of four operations per amplitude).  A rotation with
+// c < 0 is taken as the negative of its c >= 0 partner; gshear_params
+// returns 1 then, and the tile carries the sign until it is stored.
+__device__ __forceinline__ uint32_t gshear_params(float c, float q, float& k, float& t) {
+  const uint32_t neg = c < 0.f ? 1u : 0u;
+  t = neg ? -q : q;
+  k = t * __frcp_rn(1.f + fabsf(c));
+  return neg;
+}
+template <int STEP>
+__device__ __forceinline__ void gshear_step(float& x, float& y, float k, float t, bool flip) {
+  if (STEP == 1) y = fmaf(flip ? -t : t, x, y);
+  else x = fmaf(flip ? k : -k, y, x);
+}
+// one of the three shear sweeps over every register pair of the rotation
+template <int R, int X, bool QIM, int STEP>
+__device__ __forceinline__ void gshear_sweep(float2 (&v)[1 << R], float k, float t, int zr) {
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    const bool sr = (__popc(r & zr) & 1) != 0;
+    if (X == 0) {
+      gshear_step<STEP>(v[r].x, v[r].y, k, t, sr);
+    } else {
+      const int r2 = r ^ X;
+      if (r2 < r) continue;
+      if (QIM) {
+        gshear_step<STEP>(v[r].x, v[r2].y, k, t, sr);
+        gshear_step<STEP>(v[r].y, v[r2].x, k, t, !sr);
+      } else {
+        gshear_step<STEP>(v[r].x, v[r2].x, k, t, !sr);
+        gshear_step<STEP>(v[r].y, v[r2].y, k, t, !sr);
+      }
+    }
+  }
+}
+template <int R, int X, bool QIM>
+__device__ __forceinline__ void gshear_rot(float2 (&v)[1 << R], float k, float t, int zr) {
+  gshear_sweep<R, X, QIM, 0>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, 1>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, 2>(v, k, t, zr);
+}
+// psi and mu together: the sweeps interleaved for independent FMAs
+template <int R, int X, bool QIM>
+__device__ __forceinline__ void gshear_rot2(float2 (&v)[1 << R], float2 (&w)[1 << R], float k, float t, int zr) {
+  gshear_sweep<R, X, QIM, 0>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, 0>(w, k, t, zr);
+  gshear_sweep<R, X, QIM, 1>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, 1>(w, k, t, zr);
+  gshear_sweep<R, X, QIM, 2>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, 2>(w, k, t, zr);
+}
+template <int R>
+__device__ __forceinline__ void dispatch_gshear(int x, bool qim, float2 (&v)[1 << R], float k, float t, int zr) {
+  if (qim) {
+#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot<R, ((XX) < (1 << R) ? (XX) : 0), true>(v, k, t, zr); break;
+    switch (x) {
+      TCG_X16(TCG_GS)
+      default: break;
+    }
+#undef TCG_GS
+  } else {
+#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot<R, ((XX) < (1 << R) ? (XX) : 0), false>(v, k, t, zr); break;
+    switch (x) {
+      TCG_X16(TCG_GS)
+      default: break;
+    }
+#undef TCG_GS
+  }
+}
+template <int R>
+__device__ __forceinline__ void dispatch_gshear2(int x, bool qim, float2 (&v)[1 << R], float2 (&w)[1 << R], float k,
+                                                 float t, int zr) {
+  if (qim) {
+#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot2<R, ((XX) < (1 << R) ? (XX) : 0), true>(v, w, k, t, zr); break;
+    switch (x) {
+      TCG_X16(TCG_GS)
+      default: break;
+    }
+#undef TCG_GS
+  } else {
+#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot2<R, ((XX) < (1 << R) ? (XX) : 0), false>(v, w, k, t, zr); break;
+    switch (x) {
+      TCG_X16(TCG_GS)
+      default: break;
+    }
+#undef TCG_GS
+  }
+}
+
 template <int R>
 __device__ __forceinline__ void dispatch_prot(int x, float2 (&v)[1 << R], float c, float qv, int zr, bool qim) {
   if (qim) {
@@ -654,6 +745,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
 
   float2 v[NR];
   float2 w[NR];  // mu registers; dead (and removed) in modes without mu
+  uint32_t pneg = 0;  // the tile holds the negative of its true values
   bool live = false;     // registers hold the tile
   bool in_smem = false;  // smem holds the tile
   int prev = -1;
@@ -853,7 +945,9 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
         float qv = (ny <= 1) ? -cs.y : cs.y;
         if (sg) qv = -qv;
         if (MODE == MODE_FWD) {
-          dispatch_prot<R>(op.xreg, v, cs.x, qv, zr, qim);
+          float k, t;
+          pneg ^= gshear_params(cs.x, qv, k, t);
+          dispatch_gshear<R>(op.xreg, qim, v, k, t, zr);
         } else if (MODE == MODE_BWD) {
           if (op.slot >= 0) {
             // g = Im(pt z), pt = (+-)(-i)^nY: z.y, -z.x, -z.y, z.x for nY % 4 = 0..3
@@ -863,8 +957,9 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
             const float t = warp_sum1(g, nl);
             if (lane == 0) sm_slot[warp * A.max_slots + op.slot] = make_float2(t, 0.f);
           }
-          dispatch_prot<R>(op.xreg, v, cs.x, -qv, zr, qim);
-          dispatch_prot<R>(op.xreg, w, cs.x, -qv, zr, qim);
+          float k, t;
+          pneg ^= gshear_params(cs.x, -qv, k, t);
+          dispatch_gshear2<R>(op.xreg, qim, v, w, k, t, zr);
         }
       } else if (kind == OP_ZRUN) {
         if (MODE == MODE_MEAS) {
@@ -972,7 +1067,24 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
     prev = s;
   }
 
-  // ---- write the tile back
+  // ---- write the tile back (with the sign the shear rotations left pending;
+  // it is the same for every thread of the tile)
+  if ((MODE == MODE_FWD || MODE == MODE_BWD) && pneg) {
+    if (live) {
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        v[r] = make_float2(-v[r].x, -v[r].y);
+        if (HAS_MU) w[r] = make_float2(-w[r].x, -w[r].y);
+      }
+    } else if (in_smem) {
+      __syncthreads();
+      for (uint32_t j = tid; j < (1u << L); j += nthreads) {
+        sm_psi[j] = make_float2(-sm_psi[j].x, -sm_psi[j].y);
+        if (HAS_MU) sm_mu[j] = make_float2(-sm_mu[j].x, -sm_mu[j].y);
+      }
+      __syncthreads();
+    }
+  }
   if (STORE_PSI || STORE_MU) {
     if (live) {
       const DevStage& S = A.prog.stages[prev];
@@ -1020,7 +1132,6 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 // running, so waits end; the limit only guards against a broken schedule.
 // After a time-out every later wait is skipped (results are then invalid and
 // the error flag says so) so the launch still finishes.
-constexpr unsigned long long kBatchWaitNs = 2000000000ull;  // default dependency-wait limit
 
 template <int MODE, int R, bool LITE>
 __global__ void __launch_bounds__(256, LITE ? ((MODE == MODE_FWD || MODE == MODE_PACC) ? 3 : 2) : 1)
