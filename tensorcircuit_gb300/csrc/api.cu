@@ -5,6 +5,8 @@
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -106,30 +108,76 @@ bool tc_use_pass(const Program* P, int ps) {
   return pol == 1 || (pol == 2 && P->tc_prefer[t]);
 }
 
-// Per-device buffer of one forward call's fused matrices: [0, 256) error
-// flag, then batch * slots blocks of kTcMatBytes, then batch * slots
-// {1 / matrix scale, gain bound} pairs.
-int tc_scratch(Program* P, int64_t batch, unsigned int** err, uint8_t** fused, float2** scales) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
-  const size_t nmat = size_t(batch) * size_t(P->tc_slots);
-  const size_t need = 256 + nmat * kTcMatBytes + nmat * sizeof(float2) + 256;
-  std::lock_guard<std::mutex> lk(P->mu);
-  Program::TcScratch& ts = P->tc_scratch[dev];
-  if (ts.bytes < need) {
-    if (ts.base) cudaFree(ts.base);
-    ts.base = nullptr;
-    ts.bytes = 0;
-    if (cudaMalloc(&ts.base, need) != cudaSuccess) return TCG_ERR_OOM;
-    if (cudaMemset(ts.base, 0, 256) != cudaSuccess) return TCG_ERR_CUDA;
-    ts.bytes = need;
+// Fused block matrices of one forward call (batch * slots blocks of
+// kTcMatBytes, then batch * slots {1 / matrix scale, gain bound} pairs): a
+// stream-ordered allocation on the call's stream, freed in stream order after
+// the call's last pass, so that calls on different streams or threads never
+// share one.  Outside stream capture it comes from a library pool per device
+// that keeps up to kTcPoolKeep bytes between calls; under capture
+// cudaMallocAsync / cudaFreeAsync become memory nodes of the graph.
+constexpr uint64_t kTcPoolKeep = uint64_t(1) << 30;
+
+int tc_pool(int dev, cudaMemPool_t* out) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) {
+    *out = it->second;
+    return TCG_OK;
   }
-  char* b = static_cast<char*>(ts.base);
-  *err = reinterpret_cast<unsigned int*>(b);
-  *fused = reinterpret_cast<uint8_t*>(b + 256);
-  *scales = reinterpret_cast<float2*>(b + 256 + nmat * kTcMatBytes);
+  cudaMemPoolProps props;
+  std::memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return TCG_ERR_CUDA;
+  }
+  uint64_t keep = kTcPoolKeep;
+  (void)cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  pools[dev] = pool;
+  *out = pool;
   return TCG_OK;
 }
+
+int tc_alloc(int64_t batch, int slots, cudaStream_t st, void** out) {
+  const size_t nmat = size_t(batch) * size_t(slots);
+  const size_t bytes = nmat * (size_t(kTcMatBytes) + sizeof(float2));
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return TCG_ERR_CUDA;
+  }
+  cudaError_t e;
+  if (cs != cudaStreamCaptureStatusNone) {
+    e = cudaMallocAsync(out, bytes, st);
+  } else {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
+    cudaMemPool_t pool;
+    const int rc = tc_pool(dev, &pool);
+    if (rc != TCG_OK) return rc;
+    e = cudaMallocFromPoolAsync(out, bytes, pool, st);
+  }
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // an allocation failure is not a sticky error: clear it
+    *out = nullptr;
+    return TCG_ERR_OOM;
+  }
+  return TCG_OK;
+}
+
+// Frees a tc_alloc buffer in stream order when the call returns.
+struct StreamOrderedFree {
+  void* p = nullptr;
+  cudaStream_t st = nullptr;
+  ~StreamOrderedFree() {
+    if (p) (void)cudaFreeAsync(p, st);
+  }
+};
 
 // Runs every pass of a program direction: the specialised kernels when the
 // JIT policy selects them for this plan (see jit.cpp), else the generic
@@ -151,14 +199,17 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
   const uint32_t ntiles = 1u << (a.n - P->L);
   // tensor-core passes of a forward sweep: fuse this call's block matrices
   bool any_tc = false;
-  unsigned int* tc_err = nullptr;
   uint8_t* tc_fused = nullptr;
   float2* tc_scales = nullptr;
+  StreamOrderedFree tc_buf;
   if (mode == MODE_FWD && !P->tc_passes.empty()) {
     for (int ps = 0; ps < (int)P->passes.size(); ++ps) any_tc = any_tc || tc_use_pass(P, ps);
     if (any_tc) {
-      int rc = tc_scratch(P, batch, &tc_err, &tc_fused, &tc_scales);
+      int rc = tc_alloc(batch, P->tc_slots, st, &tc_buf.p);
       if (rc != TCG_OK) return rc;
+      tc_buf.st = st;
+      tc_fused = static_cast<uint8_t*>(tc_buf.p);
+      tc_scales = reinterpret_cast<float2*>(tc_fused + size_t(batch) * size_t(P->tc_slots) * kTcMatBytes);
       rc = cuda_rc(launch_tc_fuse(a.prog.tc_blocks, (int)P->tc_blocks.size(), a.prog.tc_gates, a.mats, a.mat_stride,
                                   batch, tc_fused, tc_scales, P->tc_slots, st));
       if (rc != TCG_OK) return rc;
@@ -168,7 +219,7 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
     const TcPassDesc& d = P->tc_passes[P->tc_of_pass[ps]];
     const DevPass& dp = P->passes[ps];
     return cuda_rc(launch_tc_pass(dp, d, a.prog.runs + dp.runs_off, a.prog.tc_blocks + d.block_begin, a.psi, a.n,
-                                  batch, tc_fused, tc_scales, P->tc_slots, tc_err, st));
+                                  batch, tc_fused, tc_scales, P->tc_slots, a.prog.tc_err, st));
   };
   if (jk) {
     KParams_Host kp;
@@ -307,12 +358,13 @@ int tcg_plan_check(const tcg_plan* plan, void* stream) {
   if (cudaGetDevice(&dev) != cudaSuccess) return TCG_ERR_CUDA;
   if (cudaStreamSynchronize(as_stream(stream)) != cudaSuccess) return TCG_ERR_CUDA;
   std::lock_guard<std::mutex> lk(p->fwd.mu);
-  auto it = p->fwd.tc_scratch.find(dev);
-  if (it == p->fwd.tc_scratch.end() || !it->second.base) return TCG_OK;
+  auto it = p->fwd.dev.find(dev);
+  if (it == p->fwd.dev.end()) return TCG_OK;  // never ran on this device
+  unsigned int* ef = it->second.view.tc_err;
   unsigned int flag = 0;
-  if (cudaMemcpy(&flag, it->second.base, sizeof(flag), cudaMemcpyDeviceToHost) != cudaSuccess) return TCG_ERR_CUDA;
+  if (cudaMemcpy(&flag, ef, sizeof(flag), cudaMemcpyDeviceToHost) != cudaSuccess) return TCG_ERR_CUDA;
   if (flag) {
-    if (cudaMemset(it->second.base, 0, sizeof(flag)) != cudaSuccess) return TCG_ERR_CUDA;
+    if (cudaMemset(ef, 0, sizeof(flag)) != cudaSuccess) return TCG_ERR_CUDA;
     return TCG_ERR_TIMEOUT;
   }
   return TCG_OK;

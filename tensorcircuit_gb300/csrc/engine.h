@@ -156,6 +156,7 @@ struct ProgramView {
   const TcPassDesc* tc_passes;  // tensor-core passes (forward programs)
   const TcBlock* tc_blocks;
   const TcGate* tc_gates;
+  unsigned int* tc_err;         // sticky flag: a tensor-core pass's wait ran out
 };
 
 }  // namespace tcg

@@ -940,7 +940,8 @@ int program_device_view(Program* p, ProgramView* view) {
   size_t o_tcp = al(o_z + p->zents.size() * sizeof(ZEnt));
   size_t o_tcb = al(o_tcp + p->tc_passes.size() * sizeof(TcPassDesc));
   size_t o_tcg = al(o_tcb + p->tc_blocks.size() * sizeof(TcBlock));
-  size_t total = al(o_tcg + p->tc_gates.size() * sizeof(TcGate)) + 256;
+  size_t o_err = al(o_tcg + p->tc_gates.size() * sizeof(TcGate));
+  size_t total = o_err + 256;
   std::vector<char> host(total, 0);
   if (!p->passes.empty()) std::memcpy(host.data() + o_pass, p->passes.data(), p->passes.size() * sizeof(DevPass));
   if (!p->stages.empty()) std::memcpy(host.data() + o_stage, p->stages.data(), p->stages.size() * sizeof(DevStage));
@@ -974,6 +975,7 @@ int program_device_view(Program* p, ProgramView* view) {
   c.view.tc_passes = (const TcPassDesc*)(b + o_tcp);
   c.view.tc_blocks = (const TcBlock*)(b + o_tcb);
   c.view.tc_gates = (const TcGate*)(b + o_tcg);
+  c.view.tc_err = (unsigned int*)(b + o_err);
   p->dev[dev] = c;
   *view = c.view;
   return TCG_OK;
@@ -987,13 +989,8 @@ void program_free(Program* p) {
     cudaSetDevice(kv.first);
     cudaFree(kv.second.base);
   }
-  for (auto& kv : p->tc_scratch) {
-    cudaSetDevice(kv.first);
-    cudaFree(kv.second.base);
-  }
   cudaSetDevice(cur);
   p->dev.clear();
-  p->tc_scratch.clear();
 }
 
 }  // namespace tcg

@@ -36,8 +36,8 @@ struct Program {
   std::mutex mu;
 
   // tensor-core passes (forward programs; tcpass.cu): source gates per pass,
-  // the fused blocks of the passes that qualify, and per device a buffer for
-  // the fused matrices of one call (grown on demand) with an error flag
+  // the fused blocks of the passes that qualify; the error flag of their
+  // bounded waits sits in the device copy (ProgramView::tc_err)
   std::vector<std::vector<int>> pass_gates;
   std::vector<TcPassDesc> tc_passes;
   std::vector<TcBlock> tc_blocks;
@@ -45,8 +45,6 @@ struct Program {
   std::vector<int> tc_of_pass;     // per pass: index into tc_passes, or -1
   std::vector<int> tc_prefer;      // per tensor pass: 1 if the cost model picks it
   int tc_slots = 0;                // fused matrices per circuit
-  struct TcScratch { void* base = nullptr; size_t bytes = 0; };
-  std::map<int, TcScratch> tc_scratch;
 
   // specialised kernels per mode (jit.cpp), built on demand
   std::unique_ptr<JitKernels> jit[4];

@@ -39,6 +39,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "engine.h"
@@ -723,28 +725,56 @@ __global__ void __launch_bounds__(128) tc_mma_probe_kernel(const __half* __restr
 }
 
 // ============================================================================
+namespace {
+
+// Kernel attributes are per device: one bit per device and kernel.
+std::atomic<uint64_t> g_attr_pass{0}, g_attr_probe{0};
+
+cudaError_t set_attrs_once(std::atomic<uint64_t>& done, const void* fn, int smem, bool carveout) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = uint64_t(1) << (dev & 63);
+  if (done.load() & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  if (carveout) {
+    // the largest shared-memory carveout, so that three CTAs fit on an SM
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+  }
+  done.fetch_or(bit);
+  return cudaSuccess;
+}
+
+}  // namespace
+
 cudaError_t launch_tc_fuse(const TcBlock* blocks, int nblocks, const TcGate* gates, const float2* mats,
                            int64_t mat_stride, int64_t batch, uint8_t* fused, float2* scales, int slots,
                            cudaStream_t st) {
   if (nblocks <= 0 || batch <= 0) return cudaSuccess;
-  dim3 grid((unsigned)nblocks, (unsigned)batch);
-  tc_fuse_kernel<<<grid, 256, 0, st>>>(blocks, gates, mats, mat_stride, fused, scales, slots);
-  count_launch();
-  return cudaGetLastError();
+  // grid.y is limited to 65535: larger batches go in chunks of circuits
+  constexpr int64_t kChunk = 65535;
+  for (int64_t b0 = 0; b0 < batch; b0 += kChunk) {
+    const int64_t nb = std::min(kChunk, batch - b0);
+    dim3 grid((unsigned)nblocks, (unsigned)nb);
+    tc_fuse_kernel<<<grid, 256, 0, st>>>(blocks, gates, mats + b0 * mat_stride, mat_stride,
+                                         fused + size_t(b0) * size_t(slots) * kTcMatBytes,
+                                         scales + size_t(b0) * size_t(slots), slots);
+    count_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const uint32_t* runs_dev,
                            const TcBlock* blocks_dev, float2* psi, int n, int64_t batch, const uint8_t* fused,
                            const float2* scales, int slots, unsigned int* err, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTotal);
-    if (e != cudaSuccess) return e;
-    // the largest shared-memory carveout, so that three CTAs fit on an SM
-    e = cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  const cudaError_t ea = set_attrs_once(g_attr_pass, (const void*)tc_pass_kernel, (int)kSmTotal, true);
+  if (ea != cudaSuccess) return ea;
+  // one CTA per (tile, circuit) in a 1-D grid
+  if ((int64_t(1) << (n - kTcTileBits)) * batch > int64_t(0x7fffffff)) return cudaErrorInvalidConfiguration;
   TcArgs a;
   a.psi = psi;
   a.n = n;
@@ -768,13 +798,9 @@ cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const ui
 
 cudaError_t launch_tc_mma_probe(const void* A, const void* B, float* D, int K, int N, unsigned int* err,
                                 cudaStream_t st) {
-  static bool attr_set = false;
   const int smem = 16384 + 32768 + 64;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc_mma_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  const cudaError_t ea = set_attrs_once(g_attr_probe, (const void*)tc_mma_probe_kernel, smem, false);
+  if (ea != cudaSuccess) return ea;
   tc_mma_probe_kernel<<<1, 128, smem, st>>>(static_cast<const __half*>(A), static_cast<const __half*>(B), D, K, N,
                                             err);
   count_launch();

@@ -284,7 +284,7 @@ def test_differentiable_channel_parameter(tc):
     e = engine(gt)
     e.backward()
     e0, pk = oracle(g0)
-    assert abs(float(e) - e0) <= 1e-5
+    assert abs(float(e.detach()) - e0) <= 1e-5
     eps = 1e-4
     ep, kp = oracle(g0 + eps)
     em, km = oracle(g0 - eps)

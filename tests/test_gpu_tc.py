@@ -141,3 +141,95 @@ def test_tc_zero_state_tiles(tc, policy):
     assert torch.isfinite(torch.view_as_real(psi)).all()
     want = dv.run_circuit(n, gl, "cuda")
     assert torch.linalg.vector_norm(psi.to(torch.complex128) - want).item() < 1e-6
+
+
+def _two_plans_same_structure(tc, n, depth):
+    """Two brick walls with the same gate layout and different matrices: one
+    plan, two rows of gate matrices."""
+    from tensorcircuit_gb300 import circuit as cmod
+    from tensorcircuit_gb300 import templates
+
+    gls = [templates.brickwall_gate_list(n, depth, s) for s in (11, 12)]
+    ents = [cmod._build_entry(n, templates.apply_gate_list(tc.Circuit(n), gl)._ops) for gl in gls]
+    mats = [e.const_block(torch.device("cuda")) for e in ents]
+    assert mats[0].shape == mats[1].shape
+    return gls, ents[0].plan, mats
+
+
+def test_tc_concurrent_streams_do_not_share_fused_matrices(tc, policy):
+    """One plan, two streams, two different sets of gate matrices in flight
+    at once: each call fuses into its own stream-ordered buffer, so both
+    results match the oracle."""
+    from tensorcircuit_gb300 import _native as nat
+
+    lib = nat.load()
+    n, B = 20, 4
+    gls, plan, mats = _two_plans_same_structure(tc, n, 12)
+    policy(1)
+    assert plan.tensor_passes() == plan.npasses
+    refs = [dv.run_circuit(n, gl, "cuda") for gl in gls]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    psis = []
+    torch.cuda.synchronize()
+    for rep in range(3):
+        outs = []
+        for k in (0, 1):
+            psi = torch.zeros(B, 1 << n, dtype=torch.complex64, device="cuda")
+            psi[:, 0] = 1
+            outs.append(psi)
+        torch.cuda.synchronize()
+        for k in (0, 1):
+            with torch.cuda.stream(streams[k]):
+                nat.check(lib.tcg_forward(plan.handle, outs[k].data_ptr(), B, mats[k].data_ptr(), 0,
+                                          streams[k].cuda_stream), "forward")
+        torch.cuda.synchronize()
+        psis.append(outs)
+    plan.check()
+    for outs in psis:
+        for k in (0, 1):
+            for b in range(B):
+                err = torch.linalg.vector_norm(outs[k][b].to(torch.complex128) - refs[k]).item()
+                assert err < 1e-5, (k, b, err)
+
+
+def test_tc_forward_under_graph_capture(tc, policy):
+    """A forward call captured into a CUDA graph owns its fused-matrix buffer
+    (graph memory nodes): replays stay correct after eager calls with a
+    larger batch in between."""
+    from tensorcircuit_gb300 import _native as nat
+
+    lib = nat.load()
+    n = 16
+    gls, plan, mats = _two_plans_same_structure(tc, n, 12)
+    policy(1)
+    refs = [dv.run_circuit(n, gl, "cuda") for gl in gls]
+
+    def fresh(B):
+        psi = torch.zeros(B, 1 << n, dtype=torch.complex64, device="cuda")
+        psi[:, 0] = 1
+        return psi
+
+    def fwd(psi, k):
+        st = torch.cuda.current_stream().cuda_stream
+        nat.check(lib.tcg_forward(plan.handle, psi.data_ptr(), psi.shape[0], mats[k].data_ptr(), 0, st), "forward")
+
+    # eager calls first: the plan's device program and specialised kernels
+    # are set up outside the capture
+    for _ in range(4):
+        fwd(fresh(2), 0)
+    psi_g = fresh(2)
+    start = fresh(2)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fwd(psi_g, 0)
+    for rep in range(2):
+        psi_g.copy_(start)
+        g.replay()
+        big = fresh(8)
+        fwd(big, 1)
+        torch.cuda.synchronize()
+        for b in range(2):
+            assert torch.linalg.vector_norm(psi_g[b].to(torch.complex128) - refs[0]).item() < 1e-5
+        for b in range(8):
+            assert torch.linalg.vector_norm(big[b].to(torch.complex128) - refs[1]).item() < 1e-5
+    plan.check()
