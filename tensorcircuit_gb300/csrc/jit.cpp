@@ -15,6 +15,7 @@
 #include <dlfcn.h>
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -80,9 +81,22 @@ struct OpRec {
   int pad;
 };
 
+// How a register stage's ops are emitted: 0 = a loop over constant op
+// records with a switch on the shared op bodies; 1 = straight-line code per
+// stage (operands become literals, and the compiler can overlap one op's
+// reduction with the next op's arithmetic); 2 = straight-line code whose
+// real-valued reductions (rotation gradients, Pauli-term values) are
+// collected over the stage and summed by one transpose-reduce.
+int stage_code_mode() {
+  const char* e = std::getenv("TCG_JIT_UNROLL");
+  if (!e || !*e) return 2;
+  const int v = e[0] - '0';
+  return (v >= 0 && v <= 2) ? v : 2;
+}
+
 class Gen {
  public:
-  Gen(const Program& P, int mode, int R) : P_(P), mode_(mode), R_(R) {}
+  Gen(const Program& P, int mode, int R) : P_(P), mode_(mode), R_(R), unroll_(stage_code_mode()) {}
 
   // Returns false when the op tables do not fit the 64 KiB constant bank.
   bool source(std::string* out) {
@@ -98,6 +112,11 @@ class Gen {
  private:
   const Program& P_;
   int mode_, R_;
+  int unroll_;
+  // set by op_sig when the op's real value is left in `defer_var_` for a
+  // stage-level reduction (stage code mode 2) instead of reduced in place
+  const char* defer_var_ = nullptr;
+  bool straight_ = false;  // op_sig is emitting for straight_ops
   const DevPass* dp_ = nullptr;
   int L_ = 0, NT_ = 0, NR_ = 0, NL_ = 0, NW_ = 0, MS_ = 1;
   bool has_mu_ = false;
@@ -204,7 +223,11 @@ class Gen {
 
   // One real value (a rotation's gradient): a real butterfly; the first
   // lane writes (sum, 0) where the complex reduction would.
-  std::string reduce_real(const char* var) const {
+  std::string reduce_real(const char* var) {
+    if (straight_ && unroll_ == 2 && NL_ == 32) {
+      defer_var_ = var;
+      return "";
+    }
     std::ostringstream o;
     if (NL_ < 32) {
       o << " { const float t = warp_sum1<" << NL_ << ">(" << var
@@ -232,6 +255,7 @@ class Gen {
   // straight into the stage's case.
   void op_sig(const DevOp& op, const Layout& l, OpRec* rec, bool* usesC) {
     std::memset(rec, 0, sizeof(*rec));
+    defer_var_ = nullptr;
     rec->off = op.mat_off;
     rec->slot = op.slot;
     std::ostringstream b;
@@ -471,6 +495,54 @@ class Gen {
     rec->sig = sig(b.str());
   }
 
+  // Straight-line code of one register stage: each op's body with its
+  // record as literals; in stage code mode 2 the ops' real values are kept
+  // in dv[] and reduced together at the end of the stage (pairs of values in
+  // one complex transpose-reduce, at most 32 values per reduction).
+  void straight_ops(std::ostringstream& oc, int si, const DevStage& S, const Layout& cur, bool* usesC) {
+    std::ostringstream c;
+    std::vector<int> dslots;
+    for (int oi = S.op_begin; oi < S.op_end; ++oi) {
+      OpRec r;
+      straight_ = true;
+      op_sig(P_.ops[oi], cur, &r, usesC);
+      straight_ = false;
+      c << "      { const OpRec op = {" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
+        << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}; (void)op;";
+      if (fwd() && r.pad) c << " const float2 csc = ld(Mt + " << r.off << "ll);";
+      c << " " << sig_body_[r.sig];
+      if (defer_var_) {
+        c << " dv[" << dslots.size() << "] = " << defer_var_ << ";";
+        dslots.push_back(r.slot);
+      }
+      c << " }\n";
+    }
+    if (c.str().empty()) return;
+    oc << "    case " << si << ": {\n";
+    if (!dslots.empty()) oc << "      float dv[" << dslots.size() << "];\n";
+    oc << c.str();
+    for (size_t g0 = 0; g0 < dslots.size(); g0 += 32) {
+      const int K = (int)std::min<size_t>(32, dslots.size() - g0);
+      int E2 = 1;
+      while (E2 < (K + 1) / 2) E2 <<= 1;
+      oc << "      { float2 gp[" << E2 << "];";
+      for (int i = 0; i < E2; ++i) {
+        const int a = 2 * i, bb = 2 * i + 1;
+        oc << " gp[" << i << "] = make_float2(" << (a < K ? "dv[" + std::to_string(g0 + a) + "]" : std::string("0.f"))
+           << ", " << (bb < K ? "dv[" + std::to_string(g0 + bb) + "]" : std::string("0.f")) << ");";
+      }
+      oc << " int ent; const float2 t = warp_reduce<" << E2 << ", 32>(gp, lane, ent);\n";
+      oc << "        switch (ent) {";
+      for (int i = 0; i < E2 && 2 * i < K; ++i) {
+        oc << " case " << i << ": sms[warp * " << MS_ << " + " << dslots[g0 + 2 * i] << "] = make_float2(t.x, 0.f);";
+        if (2 * i + 1 < K) oc << " sms[warp * " << MS_ << " + " << dslots[g0 + 2 * i + 1] << "] = make_float2(t.y, 0.f);";
+        oc << " break;";
+      }
+      oc << " default: break; }\n      }\n";
+    }
+    oc << "    } break;\n";
+  }
+
   // ------------------------------------------------------------------ pass
   // Emits one kernel; returns the constant-memory bytes its tables use.
   size_t pass(std::ostringstream& out, int pi) {
@@ -493,6 +565,7 @@ class Gen {
     std::vector<OpRec> recs;
     std::vector<int> so;  // slot, out pairs
     std::ostringstream cases;  // stage-entry code, one case per stage
+    std::ostringstream ops_cases;  // straight-line op code, one case per stage
     bool live = false, in_smem = false;
     Layout cur;
     const int NS = dp_->stage_end - dp_->stage_begin;
@@ -548,10 +621,19 @@ class Gen {
           regs_from_smem(c, cur, has_mu_);
           c << "      __syncthreads();\n";
         }
-        for (int oi = S.op_begin; oi < S.op_end; ++oi) {
-          OpRec r;
-          op_sig(P_.ops[oi], cur, &r, &usesC);
-          recs.push_back(r);
+        // dense ops keep the loop: straight-line code lets the compiler load
+        // several ops' matrices ahead, past the register budget
+        bool dense = false;
+        for (int oi = S.op_begin; oi < S.op_end; ++oi)
+          dense = dense || P_.ops[oi].kind == OP_DENSE1 || P_.ops[oi].kind == OP_DENSE2;
+        if (unroll_ == 0 || dense) {
+          for (int oi = S.op_begin; oi < S.op_end; ++oi) {
+            OpRec r;
+            op_sig(P_.ops[oi], cur, &r, &usesC);
+            recs.push_back(r);
+          }
+        } else {
+          straight_ops(ops_cases, si, S, cur, &usesC);
         }
       }
       const int oe = (int)recs.size();
@@ -625,9 +707,15 @@ class Gen {
       out << "      const float2 csc = csn; (void)csc;\n      if (o + 1 < oe && OPS_" << pi << "[o + 1].pad) csn = ld(Mt + OPS_"
           << pi << "[o + 1].off);\n";
     out << "      switch (op.sig) {\n";
-    for (size_t i = 0; i < sig_body_.size(); ++i)
-      out << "        case " << i << ": { " << sig_body_[i] << " } break;\n";
+    {
+      // the bodies the op records use (straight-line stages inline theirs)
+      std::vector<bool> used(sig_body_.size(), false);
+      for (const OpRec& r : recs) used[r.sig] = true;
+      for (size_t i = 0; i < sig_body_.size(); ++i)
+        if (used[i]) out << "        case " << i << ": { " << sig_body_[i] << " } break;\n";
+    }
     out << "        default: break;\n      }\n    }\n";
+    if (unroll_ != 0) out << "    switch (s) {\n" << ops_cases.str() << "    default: break;\n    }\n";
     out << "    if (useC) {\n#pragma unroll\n      for (int r = 0; r < " << NR_ << "; ++r) cmul_ip(v[r], C);\n    }\n";
     if (bwd() || meas()) {
       out << "    if (soe > sob) {\n      __syncthreads();\n";
