@@ -87,6 +87,10 @@ struct OpRec {
 // reduction with the next op's arithmetic); 2 = straight-line code whose
 // real-valued reductions (rotation gradients, Pauli-term values) are
 // collected over the stage and summed by one transpose-reduce.
+// Passes above this size (ops, counted twice when mu is held) share code
+// between stages of the same shape.
+constexpr int kShareOps = 100;
+
 int stage_code_mode() {
   const char* e = std::getenv("TCG_JIT_UNROLL");
   if (!e || !*e) return 2;
@@ -117,6 +121,10 @@ class Gen {
   // stage-level reduction (stage code mode 2) instead of reduced in place
   const char* defer_var_ = nullptr;
   bool straight_ = false;  // op_sig is emitting for straight_ops
+  int pi_ = 0;             // pass being emitted
+  bool share_ = false;     // stages of the same shape share code (large passes)
+  std::map<std::string, int> shape_id_;  // straight-line stage code -> id
+  std::vector<std::string> shape_code_;
   const DevPass* dp_ = nullptr;
   int L_ = 0, NT_ = 0, NR_ = 0, NL_ = 0, NW_ = 0, MS_ = 1;
   bool has_mu_ = false;
@@ -495,34 +503,52 @@ class Gen {
     rec->sig = sig(b.str());
   }
 
-  // Straight-line code of one register stage: each op's body with its
-  // record as literals; in stage code mode 2 the ops' real values are kept
-  // in dv[] and reduced together at the end of the stage (pairs of values in
-  // one complex transpose-reduce, at most 32 values per reduction).
-  void straight_ops(std::ostringstream& oc, int si, const DevStage& S, const Layout& cur, bool* usesC) {
+  // Straight-line code of one register stage: each op's body, its record
+  // read from the pass's stage-op table (SOPS_<pass>[rb + k], rb set by the
+  // stage's entry code), so that stages of the same shape -- e.g. the four
+  // rotations of an ansatz layer on the four register bits -- share one code
+  // block and the kernel's code stays small enough for the instruction
+  // cache.  In stage code mode 2 the ops' real values are kept in dv[] and
+  // reduced together at the end of the stage (pairs of values in one complex
+  // transpose-reduce, at most 32 values per reduction).  Returns the shape
+  // id, or -1 for a stage without ops.
+  // Where a deferred value of the stage's op k goes: a literal slot, or the
+  // slot of the op's table record when stages share code.
+  std::string slot_ref(const std::vector<OpRec>& srecs, size_t rb0, int k) const {
+    if (!share_) return std::to_string(srecs[rb0 + k].slot);
+    return "SOPS_" + std::to_string(pi_) + "[rb + " + std::to_string(k) + "].slot";
+  }
+
+  int straight_ops(const DevStage& S, const Layout& cur, bool* usesC, std::vector<OpRec>* srecs) {
     std::ostringstream c;
-    std::vector<int> dslots;
-    for (int oi = S.op_begin; oi < S.op_end; ++oi) {
+    std::vector<int> dops;  // index within the stage of each deferred value's op
+    const size_t rb0 = srecs->size();
+    int k = 0;
+    for (int oi = S.op_begin; oi < S.op_end; ++oi, ++k) {
       OpRec r;
       straight_ = true;
       op_sig(P_.ops[oi], cur, &r, usesC);
       straight_ = false;
-      c << "      { const OpRec op = {" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
-        << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}; (void)op;";
-      if (fwd() && r.pad) c << " const float2 csc = ld(Mt + " << r.off << "ll);";
+      srecs->push_back(r);
+      if (share_)
+        c << "      { const OpRec op = SOPS_" << pi_ << "[rb + " << k << "]; (void)op;";
+      else
+        c << "      { const OpRec op = {" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
+          << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}; (void)op;";
+      if (fwd() && r.pad) c << " const float2 csc = ld(Mt + op.off);";
       c << " " << sig_body_[r.sig];
       if (defer_var_) {
-        c << " dv[" << dslots.size() << "] = " << defer_var_ << ";";
-        dslots.push_back(r.slot);
+        c << " dv[" << dops.size() << "] = " << defer_var_ << ";";
+        dops.push_back(k);
       }
       c << " }\n";
     }
-    if (c.str().empty()) return;
-    oc << "    case " << si << ": {\n";
-    if (!dslots.empty()) oc << "      float dv[" << dslots.size() << "];\n";
+    if (k == 0) return -1;
+    std::ostringstream oc;
+    if (!dops.empty()) oc << "      float dv[" << dops.size() << "];\n";
     oc << c.str();
-    for (size_t g0 = 0; g0 < dslots.size(); g0 += 32) {
-      const int K = (int)std::min<size_t>(32, dslots.size() - g0);
+    for (size_t g0 = 0; g0 < dops.size(); g0 += 32) {
+      const int K = (int)std::min<size_t>(32, dops.size() - g0);
       int E2 = 1;
       while (E2 < (K + 1) / 2) E2 <<= 1;
       oc << "      { float2 gp[" << E2 << "];";
@@ -534,13 +560,22 @@ class Gen {
       oc << " int ent; const float2 t = warp_reduce<" << E2 << ", 32>(gp, lane, ent);\n";
       oc << "        switch (ent) {";
       for (int i = 0; i < E2 && 2 * i < K; ++i) {
-        oc << " case " << i << ": sms[warp * " << MS_ << " + " << dslots[g0 + 2 * i] << "] = make_float2(t.x, 0.f);";
-        if (2 * i + 1 < K) oc << " sms[warp * " << MS_ << " + " << dslots[g0 + 2 * i + 1] << "] = make_float2(t.y, 0.f);";
+        oc << " case " << i << ": sms[warp * " << MS_ << " + " << slot_ref(*srecs, rb0, dops[g0 + 2 * i])
+           << "] = make_float2(t.x, 0.f);";
+        if (2 * i + 1 < K)
+          oc << " sms[warp * " << MS_ << " + " << slot_ref(*srecs, rb0, dops[g0 + 2 * i + 1])
+             << "] = make_float2(t.y, 0.f);";
         oc << " break;";
       }
       oc << " default: break; }\n      }\n";
     }
-    oc << "    } break;\n";
+    const std::string code = oc.str();
+    auto it = shape_id_.find(code);
+    if (it != shape_id_.end()) return it->second;
+    const int id = (int)shape_code_.size();
+    shape_id_[code] = id;
+    shape_code_.push_back(code);
+    return id;
   }
 
   // ------------------------------------------------------------------ pass
@@ -565,13 +600,27 @@ class Gen {
     std::vector<OpRec> recs;
     std::vector<int> so;  // slot, out pairs
     std::ostringstream cases;  // stage-entry code, one case per stage
-    std::ostringstream ops_cases;  // straight-line op code, one case per stage
+    std::vector<OpRec> srecs;  // op records of the straight-line stages
+    shape_id_.clear();
+    shape_code_.clear();
+    pi_ = pi;
+    {
+      // Code size: literal straight-line code costs about one op body per
+      // op.  The n=20 HEA adjoint's first pass (76 ops holding psi and mu,
+      // some 250 KB of code) stalled on instruction fetch; sharing code
+      // between stages of the same shape halved those stalls there, while
+      // smaller passes ran slower with table-driven operands.
+      int nops = 0;
+      for (int st = dp_->stage_begin; st < dp_->stage_end; ++st) nops += P_.stages[st].op_end - P_.stages[st].op_begin;
+      share_ = nops * (has_mu_ ? 2 : 1) > kShareOps;
+    }
     bool live = false, in_smem = false;
     Layout cur;
     const int NS = dp_->stage_end - dp_->stage_begin;
     for (int si = 0; si < NS; ++si) {
       const DevStage& S = P_.stages[dp_->stage_begin + si];
       const int ob = (int)recs.size();
+      int shape = -1, rb = 0;  // straight-line code block and its first record
       bool usesC = false;
       std::ostringstream c;
       if (S.smem_stage) {
@@ -633,7 +682,8 @@ class Gen {
             recs.push_back(r);
           }
         } else {
-          straight_ops(ops_cases, si, S, cur, &usesC);
+          rb = (int)srecs.size();
+          shape = straight_ops(S, cur, &usesC, &srecs);
         }
       }
       const int oe = (int)recs.size();
@@ -646,7 +696,8 @@ class Gen {
       }
       const int soe = (int)so.size() / 2;
       cases << "    case " << si << ": {\n" << c.str() << "      ob = " << ob << "; oe = " << oe << "; sob = " << sob
-            << "; soe = " << soe << "; useC = " << (usesC ? "true" : "false") << ";\n    } break;\n";
+            << "; soe = " << soe << "; useC = " << (usesC ? "true" : "false") << "; sh = " << shape
+            << "; rb = " << rb << ";\n    } break;\n";
     }
 
     // constant tables
@@ -658,20 +709,30 @@ class Gen {
           << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}";
     }
     out << "};\n";
+    out << "__constant__ OpRec SOPS_" << pi << "[" << std::max<size_t>(srecs.size(), 1) << "] = {";
+    if (srecs.empty()) out << "{0, 0, -1, 0, 0, 0u, 0, 0, 0}";
+    for (size_t i = 0; i < srecs.size(); ++i) {
+      const OpRec& r = srecs[i];
+      out << (i ? ", " : "") << "{" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
+          << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}";
+    }
+    out << "};\n";
     out << "__constant__ int SO_" << pi << "[" << std::max<size_t>(so.size(), 2) << "] = {";
     if (so.empty()) out << "0, 0";
     for (size_t i = 0; i < so.size(); ++i) out << (i ? ", " : "") << so[i];
     out << "};\n";
 
     // kernel: three CTAs per SM for the modes that hold psi only (80
-    // registers), two for the ones that also hold mu or the 16 phases of a
-    // Z-rotation run (128 registers): more resident warps hide the dependent
-    // FMA chains and shuffles of these issue-bound kernels
+    // registers), two for the ones that also hold mu (128 registers): more
+    // resident warps hide the dependent FMA chains and shuffles of these
+    // issue-bound kernels.  A forward pass with Z-rotation runs (16 phases
+    // live) fits 80 registers as straight-line code (n=20 HEA: 14.31 ->
+    // 13.89 ms per value+grad step), not as the op loop.
     bool zrun = false;
     for (int s = dp_->stage_begin; s < dp_->stage_end; ++s)
       for (int o = P_.stages[s].op_begin; o < P_.stages[s].op_end; ++o)
         if (P_.ops[o].kind == OP_ZRUN) zrun = true;
-    const int min_ctas = (has_mu_ || (zrun && fwd())) ? 2 : 3;
+    const int min_ctas = (has_mu_ || (zrun && fwd() && unroll_ == 0)) ? 2 : 3;
     out << "extern \"C\" __global__ void __launch_bounds__(" << NT_ << ", " << min_ctas << ") "
         << kernel_name(mode_, pi)
         << "(KParams kp) {\n";
@@ -692,7 +753,7 @@ class Gen {
     out << "  u32 jt = 0u, gt = 0u, sjt = 0u;\n  (void)jt; (void)sjt;\n";
     out << "  u32 pneg = 0u;  // the tile's sign: rotations taken as -(partner)\n  (void)pneg;\n";
     out << "#pragma unroll 1\n  for (int s = 0; s < " << NS << "; ++s) {\n";
-    out << "    int ob = 0, oe = 0, sob = 0, soe = 0; bool useC = false;\n";
+    out << "    int ob = 0, oe = 0, sob = 0, soe = 0, sh = -1, rb = 0; bool useC = false; (void)rb;\n";
     out << "    switch (s) {\n" << cases.str() << "    default: break;\n    }\n";
     out << "    const u32 gthr = base | gt; (void)gthr;\n    float2 C = cone(); (void)C;\n";
     // forward: rotation entries (records with pad = 1) are loaded one op
@@ -715,7 +776,12 @@ class Gen {
         if (used[i]) out << "        case " << i << ": { " << sig_body_[i] << " } break;\n";
     }
     out << "        default: break;\n      }\n    }\n";
-    if (unroll_ != 0) out << "    switch (s) {\n" << ops_cases.str() << "    default: break;\n    }\n";
+    if (!shape_code_.empty()) {
+      out << "    switch (sh) {\n";
+      for (size_t i = 0; i < shape_code_.size(); ++i)
+        out << "    case " << i << ": {\n" << shape_code_[i] << "    } break;\n";
+      out << "    default: break;\n    }\n";
+    }
     out << "    if (useC) {\n#pragma unroll\n      for (int r = 0; r < " << NR_ << "; ++r) cmul_ip(v[r], C);\n    }\n";
     if (bwd() || meas()) {
       out << "    if (soe > sob) {\n      __syncthreads();\n";
@@ -757,7 +823,7 @@ class Gen {
       }
     }
     out << "}\n";
-    return recs.size() * sizeof(OpRec) + so.size() * sizeof(int);
+    return (recs.size() + srecs.size()) * sizeof(OpRec) + so.size() * sizeof(int);
   }
 };
 

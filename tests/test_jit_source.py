@@ -86,10 +86,10 @@ def test_hea_forward_and_adjoint_kernels_compile():
     regs_f, sp_f = check_compiles(e.plan.handle, 0, 0)
     regs_b, sp_b = check_compiles(e.plan.handle, 1, 1)
     print("forward registers", regs_f, "adjoint registers", regs_b, "spills", sp_f, sp_b)
-    # forward passes with Z-rotation runs and the adjoint keep two CTAs per SM
-    # (<= 128 registers); either may spill a few words
+    # forward passes (Z-rotation runs included) run three CTAs per SM (<= 80
+    # registers), the adjoint two (<= 128); either may spill a few words
     assert max(sp_f + [0]) <= 64 and max(sp_b + [0]) <= 64
-    assert max(regs_f) <= 128 and max(regs_b) <= 128, (regs_f, regs_b)
+    assert max(regs_f) <= 80 and max(regs_b) <= 128, (regs_f, regs_b)
 
 
 def test_brickwall_forward_kernels_fit_three_ctas():
