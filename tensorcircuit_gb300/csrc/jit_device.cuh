@@ -417,7 +417,9 @@ template <int NR, int X, int ZR, int NY, bool G>
 __device__ __forceinline__ u32 prot_bwd_sh(float2 (&v)[NR], float2 (&w)[NR], float c, float s, u32 sgn, float& g) {
   if (G) {
     constexpr bool IMZ = (NY & 1) == 0;
-    float zc = 0.f;
+    // four partial sums (register r into zc[r & 3]): four short FMA chains
+    // instead of one of 2 NR dependent FMAs
+    float zc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
       const float2 t = v[r ^ X];
@@ -425,14 +427,15 @@ __device__ __forceinline__ u32 prot_bwd_sh(float2 (&v)[NR], float2 (&w)[NR], flo
       const float wx = neg ? -w[r].x : w[r].x;
       const float wy = neg ? -w[r].y : w[r].y;
       if (IMZ) {
-        zc = fmaf(wx, t.y, zc);
-        zc = fmaf(-wy, t.x, zc);
+        zc[r & 3] = fmaf(wx, t.y, zc[r & 3]);
+        zc[r & 3] = fmaf(-wy, t.x, zc[r & 3]);
       } else {
-        zc = fmaf(wx, t.x, zc);
-        zc = fmaf(wy, t.y, zc);
+        zc[r & 3] = fmaf(wx, t.x, zc[r & 3]);
+        zc[r & 3] = fmaf(wy, t.y, zc[r & 3]);
       }
     }
-    g = ((NY & 3) == 0 || (NY & 3) == 3) ? zc : -zc;
+    const float zs = (zc[0] + zc[1]) + (zc[2] + zc[3]);
+    g = ((NY & 3) == 0 || (NY & 3) == 3) ? zs : -zs;
     if (sgn) g = -g;
   }
   float k, t;
