@@ -332,17 +332,27 @@ __device__ __forceinline__ void prot_rt(float2 (&v)[1 << R], float c, float qv, 
   }
 }
 
-// Im (IMZ) or Re of sum_r (-1)^{popc(r & zr)} conj(w[r]) v[r ^ X]
-template <int R, int X, bool IMZ>
+// Im (IMZ) or Re of sum_r (-1)^{popc(r & zr)} conj(w[r]) v[r ^ X]; Z0: zr is
+// known to be 0 (no Z/Y factor in the registers: rx, ry, rxx, ...), so no
+// per-register sign is computed.  Four partial sums keep the FMA chains short.
+template <int R, int X, bool IMZ, bool Z0>
 __device__ __forceinline__ float prot_dot(const float2 (&v)[1 << R], const float2 (&w)[1 << R], int zr) {
-  float z = 0.f;
+  float z[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
   for (int r = 0; r < (1 << R); ++r) {
     const float2 t = v[r ^ X];
-    const float term = IMZ ? fmaf(w[r].x, t.y, -w[r].y * t.x) : fmaf(w[r].x, t.x, w[r].y * t.y);
-    z += (__popc(r & zr) & 1) ? -term : term;
+    const bool neg = Z0 ? false : (__popc(r & zr) & 1) != 0;
+    const float wx = neg ? -w[r].x : w[r].x;
+    const float wy = neg ? -w[r].y : w[r].y;
+    if (IMZ) {
+      z[r & 3] = fmaf(wx, t.y, z[r & 3]);
+      z[r & 3] = fmaf(-wy, t.x, z[r & 3]);
+    } else {
+      z[r & 3] = fmaf(wx, t.x, z[r & 3]);
+      z[r & 3] = fmaf(wy, t.y, z[r & 3]);
+    }
   }
-  return z;
+  return (z[0] + z[1]) + (z[2] + z[3]);
 }
 
 #define TCG_X16(M) M(0) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11) M(12) M(13) M(14) M(15)
@@ -364,11 +374,12 @@ __device__ __forceinline__ void gshear_step(float& x, float& y, float k, float t
   else x = fmaf(flip ? k : -k, y, x);
 }
 // one of the three shear sweeps over every register pair of the rotation
-template <int R, int X, bool QIM, int STEP>
+// (Z0: no Z/Y factor in the registers, so no per-register sign)
+template <int R, int X, bool QIM, bool Z0, int STEP>
 __device__ __forceinline__ void gshear_sweep(float2 (&v)[1 << R], float k, float t, int zr) {
 #pragma unroll
   for (int r = 0; r < (1 << R); ++r) {
-    const bool sr = (__popc(r & zr) & 1) != 0;
+    const bool sr = Z0 ? false : (__popc(r & zr) & 1) != 0;
     if (X == 0) {
       gshear_step<STEP>(v[r].x, v[r].y, k, t, sr);
     } else {
@@ -384,57 +395,62 @@ __device__ __forceinline__ void gshear_sweep(float2 (&v)[1 << R], float k, float
     }
   }
 }
-template <int R, int X, bool QIM>
+template <int R, int X, bool QIM, bool Z0>
 __device__ __forceinline__ void gshear_rot(float2 (&v)[1 << R], float k, float t, int zr) {
-  gshear_sweep<R, X, QIM, 0>(v, k, t, zr);
-  gshear_sweep<R, X, QIM, 1>(v, k, t, zr);
-  gshear_sweep<R, X, QIM, 2>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 0>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 1>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 2>(v, k, t, zr);
 }
 // psi and mu together: the sweeps interleaved for independent FMAs
-template <int R, int X, bool QIM>
+template <int R, int X, bool QIM, bool Z0>
 __device__ __forceinline__ void gshear_rot2(float2 (&v)[1 << R], float2 (&w)[1 << R], float k, float t, int zr) {
-  gshear_sweep<R, X, QIM, 0>(v, k, t, zr);
-  gshear_sweep<R, X, QIM, 0>(w, k, t, zr);
-  gshear_sweep<R, X, QIM, 1>(v, k, t, zr);
-  gshear_sweep<R, X, QIM, 1>(w, k, t, zr);
-  gshear_sweep<R, X, QIM, 2>(v, k, t, zr);
-  gshear_sweep<R, X, QIM, 2>(w, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 0>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 0>(w, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 1>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 1>(w, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 2>(v, k, t, zr);
+  gshear_sweep<R, X, QIM, Z0, 2>(w, k, t, zr);
+}
+// X = the register-position mask of the rotation's X/Y factors (< 2^R)
+#define TCG_XC(XX) ((XX) < (1 << R) ? (XX) : 0)
+template <int R, bool QIM, bool Z0>
+__device__ __forceinline__ void dispatch_gshear_x(int x, float2 (&v)[1 << R], float k, float t, int zr) {
+#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot<R, TCG_XC(XX), QIM, Z0>(v, k, t, zr); break;
+  switch (x) {
+    TCG_X16(TCG_GS)
+    default: break;
+  }
+#undef TCG_GS
+}
+template <int R, bool QIM, bool Z0>
+__device__ __forceinline__ void dispatch_gshear2_x(int x, float2 (&v)[1 << R], float2 (&w)[1 << R], float k, float t,
+                                                   int zr) {
+#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot2<R, TCG_XC(XX), QIM, Z0>(v, w, k, t, zr); break;
+  switch (x) {
+    TCG_X16(TCG_GS)
+    default: break;
+  }
+#undef TCG_GS
 }
 template <int R>
 __device__ __forceinline__ void dispatch_gshear(int x, bool qim, float2 (&v)[1 << R], float k, float t, int zr) {
   if (qim) {
-#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot<R, ((XX) < (1 << R) ? (XX) : 0), true>(v, k, t, zr); break;
-    switch (x) {
-      TCG_X16(TCG_GS)
-      default: break;
-    }
-#undef TCG_GS
+    if (zr == 0) dispatch_gshear_x<R, true, true>(x, v, k, t, zr);
+    else dispatch_gshear_x<R, true, false>(x, v, k, t, zr);
   } else {
-#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot<R, ((XX) < (1 << R) ? (XX) : 0), false>(v, k, t, zr); break;
-    switch (x) {
-      TCG_X16(TCG_GS)
-      default: break;
-    }
-#undef TCG_GS
+    if (zr == 0) dispatch_gshear_x<R, false, true>(x, v, k, t, zr);
+    else dispatch_gshear_x<R, false, false>(x, v, k, t, zr);
   }
 }
 template <int R>
 __device__ __forceinline__ void dispatch_gshear2(int x, bool qim, float2 (&v)[1 << R], float2 (&w)[1 << R], float k,
                                                  float t, int zr) {
   if (qim) {
-#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot2<R, ((XX) < (1 << R) ? (XX) : 0), true>(v, w, k, t, zr); break;
-    switch (x) {
-      TCG_X16(TCG_GS)
-      default: break;
-    }
-#undef TCG_GS
+    if (zr == 0) dispatch_gshear2_x<R, true, true>(x, v, w, k, t, zr);
+    else dispatch_gshear2_x<R, true, false>(x, v, w, k, t, zr);
   } else {
-#define TCG_GS(XX) case XX: if ((XX) < (1 << R)) gshear_rot2<R, ((XX) < (1 << R) ? (XX) : 0), false>(v, w, k, t, zr); break;
-    switch (x) {
-      TCG_X16(TCG_GS)
-      default: break;
-    }
-#undef TCG_GS
+    if (zr == 0) dispatch_gshear2_x<R, false, true>(x, v, w, k, t, zr);
+    else dispatch_gshear2_x<R, false, false>(x, v, w, k, t, zr);
   }
 }
 
@@ -457,26 +473,23 @@ __device__ __forceinline__ void dispatch_prot(int x, float2 (&v)[1 << R], float 
   }
 }
 
+template <int R, bool IMZ, bool Z0>
+__device__ __forceinline__ float dispatch_prot_dot_x(int x, const float2 (&v)[1 << R], const float2 (&w)[1 << R],
+                                                     int zr) {
+  float z = 0.f;
+#define TCG_PD(XX) case XX: if ((XX) < (1 << R)) z = prot_dot<R, TCG_XC(XX), IMZ, Z0>(v, w, zr); break;
+  switch (x) {
+    TCG_X16(TCG_PD)
+    default: break;
+  }
+#undef TCG_PD
+  return z;
+}
 template <int R>
 __device__ __forceinline__ float dispatch_prot_dot(int x, const float2 (&v)[1 << R], const float2 (&w)[1 << R],
                                                    int zr, bool imz) {
-  float z = 0.f;
-  if (imz) {
-#define TCG_PD(XX) case XX: if ((XX) < (1 << R)) z = prot_dot<R, ((XX) < (1 << R) ? (XX) : 0), true>(v, w, zr); break;
-    switch (x) {
-      TCG_X16(TCG_PD)
-      default: break;
-    }
-#undef TCG_PD
-  } else {
-#define TCG_PD(XX) case XX: if ((XX) < (1 << R)) z = prot_dot<R, ((XX) < (1 << R) ? (XX) : 0), false>(v, w, zr); break;
-    switch (x) {
-      TCG_X16(TCG_PD)
-      default: break;
-    }
-#undef TCG_PD
-  }
-  return z;
+  if (imz) return zr == 0 ? dispatch_prot_dot_x<R, true, true>(x, v, w, zr) : dispatch_prot_dot_x<R, true, false>(x, v, w, zr);
+  return zr == 0 ? dispatch_prot_dot_x<R, false, true>(x, v, w, zr) : dispatch_prot_dot_x<R, false, false>(x, v, w, zr);
 }
 
 // (-i)^nY
