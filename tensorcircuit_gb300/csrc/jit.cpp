@@ -122,6 +122,10 @@ class Gen {
   const char* defer_var_ = nullptr;
   bool straight_ = false;  // op_sig is emitting for straight_ops
   int pi_ = 0;             // pass being emitted
+  // rotations of the pass's straight-line stages: matrix offset of (c, s)
+  // and the sign of q = +-s, for the kernel prologue's shear table
+  std::vector<int64_t> rot_off_;
+  std::vector<int> rot_sq_;
   bool share_ = false;     // stages of the same shape share code (large passes)
   std::map<std::string, int> shape_id_;  // straight-line stage code -> id
   std::vector<std::string> shape_code_;
@@ -359,9 +363,32 @@ class Gen {
         b << "const u32 sg = 0u; ";
       else
         b << "const u32 sg = __popc(gthr & op.zm) & 1u; ";
+      // (in straight-line stages the body above is replaced below)
       // three in-place shears per component pair; a rotation with cos < 0
       // toggles the tile's sign bit (applied when the tile is stored)
-      if (fwd()) {
+      if (straight_ && (fwd() || bwd())) {
+        // shear parameters from the CTA's table (the kernel prologue filled
+        // it and the tile's sign bit); rec->g0 = the rotation's table index
+        rec->g0 = (int)rot_off_.size();
+        rot_off_.push_back(op.mat_off);
+        const bool neg_q = ((op.nY & 3) <= 1) != bwd();  // q = -s: (-i)^nY sign, adjoint
+        rot_sq_.push_back(neg_q ? -1 : 1);
+        b.str("");
+        if ((op.zmask & ~(uint64_t)gr(l, NR_ - 1)) == 0)
+          b << "const u32 sg = 0u; ";
+        else
+          b << "const u32 sg = __popc(gthr & op.zm) & 1u; ";
+        b << "const float2 kt = shk[op.g0]; ";
+        if (fwd()) {
+          b << "float k = kt.x, t = kt.y; if (sg) { k = -k; t = -t; } prot_sh<" << NR_ << ", " << op.xreg << ", "
+            << zr << ", " << (op.nY & 3) << ">(v, k, t);";
+        } else {
+          const bool G = op.slot >= 0;
+          b << "float g = 0.f; prot_bwd_kt<" << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ", "
+            << (G ? "true" : "false") << ">(v, w, kt.x, kt.y, sg, g);";
+          if (G) b << reduce_real("g");
+        }
+      } else if (fwd()) {
         b << "float k, t; pneg ^= shear_params(cs.x, prot_qv<" << (op.nY & 3) << ">(cs.y, sg, false), k, t); prot_sh<"
           << NR_ << ", " << op.xreg << ", " << zr << ", " << (op.nY & 3) << ">(v, k, t);";
       } else {
@@ -535,7 +562,7 @@ class Gen {
       else
         c << "      { const OpRec op = {" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
           << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}; (void)op;";
-      if (fwd() && r.pad) c << " const float2 csc = ld(Mt + op.off);";
+      if (fwd() && r.pad && P_.ops[oi].kind != OP_PROT) c << " const float2 csc = ld(Mt + op.off);";
       c << " " << sig_body_[r.sig];
       if (defer_var_) {
         c << " dv[" << dops.size() << "] = " << defer_var_ << ";";
@@ -603,13 +630,16 @@ class Gen {
     std::vector<OpRec> srecs;  // op records of the straight-line stages
     shape_id_.clear();
     shape_code_.clear();
+    rot_off_.clear();
+    rot_sq_.clear();
     pi_ = pi;
     {
       // Code size: literal straight-line code costs about one op body per
       // op.  The n=20 HEA adjoint's first pass (76 ops holding psi and mu,
       // some 250 KB of code) stalled on instruction fetch; sharing code
-      // between stages of the same shape halved those stalls there, while
-      // smaller passes ran slower with table-driven operands.
+      // between stages of the same shape halved those stalls there (that
+      // pass 2 % faster, the whole step unchanged within run-to-run noise),
+      // while smaller passes ran slower with table-driven operands.
       int nops = 0;
       for (int st = dp_->stage_begin; st < dp_->stage_end; ++st) nops += P_.stages[st].op_end - P_.stages[st].op_begin;
       share_ = nops * (has_mu_ ? 2 : 1) > kShareOps;
@@ -717,6 +747,14 @@ class Gen {
           << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}";
     }
     out << "};\n";
+    const size_t nrot = rot_off_.size();
+    if (nrot > 0) {
+      out << "__constant__ long long ROTO_" << pi << "[" << nrot << "] = {";
+      for (size_t i = 0; i < nrot; ++i) out << (i ? ", " : "") << rot_off_[i] << "ll";
+      out << "};\n__constant__ float ROTS_" << pi << "[" << nrot << "] = {";
+      for (size_t i = 0; i < nrot; ++i) out << (i ? ", " : "") << (rot_sq_[i] < 0 ? "-1.f" : "1.f");
+      out << "};\n";
+    }
     out << "__constant__ int SO_" << pi << "[" << std::max<size_t>(so.size(), 2) << "] = {";
     if (so.empty()) out << "0, 0";
     for (size_t i = 0; i < so.size(); ++i) out << (i ? ", " : "") << so[i];
@@ -752,6 +790,16 @@ class Gen {
     if (has_mu_) out << "  float2 w[" << NR_ << "];\n";
     out << "  u32 jt = 0u, gt = 0u, sjt = 0u;\n  (void)jt; (void)sjt;\n";
     out << "  u32 pneg = 0u;  // the tile's sign: rotations taken as -(partner)\n  (void)pneg;\n";
+    if (nrot > 0) {
+      // prologue: the shear parameters of every table rotation, once per CTA,
+      // and the tile sign their c < 0 cases leave
+      out << "  __shared__ float2 shk[" << nrot << "];\n  __shared__ u32 shneg;\n";
+      out << "  if (tid == 0u) shneg = 0u;\n  __syncthreads();\n";
+      out << "  for (u32 i = tid; i < " << nrot << "u; i += " << NT_ << "u) {\n";
+      out << "    const float2 cs = ld(Mt + ROTO_" << pi << "[i]);\n    float k, t;\n";
+      out << "    if (shear_params(cs.x, ROTS_" << pi << "[i] * cs.y, k, t)) atomicXor(&shneg, 1u);\n";
+      out << "    shk[i] = make_float2(k, t);\n  }\n  __syncthreads();\n  pneg = shneg;\n";
+    }
     out << "#pragma unroll 1\n  for (int s = 0; s < " << NS << "; ++s) {\n";
     out << "    int ob = 0, oe = 0, sob = 0, soe = 0, sh = -1, rb = 0; bool useC = false; (void)rb;\n";
     out << "    switch (s) {\n" << cases.str() << "    default: break;\n    }\n";

@@ -450,6 +450,44 @@ __device__ __forceinline__ u32 prot_bwd_sh(float2 (&v)[NR], float2 (&w)[NR], flo
   return ng;
 }
 
+// The same adjoint step with the shear parameters precomputed for the
+// whole CTA (k, t of the thread-parity-even case; an odd thread parity
+// negates both), so no reciprocal sits at the head of each rotation.
+template <int NR, int X, int ZR, int NY, bool G>
+__device__ __forceinline__ void prot_bwd_kt(float2 (&v)[NR], float2 (&w)[NR], float k, float t, u32 sgn, float& g) {
+  if (G) {
+    constexpr bool IMZ = (NY & 1) == 0;
+    float zc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      const float2 tv = v[r ^ X];
+      const bool neg = (tk_popc(r & ZR) & 1) != 0;
+      const float wx = neg ? -w[r].x : w[r].x;
+      const float wy = neg ? -w[r].y : w[r].y;
+      if (IMZ) {
+        zc[r & 3] = fmaf(wx, tv.y, zc[r & 3]);
+        zc[r & 3] = fmaf(-wy, tv.x, zc[r & 3]);
+      } else {
+        zc[r & 3] = fmaf(wx, tv.x, zc[r & 3]);
+        zc[r & 3] = fmaf(wy, tv.y, zc[r & 3]);
+      }
+    }
+    const float zs = (zc[0] + zc[1]) + (zc[2] + zc[3]);
+    g = ((NY & 3) == 0 || (NY & 3) == 3) ? zs : -zs;
+    if (sgn) g = -g;
+  }
+  if (sgn) {
+    k = -k;
+    t = -t;
+  }
+  prot_sh_sweep<NR, X, ZR, NY, 0>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 0>(w, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 1>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 1>(w, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 2>(v, k, t);
+  prot_sh_sweep<NR, X, ZR, NY, 2>(w, k, t);
+}
+
 // ------------------------------------------------- runs of Z-string rotations
 // ph[c] holds the product of the run's entries of register class c (entry
 // factor e^{-i phi} when the thread's part of the parity is even, e^{+i phi}
