@@ -140,6 +140,14 @@ int tcg_debug_tc_program(const tcg_plan* plan, const void** arrays, int64_t* cou
 int tcg_forward(const tcg_plan* plan, void* psi, int64_t batch,
                 const void* mats, int64_t mat_stride, void* stream);
 
+/* tcg_forward with the input states read from elsewhere (no reference
+ * counterpart: it saves the copy of the input into the output buffer).  The
+ * first pass reads psi_in[b * in_stride ..] (in_stride 0: one state for every
+ * circuit, e.g. |0...0>; psi_in == psi with in_stride 2^n is tcg_forward) and
+ * every pass writes psi [batch][2^n]. */
+int tcg_forward_from(const tcg_plan* plan, const void* psi_in, int64_t in_stride, void* psi,
+                     int64_t batch, const void* mats, int64_t mat_stride, void* stream);
+
 /* Replaces: the reverse-mode AD that backend.vvag runs through the taped
  * tensordots (tensorcircuit/backends/pytorch_backend.py:673-709).  Adjoint
  * sweep: on entry psi = output states, mu = cotangent of the output (torch
@@ -152,6 +160,13 @@ int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch,
                  const void* mats, int64_t mat_stride, void* grads,
                  int64_t grad_stride, void* scratch, size_t scratch_bytes,
                  void* stream);
+/* tcg_backward with the output states read from psi_out [batch][2^n]
+ * (left unchanged) instead of psi: psi is written with the input states, so
+ * the caller keeps its output states without copying them first. */
+int tcg_backward_from(const tcg_plan* plan, const void* psi_out, void* psi, void* mu,
+                      int64_t batch, const void* mats, int64_t mat_stride, void* grads,
+                      int64_t grad_stride, void* scratch, size_t scratch_bytes,
+                      void* stream);
 
 /* ---- observables ---------------------------------------------------------- */
 
@@ -209,6 +224,12 @@ int tcg_expect_pauli_noalloc(const void* psi, int32_t nqubits, int64_t batch,
 int tcg_pauli_accumulate(const tcg_mplan* plan, const void* psi, void* mu,
                          int64_t batch, const float* coef, int64_t coef_stride,
                          void* stream);
+/* flags: TCG_ACC_OVERWRITE = mu[b] = sum_t ... (mu's old contents are not
+ * read, so it needs no zero fill first). */
+#define TCG_ACC_OVERWRITE 1
+int tcg_pauli_accumulate_ex(const tcg_mplan* plan, const void* psi, void* mu,
+                            int64_t batch, const float* coef, int64_t coef_stride,
+                            int32_t flags, void* stream);
 
 /* ---- sampling --------------------------------------------------------------
  * Replaces: BaseCircuit.sample(allow_state=True, status=u)

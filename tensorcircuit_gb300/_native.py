@@ -21,6 +21,7 @@ TCG_ERR_SCRATCH = 5
 TCG_ERR_OOM = 6
 TCG_ERR_TOO_LARGE = 7
 TCG_ERR_TIMEOUT = 8
+TCG_ACC_OVERWRITE = 1
 
 TCG_GATE_DENSE = 0
 TCG_GATE_DIAG = 1
@@ -93,14 +94,17 @@ SIGNATURES = [
     ("tcg_debug_tc_mma", ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
     ("tcg_debug_tc_program", ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     ("tcg_forward", ctypes.c_int, [_P, _P, _I64, _P, _I64, _P]),
+    ("tcg_forward_from", ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _I64, _P]),
     ("tcg_backward_scratch_bytes", _SZ, [_P, _I64]),
     ("tcg_backward", ctypes.c_int, [_P, _P, _P, _I64, _P, _I64, _P, _I64, _P, _SZ, _P]),
+    ("tcg_backward_from", ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _I64, _P, _I64, _P, _SZ, _P]),
     ("tcg_mplan_create", ctypes.c_int, [_I32, ctypes.POINTER(TcgPauli), _I32, ctypes.POINTER(_P)]),
     ("tcg_mplan_destroy", ctypes.c_int, [_P]),
     ("tcg_mplan_passes", ctypes.c_int, [_P]),
     ("tcg_expect_scratch_bytes", _SZ, [_P, _I64]),
     ("tcg_expect_pauli", ctypes.c_int, [_P, _P, _I64, _P, _P, _SZ, _P]),
     ("tcg_pauli_accumulate", ctypes.c_int, [_P, _P, _P, _I64, _P, _I64, _P]),
+    ("tcg_pauli_accumulate_ex", ctypes.c_int, [_P, _P, _P, _I64, _P, _I64, ctypes.c_int32, _P]),
     ("tcg_expect_pauli_noalloc", ctypes.c_int, [_P, _I32, _I64, ctypes.POINTER(TcgPauli), _I32, _P, _P]),
     ("tcg_sample_scratch_bytes", _SZ, [_I32, _I64]),
     ("tcg_sample", ctypes.c_int, [_P, _I32, _I64, _P, _I64, _I64, _P, _P, _SZ, _P]),

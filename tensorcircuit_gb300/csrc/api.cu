@@ -183,6 +183,22 @@ struct StreamOrderedFree {
 // JIT policy selects them for this plan (see jit.cpp), else the generic
 // pass kernels of pass.cu.
 int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStream_t st) {
+  if ((a.psi_in || a.mu_zero) && !P->passes.empty() && P->passes[0].stage_end == P->passes[0].stage_begin) {
+    // a first pass without stages never loads or stores its tiles: put the
+    // input where the sweep works in place instead
+    const size_t len = size_t(1) << a.n;
+    if (a.psi_in) {
+      for (int64_t b = 0; b < batch; ++b)
+        if (cudaMemcpyAsync(a.psi + size_t(b) * len, a.psi_in + size_t(b) * size_t(a.in_stride), len * sizeof(float2),
+                            cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+          return TCG_ERR_CUDA;
+      a.psi_in = nullptr;
+    }
+    if (a.mu_zero) {
+      if (cudaMemsetAsync(a.mu, 0, size_t(batch) * len * sizeof(float2), st) != cudaSuccess) return TCG_ERR_CUDA;
+      a.mu_zero = 0;
+    }
+  }
   JitKernels* jk = nullptr;
   {
     std::lock_guard<std::mutex> lk(P->jit_mu);
@@ -215,11 +231,14 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
       if (rc != TCG_OK) return rc;
     }
   }
+  // a separate input state (psi_in) and a zero start of mu (mu_zero) apply
+  // to the sweep's first pass only
   auto tc_launch = [&](int ps) -> int {
     const TcPassDesc& d = P->tc_passes[P->tc_of_pass[ps]];
     const DevPass& dp = P->passes[ps];
-    return cuda_rc(launch_tc_pass(dp, d, a.prog.runs + dp.runs_off, a.prog.tc_blocks + d.block_begin, a.psi, a.n,
-                                  batch, tc_fused, tc_scales, P->tc_slots, a.prog.tc_err, st));
+    return cuda_rc(launch_tc_pass(dp, d, a.prog.runs + dp.runs_off, a.prog.tc_blocks + d.block_begin, a.psi,
+                                  ps == 0 ? a.psi_in : nullptr, a.in_stride, a.n, batch, tc_fused, tc_scales,
+                                  P->tc_slots, a.prog.tc_err, st));
   };
   if (jk) {
     KParams_Host kp;
@@ -231,7 +250,11 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
     kp.part_stride = a.part_stride;
     kp.coef = a.coef;
     kp.coef_stride = a.coef_stride;
+    kp.in_stride = a.in_stride;
+    kp.pad = 0;
     for (int ps = 0; ps < (int)P->passes.size(); ++ps) {
+      kp.psi_in = ps == 0 ? a.psi_in : nullptr;
+      kp.mu_zero = ps == 0 ? a.mu_zero : 0;
       const int rc = (any_tc && tc_use_pass(P, ps)) ? tc_launch(ps)
                                                     : cuda_rc(jit_launch(jk, ps, kp, ntiles, batch, a.n, st));
       if (rc != TCG_OK) return rc;
@@ -239,8 +262,13 @@ int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStr
     return TCG_OK;
   }
   for (int ps = 0; ps < (int)P->passes.size(); ++ps) {
-    a.pass = ps;
-    const int rc = (any_tc && tc_use_pass(P, ps)) ? tc_launch(ps) : cuda_rc(launch_pass(mode, R, a, P->L, batch, st));
+    PassArgs ap = a;
+    ap.pass = ps;
+    if (ps > 0) {
+      ap.psi_in = nullptr;
+      ap.mu_zero = 0;
+    }
+    const int rc = (any_tc && tc_use_pass(P, ps)) ? tc_launch(ps) : cuda_rc(launch_pass(mode, R, ap, P->L, batch, st));
     if (rc != TCG_OK) return rc;
   }
   return TCG_OK;
@@ -426,17 +454,60 @@ int tcg_forward(const tcg_plan* plan, void* psi, int64_t batch, const void* mats
   return run_program(&p->fwd, MODE_FWD, kRFwd, a, batch, as_stream(stream));
 }
 
+int tcg_forward_from(const tcg_plan* plan, const void* psi_in, int64_t in_stride, void* psi, int64_t batch,
+                     const void* mats, int64_t mat_stride, void* stream) {
+  if (!plan || !psi || !psi_in || batch < 0 || in_stride < 0) return TCG_ERR_INVALID_ARG;
+  if (batch == 0) return TCG_OK;
+  const int64_t N = int64_t(1) << plan->n;
+  if (psi_in == psi && in_stride != N) return TCG_ERR_INVALID_ARG;
+  if (plan->ngates == 0 || psi_in == psi) {
+    if (psi_in != psi) {
+      // no passes: the output is the input, row by row
+      for (int64_t b = 0; b < batch; ++b)
+        if (cudaMemcpyAsync(static_cast<float2*>(psi) + b * N, static_cast<const float2*>(psi_in) + b * in_stride,
+                            size_t(N) * sizeof(float2), cudaMemcpyDeviceToDevice, as_stream(stream)) != cudaSuccess)
+          return TCG_ERR_CUDA;
+      return TCG_OK;
+    }
+    return tcg_forward(plan, psi, batch, mats, mat_stride, stream);
+  }
+  if (!mats) return TCG_ERR_INVALID_ARG;
+  tcg_plan* p = const_cast<tcg_plan*>(plan);
+  ProgramView view;
+  int rc = program_device_view(&p->fwd, &view);
+  if (rc != TCG_OK) return rc;
+  PassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.prog = view;
+  a.n = plan->n;
+  a.psi = static_cast<float2*>(psi);
+  a.psi_in = static_cast<const float2*>(psi_in);
+  a.in_stride = in_stride;
+  a.mats = static_cast<const float2*>(mats);
+  a.mat_stride = mat_stride;
+  a.max_slots = 0;
+  return run_program(&p->fwd, MODE_FWD, kRFwd, a, batch, as_stream(stream));
+}
+
 size_t tcg_backward_scratch_bytes(const tcg_plan* plan, int64_t batch) {
   if (!plan) return 0;
   const size_t ntiles = size_t(1) << (plan->n - plan->bwd.L);
   return size_t(batch) * size_t(std::max<int64_t>(plan->bwd.nout, 1)) * ntiles * sizeof(float2) + 256;
 }
 
-int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch, const void* mats,
-                 int64_t mat_stride, void* grads, int64_t grad_stride, void* scratch, size_t scratch_bytes,
-                 void* stream) {
+namespace {
+int backward_impl(const tcg_plan* plan, const void* psi_in, void* psi, void* mu, int64_t batch, const void* mats,
+                  int64_t mat_stride, void* grads, int64_t grad_stride, void* scratch, size_t scratch_bytes,
+                  void* stream) {
   if (!plan || !psi || !mu || batch < 0) return TCG_ERR_INVALID_ARG;
-  if (batch == 0 || plan->ngates == 0) return TCG_OK;
+  if (batch == 0) return TCG_OK;
+  if (plan->ngates == 0) {
+    if (psi_in && psi_in != psi &&
+        cudaMemcpyAsync(psi, psi_in, size_t(batch) * (size_t(1) << plan->n) * sizeof(float2),
+                        cudaMemcpyDeviceToDevice, as_stream(stream)) != cudaSuccess)
+      return TCG_ERR_CUDA;
+    return TCG_OK;
+  }
   if (!mats) return TCG_ERR_INVALID_ARG;
   if (plan->has_grad && (!grads || grad_stride < plan->grad_entries)) return TCG_ERR_INVALID_ARG;
   tcg_plan* p = const_cast<tcg_plan*>(plan);
@@ -451,6 +522,10 @@ int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch, const
   a.n = plan->n;
   a.psi = static_cast<float2*>(psi);
   a.mu = static_cast<float2*>(mu);
+  if (psi_in && psi_in != psi) {
+    a.psi_in = static_cast<const float2*>(psi_in);
+    a.in_stride = int64_t(1) << plan->n;
+  }
   a.mats = static_cast<const float2*>(mats);
   a.mat_stride = mat_stride;
   a.partial = static_cast<float2*>(scratch);
@@ -465,6 +540,22 @@ int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch, const
                                         as_stream(stream)));
   }
   return rc;
+}
+}  // namespace
+
+int tcg_backward(const tcg_plan* plan, void* psi, void* mu, int64_t batch, const void* mats,
+                 int64_t mat_stride, void* grads, int64_t grad_stride, void* scratch, size_t scratch_bytes,
+                 void* stream) {
+  return backward_impl(plan, nullptr, psi, mu, batch, mats, mat_stride, grads, grad_stride, scratch, scratch_bytes,
+                       stream);
+}
+
+int tcg_backward_from(const tcg_plan* plan, const void* psi_out, void* psi, void* mu, int64_t batch,
+                      const void* mats, int64_t mat_stride, void* grads, int64_t grad_stride, void* scratch,
+                      size_t scratch_bytes, void* stream) {
+  if (!psi_out) return TCG_ERR_INVALID_ARG;
+  return backward_impl(plan, psi_out, psi, mu, batch, mats, mat_stride, grads, grad_stride, scratch, scratch_bytes,
+                       stream);
 }
 
 int tcg_mplan_create(int32_t nqubits, const tcg_pauli* terms, int32_t nterms, tcg_mplan** out) {
@@ -560,8 +651,19 @@ int tcg_expect_pauli(const tcg_mplan* plan, const void* psi, int64_t batch, doub
 
 int tcg_pauli_accumulate(const tcg_mplan* plan, const void* psi, void* mu, int64_t batch, const float* coef,
                          int64_t coef_stride, void* stream) {
-  if (!plan || !psi || !mu || !coef || batch < 0) return TCG_ERR_INVALID_ARG;
-  if (batch == 0 || plan->nterms == 0) return TCG_OK;
+  return tcg_pauli_accumulate_ex(plan, psi, mu, batch, coef, coef_stride, 0, stream);
+}
+
+int tcg_pauli_accumulate_ex(const tcg_mplan* plan, const void* psi, void* mu, int64_t batch, const float* coef,
+                            int64_t coef_stride, int32_t flags, void* stream) {
+  if (!plan || !psi || !mu || !coef || batch < 0 || (flags & ~TCG_ACC_OVERWRITE)) return TCG_ERR_INVALID_ARG;
+  if (batch == 0) return TCG_OK;
+  const bool overwrite = (flags & TCG_ACC_OVERWRITE) != 0;
+  const size_t state_bytes = size_t(batch) * (size_t(1) << plan->n) * sizeof(float2);
+  if (plan->nterms == 0) {
+    if (overwrite && cudaMemsetAsync(mu, 0, state_bytes, as_stream(stream)) != cudaSuccess) return TCG_ERR_CUDA;
+    return TCG_OK;
+  }
   tcg_mplan* p = const_cast<tcg_mplan*>(plan);
   ProgramView view;
   int rc = program_device_view(&p->prog, &view);
@@ -580,8 +682,11 @@ int tcg_pauli_accumulate(const tcg_mplan* plan, const void* psi, void* mu, int64
     a.coef = coef;
     a.coef_stride = coef_stride;
     a.max_slots = 0;
+    a.mu_zero = overwrite ? 1 : 0;  // the first pass writes mu instead of adding to it
     rc = run_program(&p->prog, MODE_PACC, kRFwd, a, batch, st);
     if (rc != TCG_OK) return rc;
+  } else if (overwrite) {
+    if (cudaMemsetAsync(mu, 0, state_bytes, st) != cudaSuccess) return TCG_ERR_CUDA;
   }
   if (!p->direct.empty())
     rc = cuda_rc(launch_direct_pacc(static_cast<const float2*>(psi), static_cast<float2*>(mu), plan->n, batch,

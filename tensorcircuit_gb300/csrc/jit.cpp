@@ -192,8 +192,8 @@ class Gen {
   }
   void regs_from_global(std::ostream& o, const Layout& l, bool mu) {
     for (int r = 0; r < NR_; ++r) {
-      o << "      v[" << r << "] = S[gt + " << gr(l, r) << "u];";
-      if (mu) o << " w[" << r << "] = U[gt + " << gr(l, r) << "u];";
+      o << "      v[" << r << "] = Sl[gt + " << gr(l, r) << "u];";
+      if (mu) o << " w[" << r << "] = muz ? czero() : U[gt + " << gr(l, r) << "u];";
       o << "\n";
     }
   }
@@ -214,11 +214,11 @@ class Gen {
     o << "      for (u32 i = tid; i < " << (1u << (L_ - 1)) << "u; i += " << NT_ << "u) {\n";
     o << "        const u32 j = 2u * i; const u32 off = " << off_expr() << ";\n";
     if (psi)
-      o << "        { const float4 q = *reinterpret_cast<const float4*>(S + off); smp[swz(j)] = "
+      o << "        { const float4 q = *reinterpret_cast<const float4*>(Sl + off); smp[swz(j)] = "
            "make_float2(q.x, q.y); smp[swz(j + 1u)] = make_float2(q.z, q.w); }\n";
     if (mu)
-      o << "        { const float4 q = *reinterpret_cast<const float4*>(U + off); smu[swz(j)] = "
-           "make_float2(q.x, q.y); smu[swz(j + 1u)] = make_float2(q.z, q.w); }\n";
+      o << "        { const float4 q = muz ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(U + off); "
+           "smu[swz(j)] = make_float2(q.x, q.y); smu[swz(j + 1u)] = make_float2(q.z, q.w); }\n";
     o << "      }\n";
   }
   void staged_store(std::ostream& o, bool psi, bool mu) {
@@ -782,6 +782,11 @@ class Gen {
       out << "  base |= ((tile >> " << i << ") & 1u) << " << dp_->nlbits[i] << ";\n";
     out << "  float2* __restrict__ S = kp.psi + (unsigned long long)b * " << N << "ull + base;\n";
     if (has_mu_) out << "  float2* __restrict__ U = kp.mu + (unsigned long long)b * " << N << "ull + base;\n";
+    // the first pass of a sweep may read its input state elsewhere, and the
+    // first accumulation pass starts mu at zero
+    out << "  const float2* __restrict__ Sl = kp.psi_in ? kp.psi_in + (unsigned long long)b * (unsigned long long)"
+           "kp.in_stride + base : S;\n  (void)Sl;\n";
+    out << "  const bool muz = kp.mu_zero != 0;\n  (void)muz;\n";
     if (fwd() || bwd()) out << "  const float2* __restrict__ Mt = kp.mats + b * kp.mat_stride;\n";
     out << "  float2* const smp = smem;\n";
     if (has_mu_) out << "  float2* const smu = smem + " << TILE << ";\n";
@@ -1074,6 +1079,7 @@ cudaError_t jit_launch(JitKernels* jk, int pass, const KParams_Host& kp, uint32_
     if (a.mu) a.mu = kp.mu + b0 * len;
     if (a.mats) a.mats = kp.mats + b0 * kp.mat_stride;
     if (a.coef) a.coef = kp.coef + b0 * kp.coef_stride;
+    if (a.psi_in) a.psi_in = kp.psi_in + b0 * kp.in_stride;
     if (a.partial) a.partial = kp.partial + size_t(b0) * kp.part_stride * ntiles;
     void* args[] = {&a};
     count_launch();

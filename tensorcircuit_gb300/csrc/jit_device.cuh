@@ -19,6 +19,10 @@ struct KParams {
   long long part_stride;
   const float* coef;
   long long coef_stride;
+  const float2* psi_in;  // first pass of a sweep: read psi here (may be null)
+  long long in_stride;
+  int mu_zero;           // first pass of an accumulation: mu starts at zero
+  int pad;
 };
 
 namespace tk {

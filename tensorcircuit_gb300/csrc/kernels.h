@@ -28,6 +28,12 @@ struct PassArgs {
   const float* coef;        // PACC: [B][coef_stride]
   int64_t coef_stride;
   int max_slots;
+  // the first pass of a sweep may read its input elsewhere: psi_in
+  // ([B][in_stride], in_stride 0 = one state for every circuit) instead of
+  // psi, and (mu_zero) zeros instead of mu; every pass writes psi / mu
+  const float2* psi_in;
+  int64_t in_stride;
+  int mu_zero;
 };
 
 // Argument block of the specialised (generated) pass kernels; the same
@@ -41,6 +47,10 @@ struct KParams_Host {
   long long part_stride;
   const float* coef;
   long long coef_stride;
+  const float2* psi_in;   // see PassArgs
+  long long in_stride;
+  int mu_zero;
+  int pad;
 };
 
 // ---- uneven batches: many circuits, one persistent launch per sweep.
@@ -123,8 +133,9 @@ cudaError_t launch_tc_fuse(const TcBlock* blocks, int nblocks, const TcGate* gat
                            int64_t mat_stride, int64_t batch, uint8_t* fused, float2* scales, int slots,
                            cudaStream_t st);
 cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const uint32_t* runs_dev,
-                           const TcBlock* blocks_dev, float2* psi, int n, int64_t batch, const uint8_t* fused,
-                           const float2* scales, int slots, unsigned int* err, cudaStream_t st);
+                           const TcBlock* blocks_dev, float2* psi, const float2* psi_in, int64_t in_stride, int n,
+                           int64_t batch, const uint8_t* fused, const float2* scales, int slots, unsigned int* err,
+                           cudaStream_t st);
 cudaError_t launch_tc_mma_probe(const void* A, const void* B, float* D, int K, int N, unsigned int* err,
                                 cudaStream_t st);
 

@@ -755,6 +755,17 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
   float2* mu = HAS_MU ? (A.mu + b * state_len) : nullptr;
   const float2* mats = A.mats ? (A.mats + b * A.mat_stride) : nullptr;
   const uint32_t* runs = A.prog.runs + P.runs_off;
+  // first pass of a sweep: the input state may sit elsewhere (psi_in), and
+  // an accumulation may start mu at zero instead of reading it
+  const float2* psi_ld = A.psi_in ? (A.psi_in + b * A.in_stride) : psi;
+  const bool mu_zero = HAS_MU && A.mu_zero != 0;
+  auto load_mu_smem = [&]() {
+    if (mu_zero) {
+      for (uint32_t j = tid; j < (1u << L); j += nthreads) sm_mu[j] = make_float2(0.f, 0.f);
+    } else {
+      tile_load_smem(sm_mu, mu, base, runs, L, tid, nthreads);
+    }
+  };
 
   float2 v[NR];
   float2 w[NR];  // mu registers; dead (and removed) in modes without mu
@@ -772,8 +783,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
         if (HAS_MU) regs_to_smem<R>(w, sm_mu, ly);
         live = false;
       } else if (!in_smem) {
-        tile_load_smem(sm_psi, psi, base, runs, L, tid, nthreads);
-        if (HAS_MU) tile_load_smem(sm_mu, mu, base, runs, L, tid, nthreads);
+        tile_load_smem(sm_psi, psi_ld, base, runs, L, tid, nthreads);
+        if (HAS_MU) load_mu_smem();
       }
       in_smem = true;
       __syncthreads();
@@ -800,11 +811,18 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
         if (HAS_MU) regs_from_smem<R>(w, sm_mu, ly);
         __syncthreads();
       } else if (S.lanes_low) {
-        regs_from_global<R>(v, psi, base, ly);
-        if (HAS_MU) regs_from_global<R>(w, mu, base, ly);
+        regs_from_global<R>(v, psi_ld, base, ly);
+        if (HAS_MU) {
+          if (mu_zero) {
+#pragma unroll
+            for (int r = 0; r < NR; ++r) w[r] = make_float2(0.f, 0.f);
+          } else {
+            regs_from_global<R>(w, mu, base, ly);
+          }
+        }
       } else {
-        tile_load_smem(sm_psi, psi, base, runs, L, tid, nthreads);
-        if (HAS_MU) tile_load_smem(sm_mu, mu, base, runs, L, tid, nthreads);
+        tile_load_smem(sm_psi, psi_ld, base, runs, L, tid, nthreads);
+        if (HAS_MU) load_mu_smem();
         __syncthreads();
         regs_from_smem<R>(v, sm_psi, ly);
         if (HAS_MU) regs_from_smem<R>(w, sm_mu, ly);
@@ -1253,6 +1271,9 @@ __global__ void __launch_bounds__(256, LITE ? ((MODE == MODE_FWD || MODE == MODE
     A.coef = BL.coef ? BL.coef + C.coef_off : nullptr;
     A.coef_stride = 0;
     A.max_slots = C.max_slots;
+    A.psi_in = nullptr;
+    A.in_stride = 0;
+    A.mu_zero = 0;
     pass_tile<MODE, R, LITE>(A, (uint32_t)(item - sg.item0), 0, sg.ntiles, smem_raw);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1291,6 +1312,7 @@ static cudaError_t launch_one(const PassArgs& a, int L, int64_t batch, cudaStrea
     if (aa.mu) aa.mu = a.mu + b0 * len;
     if (aa.mats) aa.mats = a.mats + b0 * a.mat_stride;
     if (aa.coef) aa.coef = a.coef + b0 * a.coef_stride;
+    if (aa.psi_in) aa.psi_in = a.psi_in + b0 * a.in_stride;
     if (aa.partial) aa.partial = a.partial + size_t(b0) * a.part_stride * ntiles;
     dim3 grid(ntiles, (unsigned)nb);
     count_launch();

@@ -363,6 +363,8 @@ __global__ void __launch_bounds__(256) tc_fuse_kernel(const TcBlock* __restrict_
 // ============================================================================
 struct TcArgs {
   float2* psi;
+  const float2* psi_in;  // first pass of a sweep: input tiles read here (null: psi)
+  int64_t in_stride;
   int n;
   uint32_t ntiles;
   uint32_t nnonlocal;
@@ -446,6 +448,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
   for (uint32_t i = 0; i < a.nnonlocal; ++i)
     if ((tile >> i) & 1u) base |= 1u << a.nlbits[i];
   float2* psi = a.psi + b * ((int64_t)1 << a.n);
+  const float2* psi_ld = a.psi_in ? a.psi_in + b * a.in_stride : psi;
   const uint8_t* fused_b = a.fused + b * a.slots * (int64_t)kTcMatBytes;
   const float2* scales_b = a.scales + b * a.slots;
 
@@ -476,7 +479,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) tc_pass_kernel(const TcArgs a) 
   for (int u = 0; u < kTcLdIter; ++u) {
     const uint32_t j = 2u * (uint32_t)(tid + kTcThreads * u);
     const uint32_t off = __ldg(a.runs + (j >> kLo)) | (j & ((1u << kLo) - 1));
-    xv[u] = __ldcg(reinterpret_cast<const float4*>(psi + (base | off)));
+    xv[u] = __ldcg(reinterpret_cast<const float4*>(psi_ld + (base | off)));
     lmax = fmaxf(lmax, fmaxf(fmaxf(fabsf(xv[u].x), fabsf(xv[u].y)), fmaxf(fabsf(xv[u].z), fabsf(xv[u].w))));
   }
   lmax = warp_max(lmax);
@@ -769,7 +772,8 @@ cudaError_t launch_tc_fuse(const TcBlock* blocks, int nblocks, const TcGate* gat
 }
 
 cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const uint32_t* runs_dev,
-                           const TcBlock* blocks_dev, float2* psi, int n, int64_t batch, const uint8_t* fused,
+                           const TcBlock* blocks_dev, float2* psi, const float2* psi_in, int64_t in_stride, int n,
+                           int64_t batch, const uint8_t* fused,
                            const float2* scales, int slots, unsigned int* err, cudaStream_t st) {
   const cudaError_t ea = set_attrs_once(g_attr_pass, (const void*)tc_pass_kernel, (int)kSmTotal, true);
   if (ea != cudaSuccess) return ea;
@@ -777,6 +781,8 @@ cudaError_t launch_tc_pass(const DevPass& pass, const TcPassDesc& desc, const ui
   if ((int64_t(1) << (n - kTcTileBits)) * batch > int64_t(0x7fffffff)) return cudaErrorInvalidConfiguration;
   TcArgs a;
   a.psi = psi;
+  a.psi_in = psi_in;
+  a.in_stride = in_stride;
   a.n = n;
   a.ntiles = 1u << (n - kTcTileBits);
   a.nnonlocal = (uint32_t)pass.nnonlocal;

@@ -209,6 +209,18 @@ def _flat(t: torch.Tensor, lead: Tuple[int, ...], tail: int) -> torch.Tensor:
     return t.resolve_conj().resolve_neg().expand(lead + (tail,)).reshape(-1, tail)
 
 
+def _input_rows(psi0: torch.Tensor, lead: Tuple[int, ...], tail: int) -> Tuple[torch.Tensor, int]:
+    """Input states as (rows, row stride in complex entries): one row with
+    stride 0 when every circuit starts from the same state, else one row per
+    circuit."""
+    x = psi0.resolve_conj().resolve_neg()
+    if x.dtype != C64:
+        x = x.to(C64)
+    if x.numel() == tail:
+        return x.reshape(tail).contiguous(), 0
+    return _flat(x, lead, tail).contiguous(), tail
+
+
 def _bd(x: Optional[torch.Tensor], d: Optional[int]) -> Optional[torch.Tensor]:
     if x is None or d is None:
         return x
@@ -227,11 +239,18 @@ class StateFn(torch.autograd.Function):
         N = 1 << run.n
         M = mats.shape[-1]
         lead = _lead(mats.shape[:-1], psi0.shape[:-1])
-        psi = _flat(psi0, lead, N).contiguous().clone()
-        B = psi.shape[0]
+        B = int(np.prod(lead)) if lead else 1
         m = _flat(mats, lead, M).contiguous()
         if run.plan.ngates > 0 and B > 0:
-            nat.check(lib.tcg_forward(run.plan.handle, nat.ptr(psi), B, nat.ptr(m), M, _stream()), "forward")
+            # the first pass reads the input rows where they are (one shared
+            # row for a broadcast input such as |0...0>): no copy of the input
+            # into the output buffer first
+            src, stride = _input_rows(psi0, lead, N)
+            psi = torch.empty((B, N), dtype=C64, device=src.device)
+            nat.check(lib.tcg_forward_from(run.plan.handle, nat.ptr(src), stride, nat.ptr(psi), B, nat.ptr(m), M,
+                                           _stream()), "forward")
+        else:
+            psi = _flat(psi0, lead, N).contiguous().clone()
         anchor = torch.zeros(lead, dtype=torch.float32, device=psi.device)
         return psi.reshape(lead + (N,)), anchor
 
@@ -291,25 +310,33 @@ class AdjointFn(torch.autograd.Function):
         if gcoef is not None:
             shapes.append(gcoef.shape[:-1])
         lead = _lead(*shapes)
-        psi_w = _flat(psi, lead, N).contiguous().clone()
-        B = psi_w.shape[0]
+        # the output states are only read (by the accumulation and the first
+        # adjoint pass, which writes the working copy psi_w): no clone
+        psi_out = _flat(psi, lead, N).contiguous()
+        B = psi_out.shape[0]
+        st = _stream()
+        accumulate = gcoef is not None and len(spec) > 0
         if gpsi is not None:
             mu = _flat(gpsi.to(C64), lead, N).contiguous().clone()
+        elif accumulate:
+            mu = torch.empty_like(psi_out)  # the accumulation writes every entry
         else:
-            mu = torch.zeros_like(psi_w)
-        st = _stream()
-        if gcoef is not None and len(spec) > 0:
+            mu = torch.zeros_like(psi_out)
+        if accumulate:
             tp = term_plan(run.n, spec)
             coef = _flat((2.0 * gcoef.real).to(torch.float32), lead, len(spec)).contiguous()
-            nat.check(lib.tcg_pauli_accumulate(tp.handle, nat.ptr(psi_w), nat.ptr(mu), B, nat.ptr(coef),
-                                               len(spec), st), "pauli accumulate")
+            flags = 0 if gpsi is not None else nat.TCG_ACC_OVERWRITE
+            nat.check(lib.tcg_pauli_accumulate_ex(tp.handle, nat.ptr(psi_out), nat.ptr(mu), B, nat.ptr(coef),
+                                                  len(spec), flags, st), "pauli accumulate")
         m = _flat(mats, lead, M).contiguous()
         grads = torch.zeros_like(m)
         if run.plan.ngates > 0 and B > 0:
             nbytes = int(lib.tcg_backward_scratch_bytes(run.plan.handle, B))
-            scratch = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=psi_w.device)
-            nat.check(lib.tcg_backward(run.plan.handle, nat.ptr(psi_w), nat.ptr(mu), B, nat.ptr(m), M,
-                                       nat.ptr(grads), M, nat.ptr(scratch), nbytes, st), "backward")
+            scratch = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=psi_out.device)
+            psi_w = torch.empty_like(psi_out)
+            nat.check(lib.tcg_backward_from(run.plan.handle, nat.ptr(psi_out), nat.ptr(psi_w), nat.ptr(mu), B,
+                                            nat.ptr(m), M, nat.ptr(grads), M, nat.ptr(scratch), nbytes, st),
+                      "backward")
         return grads.reshape(lead + (M,)), mu.reshape(lead + (N,))
 
     @staticmethod
