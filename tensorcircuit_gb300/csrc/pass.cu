@@ -725,6 +725,8 @@ __device__ __forceinline__ bool same_layout(const DevStage& a, const DevStage& b
 // LITE drops the shared-memory stages, 2-qubit dense and diagonal ops: the
 // body of programs made of 1-qubit dense gates, Pauli rotations, Z-rotation
 // runs and Pauli terms needs half the registers.
+constexpr int kKtMax = 256;  // ops per pass with precomputed shear parameters
+
 template <int MODE, int R, bool LITE = false>
 __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int64_t b, uint32_t ntiles,
                                           float2* smem_raw) {
@@ -770,6 +772,35 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
   float2 v[NR];
   float2 w[NR];  // mu registers; dead (and removed) in modes without mu
   uint32_t pneg = 0;  // the tile holds the negative of its true values
+
+  // Shear parameters of the pass's Pauli rotations, computed once per tile
+  // by the whole CTA instead of a reciprocal per thread and rotation: op
+  // (kt_ob + i) has (k, t) at s_kt[i] for an even thread parity (an odd one
+  // negates both); the c < 0 cases' tile sign goes straight into pneg.  Ops
+  // past the table compute their own.
+  __shared__ float2 s_kt[kKtMax];
+  __shared__ uint32_t s_kneg;
+  int kt_ob = 0, kt_n = 0;
+  if (MODE == MODE_FWD || MODE == MODE_BWD) {
+    kt_ob = A.prog.stages[P.stage_begin].op_begin;
+    kt_n = A.prog.stages[P.stage_end - 1].op_end - kt_ob;
+    if (kt_n > kKtMax) kt_n = kKtMax;
+    if (tid == 0) s_kneg = 0u;
+    __syncthreads();
+    for (int i = tid; i < kt_n; i += nthreads) {
+      const DevOp& op = A.prog.ops[kt_ob + i];
+      if (op.kind == OP_PROT) {
+        const float2 cs = ldm(mats + op.mat_off);
+        float qv = ((op.nY & 3) <= 1) ? -cs.y : cs.y;
+        if (MODE == MODE_BWD) qv = -qv;  // the adjoint rotation
+        float k, t;
+        if (gshear_params(cs.x, qv, k, t)) atomicXor(&s_kneg, 1u);
+        s_kt[i] = make_float2(k, t);
+      }
+    }
+    __syncthreads();
+    pneg = s_kneg;
+  }
   bool live = false;     // registers hold the tile
   bool in_smem = false;  // smem holds the tile
   int prev = -1;
@@ -964,7 +995,6 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
           }
         }
       } else if (kind == OP_PROT) {
-        const float2 cs = ldm(mats + op.mat_off);  // (cos phi, sin phi)
         const int sg = __popc(gthr & op.zmask) & 1;
         int zr = 0;
 #pragma unroll
@@ -973,11 +1003,19 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
         // q = (0, -s) (-i)^nY: (0, -s), (-s, 0), (0, s), (s, 0) for nY % 4 = 0..3
         const int ny = op.nY & 3;
         const bool qim = (ny & 1) == 0;
-        float qv = (ny <= 1) ? -cs.y : cs.y;
-        if (sg) qv = -qv;
+        // shear parameters of this rotation (the adjoint's for MODE_BWD)
+        float k, t;
+        if (o - kt_ob < kt_n) {
+          const float2 kt = s_kt[o - kt_ob];
+          k = sg ? -kt.x : kt.x;
+          t = sg ? -kt.y : kt.y;
+        } else {
+          const float2 cs = ldm(mats + op.mat_off);  // (cos phi, sin phi)
+          float qv = (ny <= 1) ? -cs.y : cs.y;
+          if (sg) qv = -qv;
+          pneg ^= gshear_params(cs.x, MODE == MODE_BWD ? -qv : qv, k, t);
+        }
         if (MODE == MODE_FWD) {
-          float k, t;
-          pneg ^= gshear_params(cs.x, qv, k, t);
           dispatch_gshear<R>(op.xreg, qim, v, k, t, zr);
         } else if (MODE == MODE_BWD) {
           if (op.slot >= 0) {
@@ -985,11 +1023,9 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
             float g = dispatch_prot_dot<R>(op.xreg, v, w, zr, qim);
             if (ny == 1 || ny == 2) g = -g;
             if (sg) g = -g;
-            const float t = warp_sum1(g, nl);
-            if (lane == 0) sm_slot[warp * A.max_slots + op.slot] = make_float2(t, 0.f);
+            const float gs = warp_sum1(g, nl);  // (t is the shear parameter)
+            if (lane == 0) sm_slot[warp * A.max_slots + op.slot] = make_float2(gs, 0.f);
           }
-          float k, t;
-          pneg ^= gshear_params(cs.x, -qv, k, t);
           dispatch_gshear2<R>(op.xreg, qim, v, w, k, t, zr);
         }
       } else if (kind == OP_ZRUN) {
