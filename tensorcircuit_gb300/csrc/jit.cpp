@@ -122,6 +122,18 @@ class Gen {
   const char* defer_var_ = nullptr;
   bool straight_ = false;  // op_sig is emitting for straight_ops
   int pi_ = 0;             // pass being emitted
+  // Modes that hold psi only keep two tile buffers in shared memory (smp,
+  // smq): a layout change writes one and reads it back, and the next change
+  // writes the other, so the barrier after the read-back is not needed.
+  // pend_ = the buffer read last with no barrier since (-1: none); a write
+  // into that buffer first takes a barrier.
+  int pend_ = -1;
+  void guard(std::ostream& c, int b) {
+    if (pend_ == b) {
+      c << "      __syncthreads();\n";
+      pend_ = -1;
+    }
+  }
   // rotations of the pass's straight-line stages: matrix offset of (c, s)
   // and the sign of q = +-s, for the kernel prologue's shear table
   std::vector<int64_t> rot_off_;
@@ -176,16 +188,16 @@ class Gen {
         << ") & 1u) << " << dp_->lbits[l.thr_tile[i]] << ";\n";
     o << "      sjt = swz(jt);\n";
   }
-  void regs_from_smem(std::ostream& o, const Layout& l, bool mu) {
+  void regs_from_smem(std::ostream& o, const Layout& l, bool mu, const char* buf = "smp") {
     for (int r = 0; r < NR_; ++r) {
-      o << "      v[" << r << "] = smp[sjt ^ " << host_swz(tr(l, r)) << "u];";
+      o << "      v[" << r << "] = " << buf << "[sjt ^ " << host_swz(tr(l, r)) << "u];";
       if (mu) o << " w[" << r << "] = smu[sjt ^ " << host_swz(tr(l, r)) << "u];";
       o << "\n";
     }
   }
-  void regs_to_smem(std::ostream& o, const Layout& l, bool psi, bool mu) {
+  void regs_to_smem(std::ostream& o, const Layout& l, bool psi, bool mu, const char* buf = "smp") {
     for (int r = 0; r < NR_; ++r) {
-      if (psi) o << "      smp[sjt ^ " << host_swz(tr(l, r)) << "u] = v[" << r << "];";
+      if (psi) o << "      " << buf << "[sjt ^ " << host_swz(tr(l, r)) << "u] = v[" << r << "];";
       if (mu) o << " smu[sjt ^ " << host_swz(tr(l, r)) << "u] = w[" << r << "];";
       o << "\n";
     }
@@ -633,6 +645,7 @@ class Gen {
     rot_off_.clear();
     rot_sq_.clear();
     pi_ = pi;
+    pend_ = -1;
     {
       // Code size: literal straight-line code costs about one op body per
       // op.  The n=20 HEA adjoint's first pass (76 ops holding psi and mu,
@@ -655,13 +668,16 @@ class Gen {
       std::ostringstream c;
       if (S.smem_stage) {
         if (live) {
+          guard(c, 0);
           regs_to_smem(c, cur, true, has_mu_);
           live = false;
         } else if (!in_smem) {
+          guard(c, 0);
           staged_load(c, true, has_mu_);
         }
         in_smem = true;
         c << "      __syncthreads();\n";
+        pend_ = -1;
         for (int oi = S.op_begin; oi < S.op_end; ++oi) {
           const DevOp& op = P_.ops[oi];
           c << "      { const int tb[6] = {" << op.p[0] << ", " << op.p[1] << ", " << op.p[2] << ", " << op.p[3]
@@ -682,23 +698,41 @@ class Gen {
           if (in_smem) {
             regs_from_smem(c, cur, has_mu_);
             c << "      __syncthreads();\n";
+            pend_ = -1;
           } else if (cur.lanes_low) {
             regs_from_global(c, cur, has_mu_);
           } else {
+            guard(c, 0);
             staged_load(c, true, has_mu_);
             c << "      __syncthreads();\n";
             regs_from_smem(c, cur, has_mu_);
-            c << "      __syncthreads();\n";
+            if (has_mu_) {
+              c << "      __syncthreads();\n";
+              pend_ = -1;
+            } else {
+              pend_ = 0;
+            }
           }
           live = true;
           in_smem = false;
         } else if (!same_layout(cur, nl)) {
-          regs_to_smem(c, cur, true, has_mu_);
-          c << "      __syncthreads();\n";
-          cur = nl;
-          layout_code(c, cur);
-          regs_from_smem(c, cur, has_mu_);
-          c << "      __syncthreads();\n";
+          if (has_mu_) {
+            regs_to_smem(c, cur, true, has_mu_);
+            c << "      __syncthreads();\n";
+            cur = nl;
+            layout_code(c, cur);
+            regs_from_smem(c, cur, has_mu_);
+            c << "      __syncthreads();\n";
+          } else {
+            const int wb = pend_ == 0 ? 1 : 0;  // the buffer nobody may still read
+            const char* bn = wb ? "smq" : "smp";
+            regs_to_smem(c, cur, true, false, bn);
+            c << "      __syncthreads();\n";
+            cur = nl;
+            layout_code(c, cur);
+            regs_from_smem(c, cur, false, bn);
+            pend_ = wb;
+          }
         }
         // dense ops keep the loop: straight-line code lets the compiler load
         // several ops' matrices ahead, past the register budget
@@ -790,7 +824,8 @@ class Gen {
     if (fwd() || bwd()) out << "  const float2* __restrict__ Mt = kp.mats + b * kp.mat_stride;\n";
     out << "  float2* const smp = smem;\n";
     if (has_mu_) out << "  float2* const smu = smem + " << TILE << ";\n";
-    out << "  float2* const sms = smem + " << (has_mu_ ? 2 : 1) * TILE << ";\n  (void)sms;\n";
+    if (!has_mu_) out << "  float2* const smq = smem + " << TILE << ";\n  (void)smq;\n";
+    out << "  float2* const sms = smem + " << 2 * TILE << ";\n  (void)sms;\n";
     out << "  float2 v[" << NR_ << "];\n";
     if (has_mu_) out << "  float2 w[" << NR_ << "];\n";
     out << "  u32 jt = 0u, gt = 0u, sjt = 0u;\n  (void)jt; (void)sjt;\n";
@@ -867,6 +902,7 @@ class Gen {
           regs_to_global(out, cur, store_psi, store_mu);
         } else {
           std::ostringstream tmp;
+          guard(tmp, 0);
           regs_to_smem(tmp, cur, store_psi, store_mu);
           out << tmp.str() << "  __syncthreads();\n";
           staged_store(out, store_psi, store_mu);
@@ -1053,7 +1089,9 @@ bool jit_build(const Program& P, int mode, int R, JitKernels* out) {
     const int ms = P.max_slots > 0 ? P.max_slots : 1;
     out->fn.push_back(k);
     out->nthreads.push_back(nt);
-    out->smem.push_back(size_t(has_mu ? 2 : 1) * (size_t(1) << L) * 8 + size_t(nw) * ms * 8);
+    // two tiles: psi and mu, or (modes holding psi only) psi's two buffers
+    (void)has_mu;
+    out->smem.push_back(size_t(2) * (size_t(1) << L) * 8 + size_t(nw) * ms * 8);
   }
   return true;
 }
