@@ -23,6 +23,7 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 20
     for name in names:
         assert hasattr(lib, name), name
+    assert nat.TCG_ACC_OVERWRITE == 1
     bound = {n for n, _, _ in nat.SIGNATURES}
     assert set(names) == bound, set(names) ^ bound
 
@@ -51,4 +52,19 @@ def test_host_side_errors_without_gpu():
     assert lib.tcg_kraus_pick_backward(None, None, None, 0, None, 4, 1, None, None) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_kraus_pick_backward(None, None, None, 2, None, 4, 0, None, None) == nat.TCG_OK
     assert lib.tcg_kraus_pick_backward(None, None, None, 2, None, 4, 5, None, None) == nat.TCG_ERR_INVALID_ARG
+    # sweeps whose first pass reads elsewhere: argument checks come first
+    from tensorcircuit_gb300 import engine as eng
+
+    plan = eng.GatePlan(6, [(nat.TCG_GATE_DENSE, (0,), 0, -1)], 4)
+    fake = ctypes.c_void_p(0x1000)
+    other = ctypes.c_void_p(0x2000)
+    assert lib.tcg_forward_from(None, fake, 0, other, 1, fake, 4, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_forward_from(plan.handle, None, 0, other, 1, fake, 4, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_forward_from(plan.handle, fake, -1, other, 1, fake, 4, None) == nat.TCG_ERR_INVALID_ARG
+    # in place needs the state's own stride (2^6 here)
+    assert lib.tcg_forward_from(plan.handle, fake, 0, fake, 1, fake, 4, None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_forward_from(plan.handle, fake, 0, other, 0, fake, 4, None) == nat.TCG_OK
+    assert lib.tcg_backward_from(plan.handle, None, other, other, 1, fake, 4, None, 0, None, 0,
+                                 None) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_pauli_accumulate_ex(None, fake, other, 1, fake, 1, 0, None) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_launch_count() == 0
