@@ -781,10 +781,11 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
   __shared__ float2 s_kt[kKtMax];
   __shared__ uint32_t s_kneg;
   int kt_ob = 0, kt_n = 0;
-  if (MODE == MODE_FWD || MODE == MODE_BWD) {
+  if ((MODE == MODE_FWD || MODE == MODE_BWD) && P.stage_end > P.stage_begin) {
     kt_ob = A.prog.stages[P.stage_begin].op_begin;
     kt_n = A.prog.stages[P.stage_end - 1].op_end - kt_ob;
     if (kt_n > kKtMax) kt_n = kKtMax;
+    if (kt_n < 0) kt_n = 0;
     if (tid == 0) s_kneg = 0u;
     __syncthreads();
     for (int i = tid; i < kt_n; i += nthreads) {
@@ -1005,7 +1006,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
         const bool qim = (ny & 1) == 0;
         // shear parameters of this rotation (the adjoint's for MODE_BWD)
         float k, t;
-        if (o - kt_ob < kt_n) {
+        if ((unsigned)(o - kt_ob) < (unsigned)kt_n) {
           const float2 kt = s_kt[o - kt_ob];
           k = sg ? -kt.x : kt.x;
           t = sg ? -kt.y : kt.y;
