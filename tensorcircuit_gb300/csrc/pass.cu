@@ -626,6 +626,64 @@ __device__ __forceinline__ float class_pick(const float (&a)[1 << R], int c) {
   }
 }
 
+// Per-entry sums of a Z-run (measured <Z_S> partials or rotation-angle
+// gradients) written to the entries' slots of this warp.  Value of entry e:
+// the Walsh coefficient t[class_e], negated for an odd thread parity.  Full
+// warps reduce eight entries at once by a transpose-reduce (each butterfly
+// step keeps half of the values and sends the other half to the partner
+// lane; lane l ends with entry l >> 2): 9 shuffles per eight entries instead
+// of 40.  Entries without a slot are skipped.
+template <int R>
+__device__ __forceinline__ void zrun_slot_sums(const float (&t)[1 << R], const ZEnt* __restrict__ ze, int k,
+                                               uint32_t gthr, int nl, int lane, float2* wslots) {
+  if (nl < 32) {
+    for (int e = 0; e < k; ++e) {
+      const ZEnt z = ze[e];
+      if (z.slot < 0) continue;
+      float g = class_pick<R>(t, z.zreg);
+      if (__popc(gthr & z.zmask) & 1) g = -g;
+      const float s = warp_sum1(g, nl);
+      if (lane == 0) wslots[z.slot] = make_float2(s, 0.f);
+    }
+    return;
+  }
+  for (int e0 = 0; e0 < k; e0 += 8) {
+    float b[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      float x = 0.f;
+      if (e0 + q < k) {
+        const ZEnt z = ze[e0 + q];
+        if (z.slot >= 0) {
+          x = class_pick<R>(t, z.zreg);
+          if (__popc(gthr & z.zmask) & 1) x = -x;
+        }
+      }
+      b[q] = x;
+    }
+#pragma unroll
+    for (int o = 16, h = 4; o >= 4; o >>= 1, h >>= 1) {
+      const bool up = (lane & o) != 0;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (e < h) {
+          const float keep = up ? b[e + h] : b[e];
+          const float send = up ? b[e] : b[e + h];
+          b[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+      }
+    }
+    float v = b[0];
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    const int my = e0 + (lane >> 2);
+    if ((lane & 3) == 0 && my < k) {
+      const ZEnt z = ze[my];
+      if (z.slot >= 0) wslots[z.slot] = make_float2(v, 0.f);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ tile I/O
 __device__ __forceinline__ void tile_load_smem(float2* sm, const float2* __restrict__ src, uint32_t base,
                                                const uint32_t* runs, int L, int tid, int nthreads) {
@@ -1036,13 +1094,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
 #pragma unroll
           for (int r = 0; r < NR; ++r) t[r] = fmaf(v[r].x, v[r].x, v[r].y * v[r].y);
           add_walsh<R>(t);
-          for (int e = 0; e < op.k; ++e) {
-            const ZEnt ze = A.prog.zents[op.mat_off + e];
-            float g = class_pick<R>(t, ze.zreg);
-            if (__popc(gthr & ze.zmask) & 1) g = -g;
-            const float s = warp_sum1(g, nl);
-            if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = make_float2(s, 0.f);
-          }
+          zrun_slot_sums<R>(t, A.prog.zents + op.mat_off, op.k, gthr, nl, lane, sm_slot + warp * A.max_slots);
         } else if (MODE == MODE_PACC) {
           // mu += (sum_t c_t s_t(x)) psi: class sums, one transform
           float a[NR];
@@ -1079,14 +1131,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs& A, uint32_t tile, int6
 #pragma unroll
               for (int r = 0; r < NR; ++r) t[r] = fmaf(w[r].x, v[r].y, -w[r].y * v[r].x);
               add_walsh<R>(t);
-              for (int e = 0; e < op.k; ++e) {
-                const ZEnt ze = A.prog.zents[op.mat_off + e];
-                if (ze.slot < 0) continue;
-                float g = class_pick<R>(t, ze.zreg);
-                if (__popc(gthr & ze.zmask) & 1) g = -g;
-                const float s = warp_sum1(g, nl);
-                if (lane == 0) sm_slot[warp * A.max_slots + ze.slot] = make_float2(s, 0.f);
-              }
+              zrun_slot_sums<R>(t, A.prog.zents + op.mat_off, op.k, gthr, nl, lane, sm_slot + warp * A.max_slots);
             }
 #pragma unroll
             for (int r = 0; r < NR; ++r) {
