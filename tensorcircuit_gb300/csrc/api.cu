@@ -182,16 +182,28 @@ struct StreamOrderedFree {
 // Runs every pass of a program direction: the specialised kernels when the
 // JIT policy selects them for this plan (see jit.cpp), else the generic
 // pass kernels of pass.cu.
+// dst[b] = src[b * stride] for batch rows of len complex entries: one copy
+// when the rows are contiguous, one per row otherwise (stride 0: a shared row)
+int copy_rows(float2* dst, const float2* src, int64_t stride, size_t len, int64_t batch, cudaStream_t st) {
+  if (stride == int64_t(len))
+    return cudaMemcpyAsync(dst, src, size_t(batch) * len * sizeof(float2), cudaMemcpyDeviceToDevice, st) ==
+                   cudaSuccess
+               ? TCG_OK
+               : TCG_ERR_CUDA;
+  for (int64_t b = 0; b < batch; ++b)
+    if (cudaMemcpyAsync(dst + size_t(b) * len, src + size_t(b) * size_t(stride), len * sizeof(float2),
+                        cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return TCG_ERR_CUDA;
+  return TCG_OK;
+}
+
 int run_program(Program* P, int mode, int R, PassArgs& a, int64_t batch, cudaStream_t st) {
   if ((a.psi_in || a.mu_zero) && !P->passes.empty() && P->passes[0].stage_end == P->passes[0].stage_begin) {
     // a first pass without stages never loads or stores its tiles: put the
     // input where the sweep works in place instead
     const size_t len = size_t(1) << a.n;
     if (a.psi_in) {
-      for (int64_t b = 0; b < batch; ++b)
-        if (cudaMemcpyAsync(a.psi + size_t(b) * len, a.psi_in + size_t(b) * size_t(a.in_stride), len * sizeof(float2),
-                            cudaMemcpyDeviceToDevice, st) != cudaSuccess)
-          return TCG_ERR_CUDA;
+      if (copy_rows(a.psi, a.psi_in, a.in_stride, len, batch, st) != TCG_OK) return TCG_ERR_CUDA;
       a.psi_in = nullptr;
     }
     if (a.mu_zero) {
@@ -461,14 +473,9 @@ int tcg_forward_from(const tcg_plan* plan, const void* psi_in, int64_t in_stride
   const int64_t N = int64_t(1) << plan->n;
   if (psi_in == psi && in_stride != N) return TCG_ERR_INVALID_ARG;
   if (plan->ngates == 0 || psi_in == psi) {
-    if (psi_in != psi) {
-      // no passes: the output is the input, row by row
-      for (int64_t b = 0; b < batch; ++b)
-        if (cudaMemcpyAsync(static_cast<float2*>(psi) + b * N, static_cast<const float2*>(psi_in) + b * in_stride,
-                            size_t(N) * sizeof(float2), cudaMemcpyDeviceToDevice, as_stream(stream)) != cudaSuccess)
-          return TCG_ERR_CUDA;
-      return TCG_OK;
-    }
+    if (psi_in != psi)  // no passes: the output is the input
+      return copy_rows(static_cast<float2*>(psi), static_cast<const float2*>(psi_in), in_stride, size_t(N), batch,
+                       as_stream(stream));
     return tcg_forward(plan, psi, batch, mats, mat_stride, stream);
   }
   if (!mats) return TCG_ERR_INVALID_ARG;

@@ -129,3 +129,22 @@ def test_accumulate_overwrite_equals_zero_then_add(tc):
     with pytest.raises(ValueError):
         nat.check(lib.tcg_pauli_accumulate_ex(tp.handle, psi.data_ptr(), got.data_ptr(), B, coef.data_ptr(),
                                               len(spec), 2, st), "accumulate_ex")
+
+
+def test_forward_from_without_gates_copies_the_input(tc):
+    from tensorcircuit_gb300 import _native as nat
+    from tensorcircuit_gb300 import engine as eng
+
+    lib = nat.load()
+    n, B = 8, 3
+    plan = eng.GatePlan(n, [], 1)
+    st = torch.cuda.current_stream().cuda_stream
+    rows = _rand_states(B, n, 9)
+    one = _rand_states(1, n, 10)[0]
+    mats = torch.zeros(1, dtype=torch.complex64, device="cuda")
+    for src, stride, want in ((rows, 1 << n, rows), (one, 0, one.expand(B, -1))):
+        got = torch.full((B, 1 << n), float("nan"), dtype=torch.complex64, device="cuda")
+        nat.check(lib.tcg_forward_from(plan.handle, src.data_ptr(), stride, got.data_ptr(), B, mats.data_ptr(), 0,
+                                       st), "forward_from")
+        torch.cuda.synchronize()
+        assert torch.equal(got, want)
