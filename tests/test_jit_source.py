@@ -120,3 +120,68 @@ def test_measure_kernels_compile():
     tp = eng.TermPlan(n, tuple(terms))
     check_compiles(tp.handle, 2, 2)
     check_compiles(tp.handle, 2, 3)
+
+
+# ---- shared-memory barrier discipline of the generated kernels -------------
+_BUF = r"(smp|smq|smu)"
+
+
+def _stage_cases(kernel_src):
+    """The stage-entry code of one kernel in execution order (the stage loop
+    runs its cases 0, 1, ...), followed by the code after the loop."""
+    i = kernel_src.index("switch (s) {")
+    j = kernel_src.index("default: break;", i)
+    cases = re.split(r"\n    case \d+: \{", kernel_src[i:j])[1:]
+    tail = kernel_src[kernel_src.rindex("\n  }\n") :]
+    return cases + [tail]
+
+
+def _check_barriers(kernel_src):
+    """A tile buffer is never written while another thread may still be
+    reading it: after a read, the next write to the same buffer comes after
+    a __syncthreads()."""
+    pending = set()
+    for block in _stage_cases(kernel_src):
+        for line in block.split("\n"):
+            if "__syncthreads" in line:
+                pending.clear()
+            if "denseK_smem" in line:
+                buf = re.search(r"denseK_smem<\d+>\(" + _BUF, line).group(1)
+                assert buf not in pending, line
+                pending.add(buf)
+                continue
+            for m in re.finditer(_BUF + r"\[[^\]]*\]\s*=(?!=)", line):
+                assert m.group(1) not in pending, (m.group(1), line)
+            for m in re.finditer(r"=\s*" + _BUF + r"\[|, c = " + _BUF + r"\[", line):
+                pending.add(m.group(1) or m.group(2))
+
+
+def _kernels(handle, which, mode):
+    st, src = nat.jit_info(handle, which, mode, what=1)
+    return re.split(r'extern "C"', src)[1:]
+
+
+def test_tile_buffers_wait_for_readers():
+    """Kernels that hold psi only alternate two tile buffers so a layout
+    change needs one barrier; every write into a buffer must still follow a
+    barrier after the last read of that buffer (forward with register and
+    shared-memory stages, adjoint, measurement)."""
+    n, nl = 20, 8
+    c = templates.apply_hea(cmod.Circuit(n), n, nl, np.zeros(templates.hea_nparams(n, nl)))
+    e = cmod._build_entry(n, c._ops)
+    rng = np.random.default_rng(5)
+    gl = random_gate_list(14, 60, rng)
+    cr = templates.apply_gate_list(cmod.Circuit(14), gl)
+    er = cmod._build_entry(14, cr._ops)
+    terms = [eng.pauli_masks(16, [i], [], []) for i in range(16)]
+    terms += [eng.pauli_masks(16, [], [], [i, i + 1]) for i in range(15)]
+    tp = eng.TermPlan(16, tuple(terms))
+    checked = 0
+    for handle, which, mode in ((e.plan.handle, 0, 0), (e.plan.handle, 1, 1), (er.plan.handle, 0, 0),
+                                (er.plan.handle, 1, 1), (tp.handle, 2, 2), (tp.handle, 2, 3)):
+        for k in _kernels(handle, which, mode):
+            _check_barriers(k)
+            checked += 1
+    assert checked >= 10
+    # the forward kernels do use the second buffer
+    assert any("smq[" in k for k in _kernels(e.plan.handle, 0, 0))
