@@ -90,6 +90,10 @@ struct OpRec {
 // Passes above this size (ops, counted twice when mu is held) share code
 // between stages of the same shape.
 constexpr int kShareOps = 100;
+// Rotations per pass whose shear parameters come from the CTA's table
+// (8 bytes of shared memory and 12 of constant memory each); later ones
+// compute their own.
+constexpr int kRotTable = 1024;
 
 int stage_code_mode() {
   const char* e = std::getenv("TCG_JIT_UNROLL");
@@ -378,7 +382,7 @@ class Gen {
       // (in straight-line stages the body above is replaced below)
       // three in-place shears per component pair; a rotation with cos < 0
       // toggles the tile's sign bit (applied when the tile is stored)
-      if (straight_ && (fwd() || bwd())) {
+      if (straight_ && (fwd() || bwd()) && rot_off_.size() < size_t(kRotTable)) {
         // shear parameters from the CTA's table (the kernel prologue filled
         // it and the tile's sign bit); rec->g0 = the rotation's table index
         rec->g0 = (int)rot_off_.size();
@@ -574,7 +578,7 @@ class Gen {
       else
         c << "      { const OpRec op = {" << r.off << "ll, " << r.sig << ", " << r.slot << ", " << r.g0 << ", " << r.g1
           << ", " << r.zm << "u, " << r.ny << ", " << r.zr << ", " << r.pad << "}; (void)op;";
-      if (fwd() && r.pad && P_.ops[oi].kind != OP_PROT) c << " const float2 csc = ld(Mt + op.off);";
+      if (sig_body_[r.sig].find("csc") != std::string::npos) c << " const float2 csc = ld(Mt + op.off);";
       c << " " << sig_body_[r.sig];
       if (defer_var_) {
         c << " dv[" << dops.size() << "] = " << defer_var_ << ";";
@@ -912,7 +916,8 @@ class Gen {
       }
     }
     out << "}\n";
-    return (recs.size() + srecs.size()) * sizeof(OpRec) + so.size() * sizeof(int);
+    return (recs.size() + srecs.size()) * sizeof(OpRec) + so.size() * sizeof(int) +
+           nrot * (sizeof(long long) + sizeof(float));
   }
 };
 

@@ -113,3 +113,22 @@ def test_jit_expectations(tc, jit_on, n):
     got = c.expectation_ps_batch(specs).cpu().numpy()
     for t, s in enumerate(specs):
         np.testing.assert_allclose(got[t], sv.expectation_ps(psi, n, **s), atol=2e-5)
+
+
+def test_jit_pass_beyond_the_shear_table(tc, jit_on):
+    """One pass holding more rotations than the CTA's shear table (1120 rx
+    rotations of a deep ansatz on 8 qubits): the rotations past the table
+    compute their own shear parameters; the state matches the oracle."""
+    from tensorcircuit_gb300 import _native as nat
+    from tensorcircuit_gb300 import templates
+
+    n, nl = 8, 140
+    params = np.random.default_rng(12).uniform(0, 2 * np.pi, templates.hea_nparams(n, nl))
+    c = templates.apply_hea(tc.Circuit(n), n, nl, params)
+    psi = c.state()
+    run = c._engine_state()[3]
+    assert run.plan.npasses == 1
+    state, log = nat.jit_info(run.plan.handle, 0, 0)
+    assert state == 1, log[-2000:]
+    want = sv.run_circuit(n, templates.hea_gate_list(n, nl, params))
+    np.testing.assert_allclose(psi.cpu().numpy(), want, atol=5e-5)

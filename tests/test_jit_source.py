@@ -185,3 +185,18 @@ def test_tile_buffers_wait_for_readers():
     assert checked >= 10
     # the forward kernels do use the second buffer
     assert any("smq[" in k for k in _kernels(e.plan.handle, 0, 0))
+
+
+def test_long_rotation_pass_compiles():
+    """A pass with more rotations than the CTA's shear table holds (a deep
+    ansatz on few qubits: every gate in one pass) still compiles: rotations
+    past the table compute their own parameters."""
+    n, nl = 8, 140  # 1120 rx rotations (and 140 Z-rotation runs) in one pass
+    c = templates.apply_hea(cmod.Circuit(n), n, nl, np.zeros(templates.hea_nparams(n, nl)))
+    e = cmod._build_entry(n, c._ops)
+    assert e.plan.npasses == 1
+    st, src = nat.jit_info(e.plan.handle, 0, 0, what=1)
+    # table rotations read shk[]; the ones past it compute their parameters
+    assert "shk[op.g0]" in src and "pneg ^= shear_params" in src
+    rc, log = compile_source(src)
+    assert rc == 0, log[-3000:]
