@@ -21,8 +21,28 @@ OBJDIR = os.path.join(HERE, "lib", "obj")
 LIBNAME = "libtcgb300.so"
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["pass.cu", "misc.cu", "api.cu", "plan.cpp", "jit.cpp", "noalloc.cu", "batch.cu", "mlp.cu", "tcpass.cu"]
-HEADERS = ["engine.h", "kernels.h", "plan.h", "jit.h", "jit_device.cuh"]
+SOURCES = ["pass.cu", "pass_inst.cu", "misc.cu", "api.cu", "plan.cpp", "jit.cpp", "noalloc.cu", "batch.cu", "mlp.cu",
+           "tcpass.cu"]
+HEADERS = ["engine.h", "kernels.h", "plan.h", "jit.h", "jit_device.cuh", "pass.cuh"]
+
+# pass_inst.cu is compiled once per kernel family of pass.cuh (mode x body:
+# 0 pass_kernel, 1 batch_kernel full body, 2 batch_kernel light body), so the
+# twelve large kernel bodies compile in parallel.
+_PASS_FAMILIES = [(mode, kind) for mode in range(4) for kind in range(3)]
+
+
+def _units():
+    """(source, object name, extra nvcc flags) for every object of the library."""
+    out = []
+    for src in SOURCES:
+        stem = os.path.splitext(src)[0]
+        if src == "pass_inst.cu":
+            for mode, kind in _PASS_FAMILIES:
+                out.append((src, "%s_m%d_k%d.o" % (stem, mode, kind),
+                            ["-DTCG_PASS_MODE=%d" % mode, "-DTCG_PASS_KIND=%d" % kind]))
+        else:
+            out.append((src, stem + ".o", []))
+    return out
 
 
 def _write_jit_include() -> None:
@@ -65,9 +85,10 @@ def _digest() -> str:
     return h.hexdigest()[:16]
 
 
-def _compile(src: str, nvcc: str, verbose: bool) -> str:
-    obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+def _compile(unit, nvcc: str, verbose: bool) -> str:
+    src, objname, flags = unit
+    obj = os.path.join(OBJDIR, objname)
+    cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *flags,
            "-I", INCLUDE, "-I", OBJDIR, "-c", os.path.join(CSRC, src), "-o", obj]
     if src.endswith(".cpp"):
         cmd[1:1] = ["-x", "cu"]
@@ -90,8 +111,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 return lib_path()
     nvcc = nvcc_path()
     _write_jit_include()
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, nvcc, verbose), SOURCES))
+    units = _units()
+    # the slowest units first, so a machine with fewer cores than units
+    # starts them early
+    order = sorted(range(len(units)), key=lambda i: units[i][0] != "pass_inst.cu")
+    workers = min(len(units), max(2, os.cpu_count() or 2))
+    with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as ex:
+        done = dict(zip(order, ex.map(lambda i: _compile(units[i], nvcc, verbose), order)))
+    objs = [done[i] for i in range(len(units))]
     tmp = lib_path() + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)

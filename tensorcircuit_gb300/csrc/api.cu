@@ -181,7 +181,7 @@ struct StreamOrderedFree {
 
 // Runs every pass of a program direction: the specialised kernels when the
 // JIT policy selects them for this plan (see jit.cpp), else the generic
-// pass kernels of pass.cu.
+// pass kernels of pass.cuh.
 // dst[b] = src[b * stride] for batch rows of len complex entries: one copy
 // when the rows are contiguous, one per row otherwise (stride 0: a shared row)
 int copy_rows(float2* dst, const float2* src, int64_t stride, size_t len, int64_t batch, cudaStream_t st) {

@@ -1,6 +1,6 @@
 // batch.cu — uneven batches: many parameterized circuits of different sizes
 // and depths, value and adjoint gradient of each circuit's Pauli energy, with
-// one persistent launch per sweep (pass.cu: batch_kernel) instead of one
+// one persistent launch per sweep (pass.cuh: batch_kernel) instead of one
 // launch per pass per circuit.
 //
 // One call = eight kernels in a fixed order (a CUDA graph captures it):

@@ -1,5 +1,5 @@
 // engine.h — internal data structures shared by the host planner (plan.cpp)
-// and the CUDA pass kernels (pass.cu).  Not part of the C ABI.
+// and the CUDA pass kernels (pass.cuh).  Not part of the C ABI.
 //
 // Execution model.  A circuit's gate list is cut into PASSES.  A pass holds a
 // set of L "local" amplitude-index bits (the low LO bits always included, so

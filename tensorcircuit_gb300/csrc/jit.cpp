@@ -9,7 +9,7 @@
 // compiled for sm_103a with NVRTC (loaded with dlopen, so the library has no
 // link-time dependency on it), cached as cubins on disk, and loaded with
 // cudaLibraryLoadData.  When NVRTC is missing or a compile fails the caller
-// keeps the generic pass kernels of pass.cu.
+// keeps the generic pass kernels of pass.cuh.
 #include "jit.h"
 
 #include <dlfcn.h>

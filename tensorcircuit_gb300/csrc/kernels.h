@@ -108,6 +108,15 @@ int64_t launch_count();
 
 cudaError_t launch_pass(int mode, int R, const PassArgs& a, int L, int64_t batch, cudaStream_t st);
 
+// The per-family launchers behind launch_pass (one per MODE) and
+// launch_batch (one per MODE and body).  Defined in pass.cuh; each is
+// explicitly instantiated in its own translation unit (pass_inst.cu, compiled
+// once per family) so the large kernel bodies compile in parallel.
+template <int MODE>
+cudaError_t launch_pass_mode(const PassArgs& a, int L, int64_t batch, cudaStream_t st);
+template <int MODE, bool LITE>
+cudaError_t launch_batch_mode(const BatchLaunch& bl, int L, int max_slots, cudaStream_t st);
+
 // partial[b][e][t] (complex64) summed over t in fp64 for the listed entries.
 // out_c64 (complex64) or out_c128 (complex128), one of them non-null.
 cudaError_t launch_reduce_partials(const float2* partial, int64_t part_stride, uint32_t ntiles,

@@ -31,7 +31,7 @@ uint64_t gate_mask(const PGate& g) {
 }
 
 // phys-bank position a tile bit flips under the smem swizzle
-// phys(j) = j ^ (((j >> 5) ^ (j >> 10)) & 31)  (see pass.cu)
+// phys(j) = j ^ (((j >> 5) ^ (j >> 10)) & 31)  (see pass.cuh)
 inline int bankpos(int t) { return t < 5 ? t : (t < 10 ? t - 5 : t - 10); }
 
 struct StageDraft {

@@ -1,7 +1,7 @@
 """CPU replay of the engine's device programs (test infrastructure).
 
 Executes a plan's passes / stages / ops with the same index arithmetic as
-tensorcircuit_gb300/csrc/pass.cu (tile base from the non-local bits, thread
+tensorcircuit_gb300/csrc/pass.cuh (tile base from the non-local bits, thread
 and register bit deposits, register-position gate application, diagonal and
 Pauli sign rules, per-tile accumulator slots), in numpy.  It lets the CPU
 suite check the planner and every index a kernel would touch -- bijective
