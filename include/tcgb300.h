@@ -81,6 +81,9 @@ typedef struct tcg_plan tcg_plan; /* opaque, host side; owns a small device
 typedef struct tcg_plan_opts {
   int32_t tile_bits;     /* local index bits held by one CTA (<=13); 0 = default */
   int32_t max_stage_grad_entries; /* cap on cotangent entries per stage; 0 = default */
+  int32_t zrun_max;      /* fusion width of commuting Z-string rotations: the
+                            longest run applied as one phase op (1..32, 1 = each
+                            rotation on its own); 0 = default (32)          */
 } tcg_plan_opts;
 
 typedef struct tcg_plan_stats {
@@ -320,6 +323,12 @@ typedef struct tcg_ubatch_circuit {
  * circuit's qubit count (the autotuner's knob).  Host arrays are copied. */
 int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int32_t tile_bits,
                       tcg_ubatch** out);
+/* The same with the planner's options: opts->tile_bits as above (required),
+ * opts->zrun_max the Z-rotation fusion width (0 = default), and
+ * opts->max_stage_grad_entries (0 = default).  The batch autotuner searches
+ * tile width and fusion width through this entry point. */
+int tcg_ubatch_create_ex(const tcg_ubatch_circuit* circuits, int32_t ncircuits, const tcg_plan_opts* opts,
+                         tcg_ubatch** out);
 int tcg_ubatch_destroy(tcg_ubatch* batch);
 
 /* nparams_total = sum of nparams (the layout of params and grads: circuit 0's

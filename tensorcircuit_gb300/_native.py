@@ -42,7 +42,7 @@ class TcgGate(ctypes.Structure):
 
 
 class TcgPlanOpts(ctypes.Structure):
-    _fields_ = [("tile_bits", ctypes.c_int32), ("max_stage_grad_entries", ctypes.c_int32)]
+    _fields_ = [("tile_bits", ctypes.c_int32), ("max_stage_grad_entries", ctypes.c_int32), ("zrun_max", ctypes.c_int32)]
 
 
 class TcgPlanStats(ctypes.Structure):
@@ -114,6 +114,8 @@ SIGNATURES = [
     ("tcg_inner_scratch_bytes", _SZ, [_I64, _I64]),
     ("tcg_inner", ctypes.c_int, [_P, _P, _I64, _I64, _P, _P, _SZ, _P]),
     ("tcg_ubatch_create", ctypes.c_int, [ctypes.POINTER(TcgUbatchCircuit), _I32, _I32, ctypes.POINTER(_P)]),
+    ("tcg_ubatch_create_ex", ctypes.c_int,
+     [ctypes.POINTER(TcgUbatchCircuit), _I32, ctypes.POINTER(TcgPlanOpts), ctypes.POINTER(_P)]),
     ("tcg_ubatch_destroy", ctypes.c_int, [_P]),
     ("tcg_ubatch_info", ctypes.c_int, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_SZ)]),
     ("tcg_ubatch_state_offset", _I64, [_P, _I32]),

@@ -122,14 +122,33 @@ class BatchCircuit:
         self.offset = float(offset)
 
 
-_TUNED: Dict[Any, int] = {}
+_TUNED: Dict[Any, Tuple[int, int]] = {}
 _TUNED_LOCK = threading.Lock()
+
+# Candidate tile widths (local index bits per tile: also how many qubits one
+# HBM pass can fuse) and Z-rotation fusion widths (commuting Z-string
+# rotations applied as one phase op; 1 = each on its own, 0 = the default 32).
+TILE_WIDTHS = (12, 11, 10, 9)
+ZRUN_WIDTHS = (0, 16, 8, 1)
+
+
+def _has_zruns(circs: Sequence["BatchCircuit"]) -> bool:
+    """True if some circuit holds two or more Z-string rotations (the only
+    gates the Z-rotation fusion width changes)."""
+    for bc in circs:
+        nz = sum(1 for kind, _q, _mo, _go, codes in bc.gates
+                 if kind == nat.TCG_GATE_PAULI_ROT and all(c == 3 for c in codes))
+        if nz >= 2:
+            return True
+    return False
 
 
 class _Handle:
-    """tcg_ubatch handle with its scratch, for one tile width."""
+    """tcg_ubatch handle with its scratch, for one tile width and one
+    Z-rotation fusion width (0 = the planner's default)."""
 
-    def __init__(self, circs: Sequence[BatchCircuit], tile_bits: int, device: torch.device) -> None:
+    def __init__(self, circs: Sequence[BatchCircuit], tile_bits: int, device: torch.device,
+                 zrun_max: int = 0) -> None:
         lib = nat.load()
         keep: List[Any] = []
         arr = (nat.TcgUbatchCircuit * len(circs))()
@@ -168,10 +187,13 @@ class _Handle:
             a.coef = cf.ctypes.data_as(nat.ctypes.POINTER(nat.ctypes.c_float))
             a.offset = bc.offset
         h = nat.ctypes.c_void_p()
+        opts = nat.TcgPlanOpts(tile_bits=tile_bits, max_stage_grad_entries=0, zrun_max=zrun_max)
         with torch.cuda.device(device):
-            nat.check(lib.tcg_ubatch_create(arr, len(circs), tile_bits, nat.ctypes.byref(h)), "uneven batch")
+            nat.check(lib.tcg_ubatch_create_ex(arr, len(circs), nat.ctypes.byref(opts), nat.ctypes.byref(h)),
+                      "uneven batch")
         self.handle = h
         self.tile_bits = tile_bits
+        self.zrun_max = zrun_max
         npar = nat.ctypes.c_int64(0)
         nst = nat.ctypes.c_int64(0)
         nbytes = nat.ctypes.c_size_t(0)
@@ -218,12 +240,18 @@ class UnevenBatch:
     parameter vectors (float32, length ``nparams_total``) and returns
     ``(energies[C], grads[nparams_total])``.  With ``graph=True`` the call is
     captured into a CUDA graph after one eager call and replayed.
-    ``tile_bits=None`` times every admissible tile width once and keeps the
-    fastest (cached per batch shape for the process).
+    ``tile_bits=None`` leaves the tile width, and unless ``zrun_max`` is
+    given the Z-rotation fusion width too, to the autotuner: it times every
+    admissible tile width at the default fusion width, then the other fusion
+    widths at the fastest tile width, and keeps the fastest pair (cached per
+    batch shape for the process; ``tune_log`` lists
+    ``(tile_bits, zrun_max, ms)``).  A given ``tile_bits`` is used as is,
+    with ``zrun_max`` or the default fusion width (0 = runs of up to 32).
     """
 
     def __init__(self, specs: Sequence[Sequence[Any]], tile_bits: Optional[int] = None, graph: bool = True,
-                 device: Optional[torch.device] = None, wait_limit_ns: Optional[int] = None) -> None:
+                 device: Optional[torch.device] = None, wait_limit_ns: Optional[int] = None,
+                 zrun_max: Optional[int] = None) -> None:
         self.device = device or eng.device()
         self.circuits = [BatchCircuit(*s) for s in specs]
         self.nparams = sum(bc.nparams for bc in self.circuits)
@@ -231,20 +259,30 @@ class UnevenBatch:
         self.graph_enabled = graph
         self._graph: Optional[torch.cuda.CUDAGraph] = None
         nmin = min(bc.n for bc in self.circuits)
-        key = tuple((bc.n, len(bc.gates), bc.nparams, len(bc.terms)) for bc in self.circuits)
+        if zrun_max is not None and not 0 <= int(zrun_max) <= 32:
+            raise ValueError("zrun_max must be in 0..32 (0 = default), got %r" % (zrun_max,))
+        if tile_bits is not None and tile_bits > nmin:
+            raise ValueError("tile_bits %d exceeds the smallest circuit (%d qubits)" % (tile_bits, nmin))
         if tile_bits is None:
+            key = (tuple((bc.n, len(bc.gates), bc.nparams, len(bc.terms)) for bc in self.circuits), zrun_max)
             with _TUNED_LOCK:
-                tile_bits = _TUNED.get(key)
-            if tile_bits is None:
-                tile_bits = self._autotune([L for L in (12, 11, 10, 9) if L <= nmin] or [nmin])
+                tuned = _TUNED.get(key)
+            if tuned is None:
+                Ls = [L for L in TILE_WIDTHS if L <= nmin] or [nmin]
+                if zrun_max is not None:
+                    Zs = [int(zrun_max)]
+                else:
+                    Zs = list(ZRUN_WIDTHS) if _has_zruns(self.circuits) else [0]
+                tuned = self._autotune(Ls, Zs)
                 with _TUNED_LOCK:
-                    _TUNED[key] = tile_bits
+                    _TUNED[key] = tuned
+            tile_bits, zrun_max = tuned
             self.tuned = True
         else:
+            zrun_max = 0 if zrun_max is None else int(zrun_max)
             self.tuned = False
-        if tile_bits > nmin:
-            raise ValueError("tile_bits %d exceeds the smallest circuit (%d qubits)" % (tile_bits, nmin))
-        self.h = _Handle(self.circuits, tile_bits, self.device)
+        self.h = _Handle(self.circuits, tile_bits, self.device, int(zrun_max))
+        self.zrun_max = int(zrun_max)
         if wait_limit_ns is not None:
             # limit of one device-side dependency wait (default 2 s)
             nat.check(nat.load().tcg_ubatch_set_wait_limit(self.h.handle, int(wait_limit_ns)), "wait limit")
@@ -253,14 +291,17 @@ class UnevenBatch:
         self._e = torch.zeros(len(self.circuits), dtype=torch.float32, device=self.device)
         self._g = torch.zeros(max(self.nparams, 1), dtype=torch.float32, device=self.device)
 
-    def _autotune(self, candidates: Sequence[int]) -> int:
+    def _autotune(self, tile_widths: Sequence[int], zrun_widths: Sequence[int]) -> Tuple[int, int]:
+        """Coordinate search: every tile width at the first fusion width, then
+        the other fusion widths at the fastest tile width.  Each candidate is
+        one warm call and the mean of two timed calls (CUDA events)."""
         p = torch.rand(max(self.nparams, 1), device=self.device)
         e = torch.zeros(len(self.circuits), device=self.device)
         g = torch.zeros(max(self.nparams, 1), device=self.device)
-        best, best_t = candidates[0], float("inf")
-        self.tune_log: List[Tuple[int, float]] = []
-        for L in candidates:
-            h = _Handle(self.circuits, L, self.device)
+        self.tune_log: List[Tuple[int, int, float]] = []
+
+        def timed(L: int, z: int) -> float:
+            h = _Handle(self.circuits, L, self.device, z)
             h.run(p, e, g)
             torch.cuda.synchronize(self.device)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -271,10 +312,20 @@ class UnevenBatch:
             torch.cuda.synchronize(self.device)
             h.check()
             t = e0.elapsed_time(e1) / 2
-            self.tune_log.append((L, t))
-            if t < best_t:
-                best, best_t = L, t
+            self.tune_log.append((L, z, t))
             del h
+            return t
+
+        z0 = zrun_widths[0]
+        best, best_t = (tile_widths[0], z0), float("inf")
+        for L in tile_widths:
+            t = timed(L, z0)
+            if t < best_t:
+                best, best_t = (L, z0), t
+        for z in zrun_widths[1:]:
+            t = timed(best[0], z)
+            if t < best_t:
+                best, best_t = (best[0], z), t
         return best
 
     def split(self, flat: torch.Tensor) -> List[torch.Tensor]:

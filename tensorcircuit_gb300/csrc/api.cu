@@ -349,6 +349,8 @@ int tcg_plan_create(int32_t nqubits, const tcg_gate* gates, int32_t ngates, cons
     po.tile_bits_bwd = std::min(opts->tile_bits, kRBwd + 8);
   }
   if (opts && opts->max_stage_grad_entries > 0) po.max_stage_slots = std::max(16, opts->max_stage_grad_entries);
+  if (opts && opts->zrun_max < 0) return TCG_ERR_INVALID_ARG;
+  if (opts && opts->zrun_max > 0) po.zrun_max = std::min(opts->zrun_max, po.zrun_max);
   if (po.tile_bits_fwd < kRFwd + 1 || po.tile_bits_bwd < kRBwd + 1) return TCG_ERR_INVALID_ARG;
   tcg_plan* p = new (std::nothrow) tcg_plan();
   if (!p) return TCG_ERR_OOM;
@@ -358,6 +360,8 @@ int tcg_plan_create(int32_t nqubits, const tcg_gate* gates, int32_t ngates, cons
   p->grad_entries = grad_entries;
   std::vector<PGate> fwd_gates = pg;
   for (PGate& g : fwd_gates) g.grad_off = -1;
+  p->fwd.zrun_max = po.zrun_max;
+  p->bwd.zrun_max = po.zrun_max;
   int rc = build_gate_program(nqubits, fwd_gates, po.tile_bits_fwd, kRFwd, false, po.max_stage_slots, &p->fwd);
   if (rc == TCG_OK) plan_tensor_passes(&p->fwd, fwd_gates);
   if (rc == TCG_OK)

@@ -152,8 +152,19 @@ extern "C" {
 
 int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int32_t tile_bits,
                       tcg_ubatch** out) {
+  tcg_plan_opts o;
+  o.tile_bits = tile_bits;
+  o.max_stage_grad_entries = 0;
+  o.zrun_max = 0;
+  return tcg_ubatch_create_ex(circuits, ncircuits, &o, out);
+}
+
+int tcg_ubatch_create_ex(const tcg_ubatch_circuit* circuits, int32_t ncircuits, const tcg_plan_opts* opts,
+                         tcg_ubatch** out) {
   if (!out) return TCG_ERR_INVALID_ARG;
   *out = nullptr;
+  if (!opts || opts->zrun_max < 0 || opts->max_stage_grad_entries < 0) return TCG_ERR_INVALID_ARG;
+  const int tile_bits = opts->tile_bits;
   if (!circuits || ncircuits < 1 || tile_bits < kRFwd + 2 || tile_bits > kRFwd + 8) return TCG_ERR_INVALID_ARG;
   tcg_ubatch* B = new (std::nothrow) tcg_ubatch();
   if (!B) return TCG_ERR_OOM;
@@ -201,7 +212,8 @@ int tcg_ubatch_create(const tcg_ubatch_circuit* circuits, int32_t ncircuits, int
       }
     tcg_plan_opts po;
     po.tile_bits = tile_bits;
-    po.max_stage_grad_entries = 0;
+    po.max_stage_grad_entries = opts->max_stage_grad_entries;
+    po.zrun_max = opts->zrun_max;
     tcg_plan* plan = nullptr;
     int rc = tcg_plan_create(n, U.gates, U.ngates, &po, &plan);
     if (rc != TCG_OK) {

@@ -142,8 +142,10 @@ int emit_stage(Program* P, DevPass& dp, const StageDraft& sd,
     // transform per thread.
     const bool zterm = (o.kind == OP_EXPECT && o.x == 0);
     if ((o.kind == TCG_GATE_PAULI_ROT && o.x == 0) || zterm) {
+      // rotation runs follow the program's fusion width; term runs the maximum
+      const size_t run_max = zterm ? (size_t)kZRunMax : (size_t)std::max(1, std::min(kZRunMax, P->zrun_max));
       size_t sj = si;
-      while (sj < sd.ops.size() && sj - si < (size_t)kZRunMax) {
+      while (sj < sd.ops.size() && sj - si < run_max) {
         const OpDraft& q = od[sd.ops[sj]];
         if (q.kind != o.kind || q.x != 0) break;
         ++sj;

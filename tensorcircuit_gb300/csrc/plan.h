@@ -29,6 +29,8 @@ struct Program {
   std::vector<ZEnt> zents;       // OP_ZRUN entries
   int max_slots = 0;         // largest stage slot count
   int64_t nout = 0;          // per-circuit accumulator outputs (complex entries)
+  int zrun_max = 32;         // longest run of Z-string rotations fused into one
+                             // OP_ZRUN (1 = none; term runs always up to 32)
 
   // device copy, one per CUDA device, uploaded on first use
   struct DevCopy { void* base = nullptr; ProgramView view{}; };
@@ -56,6 +58,7 @@ struct PlanOpts {
   int tile_bits_fwd = 12;  // 2^(12-4) = 256 threads per CTA
   int tile_bits_bwd = 12;
   int max_stage_slots = 64;
+  int zrun_max = 32;       // fusion width of commuting Z-string rotations
 };
 
 // A planned gate (global-bit form).

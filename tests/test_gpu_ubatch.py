@@ -103,6 +103,38 @@ def test_uneven_batch_tile_widths_agree(tc):
         np.testing.assert_allclose(out[L][1].cpu().numpy(), out[12][1].cpu().numpy(), atol=5e-5)
 
 
+def test_uneven_batch_fusion_widths_match_oracle(tc):
+    """Z-rotation fusion widths 1 (every rzz on its own), 3 and the default
+    (runs of up to 32) give the oracle's energies and gradients, and the
+    autotuner searches both knobs and keeps its fastest candidate."""
+    from tensorcircuit_gb300 import batch, templates
+
+    rng = np.random.default_rng(23)
+    specs, oracles = [], []
+    for n, p in [(8, 2), (12, 3), (10, 1)]:
+        edges = templates.random_regular_graph(3, n, rng)
+        specs.append(batch.qaoa_spec(n, edges, p))
+        oracles.append(lambda prm, n=n, e=edges, p=p: _qaoa_oracle(n, e, p, prm))
+    params = [rng.uniform(0, np.pi, sp[2]).astype(np.float32) for sp in specs]
+    for z in (1, 3, 0):
+        ub = batch.UnevenBatch(specs, tile_bits=8, zrun_max=z, graph=False)
+        assert ub.zrun_max == z and not ub.tuned
+        e, g = ub.value_and_grad(params)
+        ub.check()
+        gs = ub.split(g)
+        for i, (prm, orc) in enumerate(zip(params, oracles)):
+            ve, ge = orc(prm.astype(np.float64))
+            assert abs(e[i].item() - ve) <= 1e-5 * max(1.0, abs(ve)), (z, i, e[i].item(), ve)
+            np.testing.assert_allclose(gs[i].cpu().numpy(), ge, atol=2e-5 * max(1.0, np.abs(ge).max()))
+    batch._TUNED.clear()
+    ub = batch.UnevenBatch(specs, graph=False)
+    assert ub.tuned
+    assert {z for _, z, _ in ub.tune_log} == set(batch.ZRUN_WIDTHS)
+    assert {L for L, _, _ in ub.tune_log} == {8}  # the smallest circuit bounds the tile width
+    fastest = min(ub.tune_log, key=lambda x: x[2])
+    assert (ub.tile_bits, ub.zrun_max) == fastest[:2]
+
+
 def test_uneven_batch_c4_graph_replay_vs_per_circuit_engine(tc):
     """512 QAOA MaxCut circuits, n ~ U{12, 14, ..., 24}, random 3-regular
     graphs, p ~ U{1..6}, gamma, beta ~ U[0, pi): the captured-graph batch
@@ -113,7 +145,8 @@ def test_uneven_batch_c4_graph_replay_vs_per_circuit_engine(tc):
     specs, params = templates.qaoa_uneven_workload(512, seed=5)
     ub = batch.UnevenBatch(specs, graph=True)
     flat = torch.tensor(np.concatenate(params), dtype=torch.float32, device="cuda")
-    e_eager, g_eager = batch.UnevenBatch(specs, tile_bits=ub.tile_bits, graph=False).value_and_grad(flat)
+    e_eager, g_eager = batch.UnevenBatch(specs, tile_bits=ub.tile_bits, zrun_max=ub.zrun_max,
+                                         graph=False).value_and_grad(flat)
     e1, g1 = ub.value_and_grad(flat)
     e2, g2 = ub.value_and_grad(flat)
     ub.check()

@@ -67,4 +67,18 @@ def test_host_side_errors_without_gpu():
     assert lib.tcg_backward_from(plan.handle, None, other, other, 1, fake, 4, None, 0, None, 0,
                                  None) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_pauli_accumulate_ex(None, fake, other, 1, fake, 1, 0, None) == nat.TCG_ERR_INVALID_ARG
+    # planner options: a negative Z-rotation fusion width is refused; the
+    # uneven batch's option entry point checks its options before any work
+    g = (nat.TcgGate * 1)()
+    g[0].kind, g[0].nq, g[0].mat_off, g[0].grad_off = nat.TCG_GATE_DENSE, 1, 0, -1
+    bad = nat.TcgPlanOpts(tile_bits=0, max_stage_grad_entries=0, zrun_max=-1)
+    assert lib.tcg_plan_create(6, g, 1, ctypes.byref(bad), ctypes.byref(h)) == nat.TCG_ERR_INVALID_ARG
+    ok = nat.TcgPlanOpts(tile_bits=0, max_stage_grad_entries=0, zrun_max=1)
+    assert lib.tcg_plan_create(6, g, 1, ctypes.byref(ok), ctypes.byref(h)) == nat.TCG_OK
+    assert lib.tcg_plan_destroy(h) == nat.TCG_OK
+    uc = (nat.TcgUbatchCircuit * 1)()
+    ub = ctypes.c_void_p()
+    assert lib.tcg_ubatch_create_ex(uc, 1, None, ctypes.byref(ub)) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_ubatch_create_ex(uc, 1, ctypes.byref(bad), ctypes.byref(ub)) == nat.TCG_ERR_INVALID_ARG
+    assert lib.tcg_ubatch_create_ex(None, 1, ctypes.byref(ok), ctypes.byref(ub)) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_launch_count() == 0

@@ -245,6 +245,66 @@ def test_zrun_hea_replay_forward_backward(n, nl):
         np.testing.assert_allclose(grads[grad_off].real, want, atol=1e-3, rtol=1e-4)
 
 
+def _plan_with_opts(n, gates, opts):
+    """A plan of the recorded engine gates, built with explicit planner options."""
+    lib = nat.load()
+    arr = (nat.TcgGate * max(len(gates), 1))()
+    for i, g in enumerate(gates):
+        kind, qubits, mat_off, grad_off = g[:4]
+        arr[i].kind, arr[i].nq, arr[i].mat_off, arr[i].grad_off = kind, len(qubits), mat_off, grad_off
+        for j, q in enumerate(qubits):
+            arr[i].qubits[j] = q
+        if len(g) > 4:
+            for j, code in enumerate(g[4]):
+                arr[i].pauli[j] = code
+    h = nat.ctypes.c_void_p()
+    nat.check(lib.tcg_plan_create(n, arr, len(gates), nat.ctypes.byref(opts), nat.ctypes.byref(h)), "plan")
+    return h
+
+
+@pytest.mark.parametrize("zrun_max", [1, 2, 3, 32])
+def test_zrun_fusion_width_replay(zrun_max):
+    """The Z-rotation fusion width (``tcg_plan_opts.zrun_max``, one of the
+    uneven batch's autotuned knobs) only regroups commuting Z rotations: no
+    run is longer than the width (none at all for 1), and the replayed
+    forward states and adjoint cotangents still match the oracle."""
+    n, nl = 10, 3
+    rng = np.random.default_rng(40 + zrun_max)
+    params = rng.uniform(0, 2 * np.pi, templates.hea_nparams(n, nl))
+    gl = templates.hea_gate_list(n, nl, params)
+    c, entry, mats, n_eng = build_host(n, gl)
+    h = _plan_with_opts(n, entry.gates_c, nat.TcgPlanOpts(tile_bits=0, max_stage_grad_entries=0, zrun_max=zrun_max))
+    try:
+        for which in (0, 1):
+            prog = nat.debug_program(h, which)
+            runs = [op.k for op in prog["ops"] if op.kind == 7]
+            if zrun_max == 1:
+                assert runs == []
+            else:
+                assert runs and max(runs) <= zrun_max
+                assert sum(runs) == len(prog["zents"])
+        psi0 = np.zeros(1 << n, np.complex128)
+        psi0[0] = 1
+        np.testing.assert_allclose(Replay(nat.debug_program(h, 0), n).forward(psi0, mats), sv.run_circuit(n, gl),
+                                   atol=2e-6)
+        psi_out = sv.run_circuit(n, gl)
+        mu_out = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+        psi_in, mu_in, grads = Replay(nat.debug_program(h, 1), n).backward(psi_out, mu_out, mats, max(1, mats.size))
+        want_cot, want_mu = oracle_cotangents(n, gl, mu_out)
+        np.testing.assert_allclose(mu_in, want_mu, atol=1e-4)
+        for gi, g in enumerate(entry.gates_c):
+            kind, qubits, mat_off, grad_off = g[:4]
+            z = complex(mats[mat_off])
+            pm = np.ones((1, 1), np.complex128)
+            for code in g[4]:
+                pm = np.kron(pm, sv.gate_matrix("ixyz"[code]))
+            dg = -z.imag * np.eye(pm.shape[0]) - 1j * z.real * pm
+            want = np.sum(np.conj(want_cot[gi]) * dg).real
+            np.testing.assert_allclose(grads[grad_off].real, want, atol=1e-3, rtol=1e-4)
+    finally:
+        nat.load().tcg_plan_destroy(h)
+
+
 def test_zterm_measure_program_replay():
     """Z-string terms (the TFIM's ZZ couplings) are measured as one Walsh-
     Hadamard op per run; the replayed measurement matches the oracle."""
