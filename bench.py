@@ -41,6 +41,16 @@ UNIT = "circuits/s"
 WORKLOAD = "hea_n20_l8_b64_tfim_vvag"
 
 
+def hea_config(n_gpus):
+    """The workload description both arms (engine and reference) report."""
+    from tensorcircuit_gb300 import templates
+
+    return {"workload": WORKLOAD, "n_qubits": N_QUBITS, "layers": N_LAYERS,
+            "params": int(templates.hea_nparams(N_QUBITS, N_LAYERS)), "batch_per_gpu": BATCH,
+            "parallelism": "replicas" if n_gpus > 1 else "single",
+            "l2": "no flush: per-step working set (64 states + 64 cotangents = 1 GiB) exceeds the 129 MB L2"}
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -152,7 +162,7 @@ def cpu_reference(steps, warmup, sample_circuits=1):
             "sample": "%d of the %d circuits per step (labelled torch restatement of the reference "
                       "algorithm: per-gate tensordot + taped AD via torch.func vmap/grad), %d steps" %
                       (sample_circuits, BATCH, steps),
-            "seconds_per_circuit": dt / sample_circuits}
+            "seconds_per_circuit": dt / sample_circuits, "sample_circuits": sample_circuits}
 
 
 def gpu_plain_ad(sample_circuits=8, steps=2):
@@ -187,14 +197,15 @@ def gpu_plain_ad(sample_circuits=8, steps=2):
 def run_reference_arm(args, rank):
     if rank != 0:
         return
-    # about 3 s per step on 16 cores: at most 3 timed and 5 warm-up steps
+    # two circuits per step, about 5 s on 16 cores: at most 3 timed and 2
+    # warm-up steps (the restatement has no compilation to warm up)
     steps = max(1, min(args.steps, 3))
-    warmup = min(args.warmup, 5)
-    cb = cpu_reference(steps, warmup)
+    warmup = min(args.warmup, 2)
+    cb = cpu_reference(steps, warmup, sample_circuits=2)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": "bounded", "threads": cb["cores"]},
+            "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 * cb["sample_circuits"] / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": hea_config(args.gpus),
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -343,17 +354,15 @@ def run_gb300_arm(args, rank, world):
     cpu = None
     plain_ad = None
     if world == 1 and not args.no_cpu:
-        cpu = cpu_reference(steps=1, warmup=1)
+        cpu = cpu_reference(steps=1, warmup=1, sample_circuits=4)  # about 11 s on 16 cores
         plain_ad = gpu_plain_ad()
     line = {
         "metric": METRIC, "value": circ_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_qubits": n, "layers": nl, "params": int(params.shape[1]),
-                   "batch_per_gpu": BATCH, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "no flush: per-step working set (64 states + 64 cotangents = 1 GiB) exceeds the 129 MB L2",
-                   "fwd_passes": plan.npasses, "bwd_passes": nb_pass},
+        "config": hea_config(world),
         "roofline": {"bound": "hbm", "kernel": "pass_kernel<BWD> (adjoint sweep, tcg_backward)",
+                     "passes": nb_pass,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic,
                      "alg_bytes_per_launch": alg_bytes / nb_pass, "ms_per_sweep": ms_bwd,
@@ -684,6 +693,11 @@ def measure_qaoa(args, rank, world, nested=False):
     alg_bwd = st["adjoint"]["alg_bytes"] + st["accumulate"]["alg_bytes"]
     peak, peak_kind = _peaks()
     achieved = alg_total / (ms / 1e3) / 1e9
+    # DRAM bytes of the four sweeps per algorithmic byte, from the capture of
+    # a 64-circuit prefix of the same workload (the sweeps stream every tile
+    # once, so traffic grows with the algorithmic bytes)
+    ratio = _traffic("batch_kernel_traffic_per_alg_byte", True)
+    traffic = float(ratio) * alg_total if ratio is not None else None
     if rank != 0:
         return
     cpu = None if args.no_cpu else cpu_qaoa(specs, params)
@@ -695,12 +709,15 @@ def measure_qaoa(args, rank, world, nested=False):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
         "config": {"workload": QB_WORKLOAD, "circuits": QB_COUNT, "seed": QB_SEED, "n_min": min(ns),
                    "n_max": max(ns), "params": int(ub.nparams), "tile_bits": ub.tile_bits,
+                   "zrun_max": ub.zrun_max,
+                   "autotune": "tile width x Z-rotation fusion width (0 = runs of up to 32, 1 = none); "
+                               "autotune_ms lists [tile_bits, zrun_max, ms per call]",
                    "autotune_ms": getattr(ub, "tune_log", None), "setup_s": setup_s,
                    "state_gib": float(sum(1 << n for n in ns) * 8 / 2 ** 30),
                    "l2": "no flush: the 12 GiB of states exceed the 129 MB L2"},
         "roofline": {"bound": "hbm", "kernel": "batch_kernel (all four persistent sweeps of one step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": None, "alg_bytes_per_step": alg_total,
+                     "peak_source": peak_kind, "traffic": traffic, "alg_bytes_per_step": alg_total,
                      "value_only_ms": ms_val,
                      "adjoint_part": {"ms": ms - ms_val, "alg_bytes": alg_bwd,
                                       "GB_per_s": alg_bwd / max(ms - ms_val, 1e-6) * 1e3 / 1e9},
