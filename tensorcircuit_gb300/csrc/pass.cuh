@@ -233,21 +233,6 @@ __device__ __forceinline__ void dispatch_dense2_bwd(int p0, int p1, float2 (&v)[
 }
 
 // ---------------------------------------------------------------- Pauli terms
-// acc += sum_r conj(v[r]) s(r) v[r ^ X], s(r) = (-1)^(sbase ^ popc(r & zr))
-template <int R, int X>
-__device__ __forceinline__ float2 expect_x(const float2 (&v)[1 << R], int sbase, int zr) {
-  float2 acc = czero();
-#pragma unroll
-  for (int r = 0; r < (1 << R); ++r) {
-    const float2 t = v[r ^ X];
-    const float2 c = make_float2(fmaf(v[r].x, t.x, v[r].y * t.y), fmaf(v[r].x, t.y, -v[r].y * t.x));
-    const int s = (sbase ^ __popc(r & zr)) & 1;
-    acc.x += s ? -c.x : c.x;
-    acc.y += s ? -c.y : c.y;
-  }
-  return acc;
-}
-
 // w[r] += cf * s(r) * v[r ^ X]   (cf complex, includes (-i)^nY and the coefficient)
 template <int R, int X>
 __device__ __forceinline__ void pacc_x(const float2 (&v)[1 << R], float2 (&w)[1 << R], float2 cf,
@@ -266,16 +251,37 @@ __device__ __forceinline__ void pacc_x(const float2 (&v)[1 << R], float2 (&w)[1 
   M(0) M(1) M(2) M(4) M(8) M(16) M(3) M(5) M(9) M(17) M(6) M(10) M(18) M(12) \
   M(20) M(24)
 
+// acc = sum_r conj(v[r]) s(r) v[r ^ x], s(r) = (-1)^(sbase ^ popc(r & zr)).
+// The measurement form: t[r] = v[r ^ x] built by one conditional exchange
+// per register bit of x, then one pass over compile-time indices.  (A switch
+// over the 16 compiled patterns, as the accumulation below uses, gave the
+// measurement kernels a 1 KiB local-memory stack frame, and the uneven
+// batch's measurement sweep 4.8x its algorithmic DRAM bytes, mostly writes.)
 template <int R>
 __device__ __forceinline__ float2 dispatch_expect(int x, const float2 (&v)[1 << R], int sbase, int zr) {
-  float2 r = czero();
-#define TCG_EX(XX) case XX: if ((XX) < (1 << R)) r = expect_x<R, ((XX) < (1 << R) ? (XX) : 0)>(v, sbase, zr); break;
-  switch (x) {
-    TCG_XCASES(TCG_EX)
-    default: break;
+  float2 t[1 << R];
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) t[r] = v[r];
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const bool f = (x >> j) & 1;
+#pragma unroll
+    for (int r = 0; r < (1 << R); ++r)
+      if (!((r >> j) & 1)) {
+        const float2 a = t[r], b = t[r | (1 << j)];
+        t[r] = f ? b : a;
+        t[r | (1 << j)] = f ? a : b;
+      }
   }
-#undef TCG_EX
-  return r;
+  float2 acc = czero();
+#pragma unroll
+  for (int r = 0; r < (1 << R); ++r) {
+    const float2 c = make_float2(fmaf(v[r].x, t[r].x, v[r].y * t[r].y), fmaf(v[r].x, t[r].y, -v[r].y * t[r].x));
+    const int s = (sbase ^ __popc(r & zr)) & 1;
+    acc.x += s ? -c.x : c.x;
+    acc.y += s ? -c.y : c.y;
+  }
+  return acc;
 }
 
 template <int R>
