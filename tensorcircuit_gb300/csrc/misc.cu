@@ -39,8 +39,20 @@ __global__ void reduce_partials_kernel(const float2* __restrict__ partial, int64
   if (ei >= nentries) return;
   const int64_t e = entries ? entries[ei] : ei;  // null: entries 0 .. nentries-1
   const float2* p = partial + (size_t(b) * part_stride + e) * ntiles;
+  // eight loads in flight per lane, summed in a fixed order
   double sx = 0.0, sy = 0.0;
-  for (uint32_t t = lane; t < ntiles; t += 32) {
+  uint32_t t = lane;
+  for (; t + 7 * 32 < ntiles; t += 8 * 32) {
+    float2 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = p[t + k * 32];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      sx += v[k].x;
+      sy += v[k].y;
+    }
+  }
+  for (; t < ntiles; t += 32) {
     const float2 v = p[t];
     sx += v.x;
     sy += v.y;
@@ -205,17 +217,21 @@ constexpr int kScanThreads = 256;
 constexpr int kScanPer = 16;
 constexpr int kScanBlock = kScanThreads * kScanPer;  // 4096 amplitudes
 
-// phase A: block sums
+// phase A: block sums (the 16 loads of a thread are issued before any sum)
 __global__ void sample_blocksum_kernel(const float2* __restrict__ psi, size_t len, uint64_t* bsum,
                                        uint32_t nblocks) {
   const int64_t b = blockIdx.y;
   const float2* s = psi + b * len;
   const size_t beg = size_t(blockIdx.x) * kScanBlock;
-  uint64_t acc = 0;
-  for (int i = threadIdx.x; i < kScanBlock; i += kScanThreads) {
-    const size_t a = beg + i;
-    if (a < len) acc += qamp(s[a]);
+  float2 v[kScanPer];
+#pragma unroll
+  for (int r = 0; r < kScanPer; ++r) {
+    const size_t a = beg + size_t(r) * kScanThreads + threadIdx.x;
+    v[r] = (a < len) ? s[a] : make_float2(0.f, 0.f);
   }
+  uint64_t acc = 0;
+#pragma unroll
+  for (int r = 0; r < kScanPer; ++r) acc += qamp(v[r]);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   __shared__ uint64_t red[kScanThreads / 32];
@@ -258,47 +274,51 @@ __global__ void sample_scan_bsum_kernel(uint64_t* bsum, uint32_t nblocks) {
   }
 }
 
-// phase C: per-amplitude inclusive CDF
+// phase C: per-amplitude inclusive CDF.  The block's 4096 amplitudes are
+// scanned in 16 rounds of 256 consecutive ones: every thread loads its 16
+// amplitudes up front (coalesced), then per round a warp-shuffle scan plus
+// the eight warp totals from shared memory (double-buffered: one barrier per
+// round) give each amplitude its prefix, stored coalesced.  (Integer sums, so
+// any order gives the same bits.  A per-thread scan of 16 consecutive
+// amplitudes in shared memory put every lane of a warp on the same bank:
+// 16-word strides.)
 __global__ void sample_cdf_kernel(const float2* __restrict__ psi, size_t len, const uint64_t* bsum,
                                   uint32_t nblocks, uint64_t* cdf) {
   const int64_t b = blockIdx.y;
   const float2* s = psi + b * len;
   uint64_t* c = cdf + b * len;
   const size_t beg = size_t(blockIdx.x) * kScanBlock;
-  __shared__ uint64_t q[kScanBlock];
-  for (int i = threadIdx.x; i < kScanBlock; i += kScanThreads) {
-    const size_t a = beg + i;
-    q[i] = (a < len) ? qamp(s[a]) : 0ull;
-  }
-  __syncthreads();
-  // each thread scans its contiguous chunk
-  uint64_t loc = 0;
-  const int off = threadIdx.x * kScanPer;
-#pragma unroll
-  for (int i = 0; i < kScanPer; ++i) {
-    loc += q[off + i];
-    q[off + i] = loc;
-  }
-  // exclusive scan of chunk totals across the block (warp shuffles + smem)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint64_t inc = loc;
+  __shared__ uint64_t wsum[2][kScanThreads / 32];
+  float2 v[kScanPer];
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint64_t t = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += t;
+  for (int r = 0; r < kScanPer; ++r) {
+    const size_t a = beg + size_t(r) * kScanThreads + threadIdx.x;
+    v[r] = (a < len) ? s[a] : make_float2(0.f, 0.f);
   }
-  __shared__ uint64_t wsum[kScanThreads / 32];
-  if (lane == 31) wsum[warp] = inc;
-  __syncthreads();
-  uint64_t wpre = 0;
-  for (int w = 0; w < warp; ++w) wpre += wsum[w];
-  const uint64_t excl = bsum[size_t(b) * nblocks + blockIdx.x] + wpre + (inc - loc);
+  uint64_t carry = bsum[size_t(b) * nblocks + blockIdx.x];  // exclusive prefix of the block
 #pragma unroll
-  for (int i = 0; i < kScanPer; ++i) q[off + i] += excl;
-  __syncthreads();
-  for (int i = threadIdx.x; i < kScanBlock; i += kScanThreads) {
-    const size_t a = beg + i;
-    if (a < len) c[a] = q[i];
+  for (int r = 0; r < kScanPer; ++r) {
+    uint64_t x = qamp(v[r]);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    // round r writes buffer r & 1; a thread can reach round r + 2's write only
+    // after every thread passed round r + 1's barrier, i.e. read round r's
+    if (lane == 31) wsum[r & 1][warp] = x;
+    __syncthreads();
+    uint64_t pre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+      const uint64_t t = wsum[r & 1][w];
+      pre += (w < warp) ? t : 0ull;
+      tot += t;
+    }
+    const size_t a = beg + size_t(r) * kScanThreads + threadIdx.x;
+    if (a < len) c[a] = carry + pre + x;
+    carry += tot;
   }
 }
 
