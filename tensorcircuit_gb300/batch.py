@@ -132,6 +132,24 @@ TILE_WIDTHS = (12, 11, 10, 9)
 ZRUN_WIDTHS = (0, 16, 8, 1)
 
 
+def coordinate_search(tile_widths: Sequence[int], zrun_widths: Sequence[int],
+                      timed: Callable[[int, int], float]) -> Tuple[int, int]:
+    """The autotuner's search: ``timed(L, z)`` for every tile width at the
+    first fusion width, then for the other fusion widths at the fastest tile
+    width; returns the fastest ``(L, z)`` (the first one on ties)."""
+    z0 = zrun_widths[0]
+    best, best_t = (tile_widths[0], z0), float("inf")
+    for L in tile_widths:
+        t = timed(L, z0)
+        if t < best_t:
+            best, best_t = (L, z0), t
+    for z in zrun_widths[1:]:
+        t = timed(best[0], z)
+        if t < best_t:
+            best, best_t = (best[0], z), t
+    return best
+
+
 def _has_zruns(circs: Sequence["BatchCircuit"]) -> bool:
     """True if some circuit holds two or more Z-string rotations (the only
     gates the Z-rotation fusion width changes)."""
@@ -252,17 +270,17 @@ class UnevenBatch:
     def __init__(self, specs: Sequence[Sequence[Any]], tile_bits: Optional[int] = None, graph: bool = True,
                  device: Optional[torch.device] = None, wait_limit_ns: Optional[int] = None,
                  zrun_max: Optional[int] = None) -> None:
-        self.device = device or eng.device()
+        if zrun_max is not None and not 0 <= int(zrun_max) <= 32:
+            raise ValueError("zrun_max must be in 0..32 (0 = default), got %r" % (zrun_max,))
         self.circuits = [BatchCircuit(*s) for s in specs]
+        nmin = min(bc.n for bc in self.circuits)
+        if tile_bits is not None and tile_bits > nmin:
+            raise ValueError("tile_bits %d exceeds the smallest circuit (%d qubits)" % (tile_bits, nmin))
+        self.device = device or eng.device()
         self.nparams = sum(bc.nparams for bc in self.circuits)
         self.offsets = np.cumsum([0] + [bc.nparams for bc in self.circuits])
         self.graph_enabled = graph
         self._graph: Optional[torch.cuda.CUDAGraph] = None
-        nmin = min(bc.n for bc in self.circuits)
-        if zrun_max is not None and not 0 <= int(zrun_max) <= 32:
-            raise ValueError("zrun_max must be in 0..32 (0 = default), got %r" % (zrun_max,))
-        if tile_bits is not None and tile_bits > nmin:
-            raise ValueError("tile_bits %d exceeds the smallest circuit (%d qubits)" % (tile_bits, nmin))
         if tile_bits is None:
             key = (tuple((bc.n, len(bc.gates), bc.nparams, len(bc.terms)) for bc in self.circuits), zrun_max)
             with _TUNED_LOCK:
@@ -316,17 +334,7 @@ class UnevenBatch:
             del h
             return t
 
-        z0 = zrun_widths[0]
-        best, best_t = (tile_widths[0], z0), float("inf")
-        for L in tile_widths:
-            t = timed(L, z0)
-            if t < best_t:
-                best, best_t = (L, z0), t
-        for z in zrun_widths[1:]:
-            t = timed(best[0], z)
-            if t < best_t:
-                best, best_t = (best[0], z), t
-        return best
+        return coordinate_search(tile_widths, zrun_widths, timed)
 
     def split(self, flat: torch.Tensor) -> List[torch.Tensor]:
         return [flat[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self.circuits))]

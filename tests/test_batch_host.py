@@ -68,3 +68,47 @@ def test_uneven_workload_shape():
     assert all(n % 2 == 0 and 12 <= n <= 24 for n in ns)
     assert all(1 <= s[2] // 2 <= 6 and len(p) == s[2] for s, p in zip(specs, params))
     assert all(0 <= x < np.pi for p in params for x in p)
+
+
+def test_autotune_coordinate_search():
+    """Every tile width at the first fusion width, then the other fusion
+    widths at the fastest tile width; the fastest pair wins, ties keep the
+    first candidate."""
+    cost = {(12, 0): 5.0, (11, 0): 4.0, (10, 0): 6.0, (11, 16): 3.5, (11, 8): 3.9, (11, 1): 9.0}
+    calls = []
+
+    def timed(L, z):
+        calls.append((L, z))
+        return cost[(L, z)]
+
+    assert batch.coordinate_search([12, 11, 10], [0, 16, 8, 1], timed) == (11, 16)
+    assert calls == [(12, 0), (11, 0), (10, 0), (11, 16), (11, 8), (11, 1)]
+    # a single fusion width tunes the tile width only
+    calls.clear()
+    assert batch.coordinate_search([12, 11, 10], [0], timed) == (11, 0)
+    assert calls == [(12, 0), (11, 0), (10, 0)]
+    # ties keep the earlier candidate
+    assert batch.coordinate_search([9, 8], [0, 4], lambda L, z: 1.0) == (9, 0)
+
+
+def test_fusion_width_tuned_only_with_z_runs():
+    """The Z-rotation fusion width changes only circuits with two or more
+    Z-string rotations; batches without them tune the tile width alone."""
+    rng = np.random.default_rng(3)
+    qaoa = batch.BatchCircuit(*batch.qaoa_spec(8, templates.random_regular_graph(3, 8, rng), 1))
+    assert batch._has_zruns([qaoa])
+
+    def build(c, params):
+        c.rx(0, theta=params[0])
+        c.rzz(1, 2, theta=params[1])
+        c.ry(3, theta=params[0])
+
+    single = batch.BatchCircuit(8, build, 2, [(1.0, {"z": [0]})])
+    assert not batch._has_zruns([single])
+    assert batch.ZRUN_WIDTHS[0] == 0 and 1 in batch.ZRUN_WIDTHS
+    # argument checks come before any device work
+    spec = batch.qaoa_spec(8, templates.random_regular_graph(3, 8, rng), 1)
+    with pytest.raises(ValueError):
+        batch.UnevenBatch([spec], tile_bits=8, zrun_max=33)
+    with pytest.raises(ValueError):
+        batch.UnevenBatch([spec], tile_bits=9)  # wider than the 8-qubit circuit
