@@ -281,7 +281,9 @@ size_t tcg_inner_scratch_bytes(int64_t len, int64_t batch);
 
 /* ---- misc ------------------------------------------------------------------ */
 const char* tcg_status_string(int32_t status);
-/* 2: tcg_gate gained `pauli` (Pauli-rotation gates); uneven batches added. */
+/* 2: tcg_gate gained `pauli` (Pauli-rotation gates); uneven batches added.
+ * 3: tcg_plan_opts gained `zrun_max` (its size changed: callers built against
+ *    an older header must rebuild); tcg_ubatch_create_ex added. */
 int32_t tcg_abi_version(void);
 
 /* ---- uneven batches --------------------------------------------------------

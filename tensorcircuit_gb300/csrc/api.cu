@@ -17,7 +17,7 @@ using namespace tcg;
 
 namespace {
 
-constexpr int kAbiVersion = 2;
+constexpr int kAbiVersion = 3;
 
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 

@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_status_strings_and_version():
     lib = nat.load()
-    assert lib.tcg_abi_version() == 2
+    assert lib.tcg_abi_version() == 3
     assert lib.tcg_status_string(0) == b"ok"
     assert b"twice" in lib.tcg_status_string(2)
 
