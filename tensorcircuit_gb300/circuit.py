@@ -1179,10 +1179,7 @@ class Circuit:
         the engine's probability kernel (computed as re^2 + im^2; the
         reference squares abs(psi), which can differ in the last bit),
         differentiable through its autograd Function."""
-        s = self.wavefunction()
-        if s.is_cuda:
-            return eng.ProbabilityFn.apply(s)
-        return torch.abs(s) ** 2
+        return eng.ProbabilityFn.apply(self.wavefunction())
 
     def amplitude(self, l: Union[str, Tensor]) -> Tensor:
         """<l|psi> for a bitstring (basecircuit.py:447-508)."""

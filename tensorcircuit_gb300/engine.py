@@ -574,7 +574,10 @@ class ProbabilityFn(torch.autograd.Function):
 
 
 def probability_native(psi: torch.Tensor) -> torch.Tensor:
-    """|psi|^2 through the engine kernel (no autograd)."""
+    """|psi|^2 through the engine kernel (no autograd).  The state must be a
+    CUDA tensor: the engine has no CPU path."""
+    if not psi.is_cuda:
+        raise RuntimeError("probability: the state must be a CUDA tensor (the engine has no CPU path)")
     lib = nat.load()
     p = torch.empty(psi.shape, dtype=torch.float32, device=psi.device)
     src = psi.detach().resolve_conj().resolve_neg().contiguous()

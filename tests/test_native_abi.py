@@ -5,6 +5,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from tensorcircuit_gb300 import _native as nat
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -81,4 +83,10 @@ def test_host_side_errors_without_gpu():
     assert lib.tcg_ubatch_create_ex(uc, 1, None, ctypes.byref(ub)) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_ubatch_create_ex(uc, 1, ctypes.byref(bad), ctypes.byref(ub)) == nat.TCG_ERR_INVALID_ARG
     assert lib.tcg_ubatch_create_ex(None, 1, ctypes.byref(ok), ctypes.byref(ub)) == nat.TCG_ERR_INVALID_ARG
+    # the probability kernel takes device states only: a host tensor is refused
+    # before anything reaches the library
+    import torch
+
+    with pytest.raises(RuntimeError, match="CUDA tensor"):
+        eng.probability_native(torch.zeros(8, dtype=torch.complex64))
     assert lib.tcg_launch_count() == 0
