@@ -281,6 +281,10 @@ def check(status: int, what: str = "") -> None:
 
 
 def ptr(t: Any) -> int:
+    """Device address of a tensor handed to a kernel entry point."""
+    # a host address must never reach a kernel
+    if not t.is_cuda:
+        raise ValueError("a host tensor reached a device entry point of the engine; move it to the GPU first")
     # a lazily conjugated / negated view shares the raw buffer of its base:
     # the kernels would read the unconjugated values
     if t.is_conj() or t.is_neg():

@@ -89,4 +89,7 @@ def test_host_side_errors_without_gpu():
 
     with pytest.raises(RuntimeError, match="CUDA tensor"):
         eng.probability_native(torch.zeros(8, dtype=torch.complex64))
+    # and no host tensor's address is handed to a kernel entry point
+    with pytest.raises(ValueError, match="host tensor"):
+        nat.ptr(torch.zeros(4))
     assert lib.tcg_launch_count() == 0
