@@ -79,7 +79,8 @@ typedef struct tcg_plan tcg_plan; /* opaque, host side; owns a small device
                                      copy of its pass program               */
 
 typedef struct tcg_plan_opts {
-  int32_t tile_bits;     /* local index bits held by one CTA (<=13); 0 = default */
+  int32_t tile_bits;     /* local index bits held by one CTA, 5..12 (larger values
+                            are clamped to 12: 256 threads per CTA); 0 = 12 */
   int32_t max_stage_grad_entries; /* cap on cotangent entries per stage; 0 = default */
   int32_t zrun_max;      /* fusion width of commuting Z-string rotations: the
                             longest run applied as one phase op (1..32, 1 = each
