@@ -113,8 +113,11 @@ int tcg_plan_get_stats(const tcg_plan* plan, tcg_plan_stats* out);
  * tile as a complex GEMM on the tensor cores (tcgen05, fp16 hi/lo operand
  * split, fp32 accumulation).  Which passes do so follows the environment
  * variable TCG_TC (0 none, 1 every pass that qualifies, unset the passes the
- * planner's cost model prefers).  The plan then keeps one device buffer per
- * device for a call's fused matrices (grown when a call's batch is larger).
+ * planner's cost model prefers).  A call with such passes takes its fused
+ * matrices (32 KiB per block and circuit) from a stream-ordered allocation on
+ * its own stream, from a library memory pool per device that keeps up to
+ * 1 GiB between calls, and frees it in stream order when it returns (under
+ * stream capture the allocation becomes the graph's own memory nodes).
  * tcg_plan_tensor_passes returns how many forward passes take that path. */
 int tcg_plan_tensor_passes(const tcg_plan* plan);
 /* Sets the policy TCG_TC selects (0, 1 or 2 = cost model) for later calls of
