@@ -424,15 +424,26 @@ def cpu_brickwall(n_cpu=22):
 
     threads = len(os.sched_getaffinity(0))
     gl = templates.brickwall_gate_list(n_cpu, BW_DEPTH, BW_SEED)
+    scale = float(1 << (BW_N - n_cpu))
     ra.run_gate_list(n_cpu, gl[:4], threads)
     t0 = time.perf_counter()
     ra.run_gate_list(n_cpu, gl, threads)
     dt = time.perf_counter() - t0
-    scale = float(1 << (BW_N - n_cpu))
-    return {"value": len(gl) / dt / scale, "unit": BW_UNIT, "cores": threads, "kind": "port",
-            "sample": "brick wall depth %d at n=%d (%d gates, %.2f s; labelled torch restatement of the "
-                      "reference's per-gate tensordot), scaled by 2^%d amplitudes to n=%d" %
-                      (BW_DEPTH, n_cpu, len(gl), dt, BW_N - n_cpu, BW_N)}
+    # the numpy backend's form of the same contraction (numpy.tensordot per
+    # gate), reported beside it; the value is the faster of the two
+    try:
+        t0 = time.perf_counter()
+        ra.run_gate_list_numpy(n_cpu, gl)
+        dt_np = time.perf_counter() - t0
+        numpy_form = {"value": len(gl) / dt_np / scale, "seconds": dt_np}
+    except Exception as exc:  # reported, never fatal for the bench line
+        dt_np, numpy_form = float("inf"), {"unavailable": "%s: %s" % (type(exc).__name__, str(exc)[:200])}
+    best = min(dt, dt_np)
+    return {"value": len(gl) / best / scale, "unit": BW_UNIT, "cores": threads, "kind": "port",
+            "sample": "brick wall depth %d at n=%d (%d gates; labelled restatements of the reference's "
+                      "per-gate tensordot: torch %.2f s, numpy %.2f s, the faster counts), scaled by 2^%d "
+                      "amplitudes to n=%d" % (BW_DEPTH, n_cpu, len(gl), dt, dt_np, BW_N - n_cpu, BW_N),
+            "torch_form": {"value": len(gl) / dt / scale, "seconds": dt}, "numpy_form": numpy_form}
 
 
 def run_brickwall(args, rank, world):

@@ -100,6 +100,24 @@ def run_gate_list(n: int, gl: Sequence[Tuple[str, Tuple[int, ...], Dict[str, Any
     return psi.reshape(-1)
 
 
+def run_gate_list_numpy(n: int, gl: Sequence[Tuple[str, Tuple[int, ...], Dict[str, Any]]]) -> np.ndarray:
+    """The same forward contraction on numpy arrays: one ``numpy.tensordot``
+    per gate in circuit order on a complex64 state, as the reference's numpy
+    backend runs it (tensorcircuit/backends/numpy_backend.py:12-16 builds on
+    tensornetwork's NumPy backend, whose tensordot is ``numpy.tensordot``;
+    the plain contractor's order, tensorcircuit/cons.py:334-370)."""
+    psi = np.zeros([2] * n, dtype=np.complex64)
+    psi.reshape(-1)[0] = 1.0
+    for name, q, p in gl:
+        if name not in ("any", "unitary"):
+            raise NotImplementedError(name)
+        k = len(q)
+        g = np.asarray(p["unitary"], dtype=np.complex64).reshape([2] * (2 * k))
+        out = np.tensordot(g, psi, axes=(list(range(k, 2 * k)), list(q)))
+        psi = np.moveaxis(out, list(range(k)), list(q))
+    return np.ascontiguousarray(psi).reshape(-1)
+
+
 def _exp1_zz(theta: torch.Tensor) -> torch.Tensor:
     """exp1(ZZ, theta) = cos(theta) I - i sin(theta) ZZ (tensorcircuit/gates.py:825-846, half=False)."""
     c = torch.cos(theta).to(C64)

@@ -178,3 +178,32 @@ def test_device_oracle_random_circuits_and_adjoint():
     v1, g1 = dv.value_and_grad_adjoint(n, ops, pidx, params, terms, "cpu")
     assert abs(v0 - v1) < 1e-12
     np.testing.assert_allclose(g1, g0, atol=1e-9)
+
+
+def test_cpu_baseline_restatements_match_oracle():
+    """The timed CPU baselines compute what the oracle computes: the per-gate
+    tensordot restatements (torch and numpy forms) of a Haar brick wall, and
+    the taped-AD value+gradient of the HEA energy."""
+    import torch
+
+    from oracle import reference_algo as ra
+    from tensorcircuit_gb300 import templates
+
+    threads0 = torch.get_num_threads()  # the restatements set torch's thread count
+    n = 9
+    gl = templates.brickwall_gate_list(n, 6, 11)
+    want = sv.run_circuit(n, gl)
+    np.testing.assert_allclose(ra.run_gate_list_numpy(n, gl), want, atol=2e-6)
+    np.testing.assert_allclose(ra.run_gate_list(n, gl, 2).numpy(), want, atol=2e-6)
+    nl = 2
+    layout = templates.hea_layout(n, nl)
+    terms = templates.tfim_terms(n, -1.0, -1.0)
+    params = np.random.default_rng(5).uniform(0, 2 * np.pi, (2, templates.hea_nparams(n, nl))).astype(np.float32)
+    v, g = ra.vvag_hea(n, layout, terms, params, 2)
+    ops = [(name, q, {"theta": 0.0}) for name, q, _ in layout]
+    pidx = [k for _, _, k in layout]
+    for b in range(2):
+        ve, ge = sv.value_and_grad_adjoint(n, ops, pidx, params[b].astype(np.float64), terms)
+        assert abs(v[b] - ve) < 1e-4
+        np.testing.assert_allclose(g[b], ge, atol=1e-4)
+    torch.set_num_threads(threads0)
