@@ -78,6 +78,31 @@ KATS = [
     # abstractcircuit.py docstring of expectation_ps (:1221-1225)
     dict(id="doc_xh", src="tensorcircuit/abstractcircuit.py:1221-1225", n=2,
          ops=[("x", (0,), {}), ("h", (1,), {})], query=("ps", dict(x=[1], z=[0])), expect=-1.0, atol=1e-5),
+    # tests/test_circuit.py:240-245 -- <Z0> after H
+    dict(id="h_z0", src="tests/test_circuit.py:240-245", n=2, ops=[("h", (0,), {})],
+         query=("expect_ops", [("z", [0])]), expect=0.0, atol=1e-7),
+    # tests/test_circuit.py:319-323 -- one-qubit state
+    dict(id="single_h_state", src="tests/test_circuit.py:319-323", n=1, ops=[("h", (0,), {})],
+         query=("state",), expect=np.array([1, 1]) * S2, atol=1e-4),
+    # tests/test_circuit.py:371-390 -- X on given input states
+    dict(id="inputs_11_x_z0", src="tests/test_circuit.py:372-375", n=2, inputs=np.array([0.0, 0.0, 0.0, 1.0]),
+         ops=[("x", (0,), {})], query=("expect_ops", [("z", [0])]), expect=1.0, atol=0.0),
+    dict(id="inputs_10_x_z0", src="tests/test_circuit.py:376-379", n=2, inputs=np.array([0.0, 0.0, 1.0, 0.0]),
+         ops=[("x", (0,), {})], query=("expect_ops", [("z", [0])]), expect=1.0, atol=0.0),
+    dict(id="inputs_00_x_z0", src="tests/test_circuit.py:380-383", n=2, inputs=np.array([1.0, 0.0, 0.0, 0.0]),
+         ops=[("x", (0,), {})], query=("expect_ops", [("z", [0])]), expect=-1.0, atol=0.0),
+    dict(id="inputs_plus_x_z0", src="tests/test_circuit.py:384-390", n=2, inputs=np.array([S2, 0.0, S2, 0.0]),
+         ops=[("x", (0,), {})], query=("expect_ops", [("z", [0])]), expect=0.0, atol=1e-4),
+    # tests/test_circuit.py:584-589 -- state after x(1), cnot(0, 1)
+    dict(id="x1_cnot_state", src="tests/test_circuit.py:587-589", n=2,
+         ops=[("x", (1,), {}), ("cnot", (0, 1), {})], query=("state",),
+         expect=np.array([0, 1.0, 0, 0]), atol=1e-5),
+    # tests/test_circuit.py:707-727 -- a circuit rebuilt from its qir and the
+    # same qir appended once more: <Z1> of the doubled gate list
+    dict(id="toqir_append_z1", src="tests/test_circuit.py:707-727", n=3,
+         ops=[("h", (0,), {}), ("rx", (1,), {"theta": 0.7}),
+              ("exp1", (0, 1), {"unitary": np.diag([1.0, -1.0, -1.0, 1.0]), "theta": -0.2})] * 2,
+         query=("expect_ops", [("z", [1])]), expect=0.202728, atol=1e-5),
 ]
 
 # tests/test_circuit.py:1392-1406 -- a 4-qubit circuit whose sampled and
