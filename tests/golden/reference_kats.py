@@ -105,6 +105,36 @@ KATS = [
          query=("expect_ops", [("z", [1])]), expect=0.202728, atol=1e-5),
 ]
 
+# Gate conventions from the reference's gate tests (tests/test_gates.py).
+# Checked on the oracle and, through the engine's planner and the CPU replay
+# of its device programs, on the engine's own program (tests/
+# test_oracle_kats.py, tests/test_plan_replay.py).
+_WROOT = np.array([[1, -np.sqrt(1j)], [np.sqrt(-1j), 1]]) * S2  # tensorcircuit/gates.py:39-43
+_OCX = np.eye(8, dtype=np.complex128)  # ocontrolled(cx) on (1, 0, 2): CX on (0, 2) when qubit 1 is 0
+_OCX[:4, :4] = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]])
+GATE_KATS = [
+    dict(id="phase_h", src="tests/test_gates.py:18-22", n=1,
+         ops=[("h", (0,), {}), ("phase", (0,), {"theta": np.pi / 2})],
+         query=("amp_complex", 1), expect=0.7071j, atol=1e-4),
+    dict(id="cu_block", src="tests/test_gates.py:25-31", n=2, inputs=np.eye(4).reshape(-1),
+         ops=[("cu", (0, 1), {"theta": np.pi / 2, "phi": -np.pi / 4, "lbd": np.pi / 4})],
+         query=("state4x4",),
+         expect=np.block([[np.eye(2), np.zeros((2, 2))], [np.zeros((2, 2)), _WROOT]]), atol=1e-5),
+    dict(id="fsim", src="tests/test_gates.py:61-77", n=2, inputs=np.eye(4).reshape(-1),
+         ops=[("iswap", (0, 1), {"theta": -0.2}), ("cphase", (0, 1), {"theta": -0.3})],
+         query=("state4x4",),
+         expect=np.array([[1.0, 0, 0, 0], [0, 0.95105654, -0.309017j, 0], [0, -0.309017j, 0.95105654, 0],
+                          [0, 0, 0, 0.9553365 - 0.29552022j]]), atol=1e-5),
+    dict(id="exp_zz", src="tests/test_gates.py:80-90", n=2,
+         ops=[("exp", (0, 1), {"unitary": np.diag([1.0, -1.0, -1.0, 1.0]), "theta": np.pi / 2})],
+         query=("amp_complex", 0), expect=-1j, atol=1e-6),
+    dict(id="any_eye_z0", src="tests/test_gates.py:93-96", n=2, ops=[("any", (0,), {"unitary": np.eye(2)})],
+         query=("expect_ops", [("z", [0])]), expect=1.0, atol=1e-7),
+    dict(id="ocx_z2", src="tests/test_gates.py:111-124", n=3,
+         ops=[("x", (0,), {}), ("any", (1, 0, 2), {"unitary": _OCX})],
+         query=("expect_ops", [("z", [2])]), expect=-1.0, atol=1e-5),
+]
+
 # tests/test_circuit.py:1392-1406 -- a 4-qubit circuit whose sampled and
 # exact Pauli expectations must agree (exact within 1e-5, 81920 shots
 # within 0.01); the value itself is not asserted by the reference.

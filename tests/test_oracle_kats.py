@@ -24,6 +24,8 @@ def _query(case, psi, ntot):
         return psi[q[1]].real
     if q[0] == "bitstring":
         return psi[int(q[1], 2)].real
+    if q[0] == "amp_complex":
+        return psi[q[1]]
     if q[0] == "state":
         return psi
     if q[0] == "state4x4":
@@ -47,6 +49,13 @@ def _query(case, psi, ntot):
 
 @pytest.mark.parametrize("case", K.KATS, ids=[c["id"] for c in K.KATS])
 def test_oracle_matches_reference_kat(case):
+    psi, ntot = _oracle_state(case)
+    got = _query(case, psi, ntot)
+    np.testing.assert_allclose(got, case["expect"], atol=max(case["atol"], 1e-12))
+
+
+@pytest.mark.parametrize("case", K.GATE_KATS, ids=[c["id"] for c in K.GATE_KATS])
+def test_oracle_matches_reference_gate_kat(case):
     psi, ntot = _oracle_state(case)
     got = _query(case, psi, ntot)
     np.testing.assert_allclose(got, case["expect"], atol=max(case["atol"], 1e-12))
