@@ -103,6 +103,21 @@ KATS = [
          ops=[("h", (0,), {}), ("rx", (1,), {"theta": 0.7}),
               ("exp1", (0, 1), {"unitary": np.diag([1.0, -1.0, -1.0, 1.0]), "theta": -0.2})] * 2,
          query=("expect_ops", [("z", [1])]), expect=0.202728, atol=1e-5),
+    # tests/test_templates.py:17-26 -- any_measurements (codes 1 = X, 3 = Z, 0 = I) after H on both
+    dict(id="anymeas_xx", src="tests/test_templates.py:17-23", n=2, ops=[("h", (0,), {}), ("h", (1,), {})],
+         query=("ps", dict(x=[0, 1])), expect=1.0, atol=1e-5),
+    dict(id="anymeas_z0", src="tests/test_templates.py:24-26", n=2, ops=[("h", (0,), {}), ("h", (1,), {})],
+         query=("ps", dict(z=[0])), expect=0.0, atol=1e-5),
+    # tests/test_templates.py:30-39 -- local measurements in bases Z, Z, X
+    dict(id="localmeas_z0", src="tests/test_templates.py:30-39", n=3,
+         ops=[("x", (0,), {}), ("cnot", (0, 1), {}), ("h", (-1,), {})],
+         query=("ps", dict(z=[0])), expect=-1.0, atol=1e-5),
+    dict(id="localmeas_z1", src="tests/test_templates.py:30-39", n=3,
+         ops=[("x", (0,), {}), ("cnot", (0, 1), {}), ("h", (-1,), {})],
+         query=("ps", dict(z=[1])), expect=-1.0, atol=1e-5),
+    dict(id="localmeas_x2", src="tests/test_templates.py:30-39", n=3,
+         ops=[("x", (0,), {}), ("cnot", (0, 1), {}), ("h", (-1,), {})],
+         query=("ps", dict(x=[2])), expect=1.0, atol=1e-5),
 ]
 
 # Gate conventions from the reference's gate tests (tests/test_gates.py).
