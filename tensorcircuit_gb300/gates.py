@@ -20,7 +20,6 @@ keeps them differentiable: the engine's adjoint kernel returns the cotangent
 of each matrix entry and torch maps it back to the parameters.
 """
 
-from functools import reduce
 from operator import mul
 from typing import Any, Callable, Dict, List, Optional, Sequence, Tuple
 

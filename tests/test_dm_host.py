@@ -4,7 +4,6 @@ recording, the trace gather's indices and phases) and of the qir tools
 (from_qir, inverse, append, prepend) checked without a GPU."""
 
 import numpy as np
-import pytest
 import torch
 
 from oracle import densitymatrix as dmo

@@ -9,8 +9,6 @@ tcgen05, fp16 hi/lo operands, fp32 accumulation).
 * the bounded-wait flag stays clear.
 """
 
-import ctypes
-
 import numpy as np
 import pytest
 import torch

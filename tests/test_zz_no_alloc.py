@@ -9,8 +9,6 @@ requests must be refused.  (This file sorts last so that a run stopping at
 its first failure has run every other test first.)
 """
 
-import ctypes
-
 import numpy as np
 import pytest
 import torch
